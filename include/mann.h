@@ -1,0 +1,110 @@
+/*
+ * mann.h -- C ABI of libmanngpu.so, the GB300 (sm_103a) implementation of
+ * ManifoldANN's exact-kNN / kNN-graph / KMeans-assignment hot path.
+ *
+ * Layout: a Julia Matrix{Float32} of size d x n (column-major, one point per
+ * column) is, byte for byte, a row-major [n][d] array; pass pointer(data).
+ * Ids are 0-based int32 (a Julia shim adds 1).  Outputs are caller-allocated
+ * [q][k] arrays.  Every entry point returns a mann_status; MANN_OK is 0 and
+ * mann_last_error() gives the calling thread's last message.
+ *
+ * Entry points with host pointers copy inputs to the GPU and results back on
+ * every call (the reference passes `data` on every query,
+ * src/ann_index.jl:1-10).  The *_device variants take device pointers on the
+ * current device and a cudaStream_t (NULL = the legacy default stream); they
+ * return once the work is enqueued, results are valid after the stream
+ * synchronises.
+ *
+ * All entry points are thread-safe; calls on one device are serialised
+ * internally (the reference's re-entrancy contract, src/ann_index.jl:60-66).
+ */
+#ifndef MANN_H
+#define MANN_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t mann_status;
+#define MANN_OK 0
+#define MANN_EINVAL_DIM 1 /* Julia: DimensionMismatch (src/utils/validation.jl:8-12) */
+#define MANN_EINVAL_ARG 2 /* Julia: ArgumentError (validation.jl:13-17, knn_graph.jl:55-59) */
+#define MANN_ENOMEM 3
+#define MANN_ECUDA 4
+#define MANN_ETIMEOUT 5 /* a bounded device-side wait ran out; the context stays usable */
+#define MANN_ENODEV 6
+
+/* Distances.jl metrics aliased in src/utils/distances.jl:15-18 */
+#define MANN_METRIC_EUCLIDEAN 0   /* Euclidean()   sqrt(sum((x-y)^2)) -- the reference default */
+#define MANN_METRIC_SQEUCLIDEAN 1 /* SqEuclidean() sum((x-y)^2) */
+#define MANN_METRIC_COSINE 2      /* CosineDist()  max(1 - x.y/(|x||y|), 0) */
+
+/* Arithmetic forms of the exact search */
+#define MANN_PREC_FP32 0 /* FP32 difference-form tiles + fused top-k (reference semantics) */
+#define MANN_PREC_BF16 1 /* BF16 tcgen05 tiles, certified top-(k+m), exact FP32 rerank */
+#define MANN_PREC_AUTO 3 /* library picks (BF16 form when d >= 128 and the metric is L2) */
+
+/* Flags */
+#define MANN_FLAG_FP64_TIES 1u /* order near-ties at the k-th boundary by FP64 distances */
+
+typedef struct {
+  int32_t metric;    /* MANN_METRIC_* */
+  int32_t k;         /* neighbours per query; k <= 0 writes nothing (bruteforce.jl:55-56) */
+  int32_t precision; /* MANN_PREC_* */
+  int32_t margin;    /* extra candidates kept by reduced-precision forms; 0 = autotuned */
+  uint32_t flags;    /* MANN_FLAG_* */
+  int32_t reserved[3];
+} mann_knn_params;
+
+/* Optional per-call report (pass NULL to skip). */
+typedef struct {
+  int64_t rows;              /* query rows processed */
+  int64_t rows_fallback;     /* rows whose reduced-precision candidate set could not be
+                                certified and that were re-run by the exact FP32 scan */
+  int64_t rows_fp64_ties;    /* rows where an FP64 recompute ordered a near-tie */
+  int64_t candidates;        /* candidates reranked in exact FP32 */
+  double max_abs_err_fp64;   /* filled when reserved for future use: -1 */
+  int32_t precision_used;    /* MANN_PREC_* actually run */
+  int32_t margin_used;
+} mann_knn_report;
+
+const char* mann_version(void);
+/* Message for the calling thread's last non-OK status ("" if none). */
+const char* mann_last_error(void);
+mann_status mann_device_count(int32_t* out_count);
+
+/* Page-lock (pin) a caller buffer so host<->device copies run at full speed
+ * (Julia: call once on a long-lived Matrix). */
+mann_status mann_host_register(void* ptr, int64_t bytes);
+mann_status mann_host_unregister(void* ptr);
+
+/* Exact kNN of q queries against n points (d dims each).
+ * Replaces query(::BruteForceIndex, data, Q::AbstractMatrix, k)
+ * (src/ann_index.jl:71-101 looping src/indices/bruteforce.jl:46-71).
+ * out_ids/out_dists: [q][k]; columns >= min(k, n) are written as -1 / +inf.
+ * Order: ascending (distance, id) -- partialsortperm, bruteforce.jl:65. */
+mann_status mann_knn(const mann_knn_params* p, const float* base, int64_t n,
+                     const float* queries, int64_t q, int32_t d, int32_t* out_ids,
+                     float* out_dists, mann_knn_report* report);
+mann_status mann_knn_device(const mann_knn_params* p, const float* base, int64_t n,
+                            const float* queries, int64_t q, int32_t d, int32_t* out_ids,
+                            float* out_dists, mann_knn_report* report, void* stream);
+
+/* kNN graph of n points against themselves.
+ * Replaces the column loop of build_knn_graph (src/graphs/knn_graph.jl:42-81):
+ * each point queries k+1 neighbours (k when include_self), the point itself is
+ * dropped wherever it appears and the first k others are kept
+ * (_prepare_neighbors, knn_graph.jl:105-130).  MANN_EINVAL_ARG unless
+ * 0 < k <= n - (include_self ? 0 : 1).  out: [n][k]. */
+mann_status mann_knn_graph(const mann_knn_params* p, const float* data, int64_t n, int32_t d,
+                           int32_t include_self, int32_t* out_ids, float* out_dists,
+                           mann_knn_report* report);
+mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, int64_t n,
+                                  int32_t d, int32_t include_self, int32_t* out_ids,
+                                  float* out_dists, mann_knn_report* report, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,26 @@
+"""manifoldann_gb300 -- GB300 (sm_103a) implementation of ManifoldANN's exact
+kNN / kNN-graph / KMeans-assignment hot path.
+
+The compute lives in ``libmanngpu.so`` (C ABI: ``include/mann.h``); this
+package mirrors the reference's Julia API on top of it (names follow
+src/ManifoldANN.jl's exports; Julia's ``insert!``/``fit!`` are ``insert``/``fit``).
+"""
+from ._lib import ArgumentError, DimensionMismatch, MannError
+from .distances import (CosineDist, Euclidean, SqEuclidean, cosine_distance, default_distance,
+                        default_squared_distance, euclidean_distance)
+from .eval_utils import recall_at_k
+from .graphs import (KNNGraph, build_knn_graph, graph_metadata, has_metadata, knn_graph_arrays,
+                     node_metadata)
+from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
+                      index_distance, insert, knn_arrays, neighbor_ids, query, supports_mutation)
+
+__all__ = [
+    "ArgumentError", "DimensionMismatch", "MannError",
+    "CosineDist", "Euclidean", "SqEuclidean", "cosine_distance", "default_distance",
+    "default_squared_distance", "euclidean_distance",
+    "recall_at_k",
+    "KNNGraph", "build_knn_graph", "graph_metadata", "has_metadata", "knn_graph_arrays",
+    "node_metadata",
+    "AbstractANNIndex", "BruteForceIndex", "Neighbor", "build_index", "configured_k",
+    "index_distance", "insert", "knn_arrays", "neighbor_ids", "query", "supports_mutation",
+]

@@ -1,0 +1,195 @@
+// api.cu -- extern "C" entry points of libmanngpu (declared in include/mann.h).
+#include <string>
+
+#include "kernels.cuh"
+
+namespace mann {
+const char* last_error_cstr();
+
+namespace {
+
+bool valid_metric(int m) {
+  return m == MANN_METRIC_EUCLIDEAN || m == MANN_METRIC_SQEUCLIDEAN || m == MANN_METRIC_COSINE;
+}
+
+mann_status check_common(const mann_knn_params* p, int64_t n, int32_t d) {
+  if (!p) return fail(MANN_EINVAL_ARG, "params must not be NULL");
+  if (d <= 0) return fail(MANN_EINVAL_ARG, "Dataset must have at least one dimension");
+  if (n <= 0) return fail(MANN_EINVAL_ARG, "Dataset must contain at least one point");
+  if (n > 0x7FFFFFFFll) return fail(MANN_EINVAL_ARG, "at most 2^31-1 points (int32 ids)");
+  if (!valid_metric(p->metric)) return fail(MANN_EINVAL_ARG, "unknown metric code");
+  if (p->precision != MANN_PREC_FP32 && p->precision != MANN_PREC_BF16 &&
+      p->precision != MANN_PREC_AUTO)
+    return fail(MANN_EINVAL_ARG, "unknown precision code");
+  return MANN_OK;
+}
+
+// One exact search on device buffers.  graph_self >= 0: the queries are the
+// points themselves (row r is point r) and `kreq` = k+1 lists drop the self id.
+mann_status search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p,
+                          const float* base, int64_t n, const float* qs, int64_t nq, int d,
+                          int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
+                          mann_knn_report* rep) {
+  if (rep) {
+    *rep = mann_knn_report{};
+    rep->rows = nq;
+    rep->max_abs_err_fp64 = -1.0;
+    rep->precision_used = MANN_PREC_FP32;
+  }
+  if (nq <= 0 || kout <= 0) return MANN_OK;
+  if (kreq > KMAX_FUSED)
+    return fail(MANN_EINVAL_ARG, "k = " + std::to_string(kreq) + " exceeds the fused top-k limit " +
+                                     std::to_string(KMAX_FUSED));
+  const float* qn = nullptr;
+  const float* bn = nullptr;
+  if (p->metric == MANN_METRIC_COSINE) {
+    float *db = nullptr, *dq = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &db));
+    MANN_TRY(launch_row_sqnorm(base, n, d, db, s));
+    bn = db;
+    if (qs == base) {
+      qn = db;
+    } else {
+      MANN_TRY(ctx->scratch_t(SLOT_NORMS_Q, (size_t)nq, &dq));
+      MANN_TRY(launch_row_sqnorm(qs, nq, d, dq, s));
+      qn = dq;
+    }
+  }
+  uint64_t* keys = nullptr;
+  MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, nullptr, qn, bn, &keys,
+                         SLOT_PARTIAL, SLOT_KEYS));
+  MANN_TRY(launch_finish(keys, nq, kreq, kout, graph_self, nullptr, ids, dists, s));
+  return MANN_OK;
+}
+
+mann_status knn_impl(const mann_knn_params* p, const float* base, int64_t n, const float* qs,
+                     int64_t q, int32_t d, int32_t* ids, float* dists, mann_knn_report* rep,
+                     bool host, cudaStream_t user_stream) {
+  clear_error();
+  MANN_TRY(check_common(p, n, d));
+  if (q < 0) return fail(MANN_EINVAL_ARG, "negative query count");
+  if (rep) *rep = mann_knn_report{};
+  if (p->k <= 0 || q == 0) return MANN_OK;
+  if (!base || !qs || !ids || !dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  const int kout = p->k;
+  const int kreq = (int)std::min<int64_t>(p->k, n);
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = host ? ctx->stream : user_stream;
+  CallScope scope(ctx, s);
+  if (!host) return search_device(ctx, s, p, base, n, qs, q, d, -1, kreq, kout, ids, dists, rep);
+
+  float *db = nullptr, *dq = nullptr, *dd = nullptr;
+  int32_t* di = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_BASE, (size_t)n * d, &db));
+  MANN_TRY(ctx->scratch_t(SLOT_QUERIES, (size_t)q * d, &dq));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_IDS, (size_t)q * kout, &di));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_DISTS, (size_t)q * kout, &dd));
+  MANN_CUDA_TRY(cudaMemcpyAsync(db, base, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dq, qs, sizeof(float) * q * d, cudaMemcpyHostToDevice, s));
+  MANN_TRY(search_device(ctx, s, p, db, n, dq, q, d, -1, kreq, kout, di, dd, rep));
+  MANN_CUDA_TRY(cudaMemcpyAsync(ids, di, sizeof(int32_t) * q * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dists, dd, sizeof(float) * q * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  return MANN_OK;
+}
+
+mann_status graph_impl(const mann_knn_params* p, const float* data, int64_t n, int32_t d,
+                       int32_t include_self, int32_t* ids, float* dists, mann_knn_report* rep,
+                       bool host, cudaStream_t user_stream) {
+  clear_error();
+  MANN_TRY(check_common(p, n, d));
+  if (rep) *rep = mann_knn_report{};
+  const int64_t max_neighbors = n - (include_self ? 0 : 1);
+  if (!(p->k > 0 && p->k <= max_neighbors))
+    return fail(MANN_EINVAL_ARG, "k must satisfy 0 < k <= " + std::to_string(max_neighbors) +
+                                     " for dataset with " + std::to_string(n) + " points");
+  if (!data || !ids || !dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  const int kout = p->k;
+  const int kreq = p->k + (include_self ? 0 : 1);
+  const int64_t self = include_self ? -1 : 0;
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = host ? ctx->stream : user_stream;
+  CallScope scope(ctx, s);
+  if (!host) return search_device(ctx, s, p, data, n, data, n, d, self, kreq, kout, ids, dists, rep);
+
+  float *db = nullptr, *dd = nullptr;
+  int32_t* di = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_BASE, (size_t)n * d, &db));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_IDS, (size_t)n * kout, &di));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_DISTS, (size_t)n * kout, &dd));
+  MANN_CUDA_TRY(cudaMemcpyAsync(db, data, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+  MANN_TRY(search_device(ctx, s, p, db, n, db, n, d, self, kreq, kout, di, dd, rep));
+  MANN_CUDA_TRY(cudaMemcpyAsync(ids, di, sizeof(int32_t) * n * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dists, dd, sizeof(float) * n * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  return MANN_OK;
+}
+
+}  // namespace
+}  // namespace mann
+
+using namespace mann;
+
+extern "C" {
+
+const char* mann_version(void) { return "manifoldann-gb300 0.1.0 (sm_103a)"; }
+
+const char* mann_last_error(void) { return last_error_cstr(); }
+
+mann_status mann_device_count(int32_t* out_count) {
+  clear_error();
+  if (!out_count) return fail(MANN_EINVAL_ARG, "out_count must not be NULL");
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    *out_count = 0;
+    return MANN_OK;
+  }
+  *out_count = c;
+  return MANN_OK;
+}
+
+mann_status mann_host_register(void* ptr, int64_t bytes) {
+  clear_error();
+  if (!ptr || bytes <= 0) return fail(MANN_EINVAL_ARG, "bad buffer");
+  MANN_CUDA_TRY(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+  return MANN_OK;
+}
+
+mann_status mann_host_unregister(void* ptr) {
+  clear_error();
+  if (!ptr) return fail(MANN_EINVAL_ARG, "bad buffer");
+  MANN_CUDA_TRY(cudaHostUnregister(ptr));
+  return MANN_OK;
+}
+
+mann_status mann_knn(const mann_knn_params* p, const float* base, int64_t n, const float* queries,
+                     int64_t q, int32_t d, int32_t* out_ids, float* out_dists,
+                     mann_knn_report* report) {
+  return knn_impl(p, base, n, queries, q, d, out_ids, out_dists, report, true, nullptr);
+}
+
+mann_status mann_knn_device(const mann_knn_params* p, const float* base, int64_t n,
+                            const float* queries, int64_t q, int32_t d, int32_t* out_ids,
+                            float* out_dists, mann_knn_report* report, void* stream) {
+  return knn_impl(p, base, n, queries, q, d, out_ids, out_dists, report, false,
+                  static_cast<cudaStream_t>(stream));
+}
+
+mann_status mann_knn_graph(const mann_knn_params* p, const float* data, int64_t n, int32_t d,
+                           int32_t include_self, int32_t* out_ids, float* out_dists,
+                           mann_knn_report* report) {
+  return graph_impl(p, data, n, d, include_self, out_ids, out_dists, report, true, nullptr);
+}
+
+mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, int64_t n,
+                                  int32_t d, int32_t include_self, int32_t* out_ids,
+                                  float* out_dists, mann_knn_report* report, void* stream) {
+  return graph_impl(p, data, n, d, include_self, out_ids, out_dists, report, false,
+                    static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

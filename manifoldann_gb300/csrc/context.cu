@@ -1,0 +1,80 @@
+// context.cu -- error reporting and per-device contexts.
+#include <memory>
+
+#include "context.cuh"
+
+namespace mann {
+
+namespace {
+thread_local std::string g_last_error;
+std::mutex g_ctx_mu;
+std::unique_ptr<Context> g_ctx[64];
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+mann_status Context::scratch(int slot, size_t bytes, void** out) {
+  if (bytes == 0) bytes = 256;
+  if (slot_bytes[slot] < bytes) {
+    if (slot_ptr[slot]) {
+      MANN_CUDA_TRY(cudaFree(slot_ptr[slot]));
+      slot_ptr[slot] = nullptr;
+      slot_bytes[slot] = 0;
+    }
+    // round up to 2 MiB to limit regrowth
+    const size_t want = (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return fail(MANN_ENOMEM, "cudaMalloc of " + std::to_string(want) + " bytes failed (" +
+                                   cudaGetErrorString(e) + ")");
+    }
+    slot_ptr[slot] = p;
+    slot_bytes[slot] = want;
+  }
+  *out = slot_ptr[slot];
+  return MANN_OK;
+}
+
+mann_status get_context(Context** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(MANN_ENODEV, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  if (dev < 0 || dev >= 64) return fail(MANN_ENODEV, "device ordinal out of range");
+  std::lock_guard<std::mutex> g(g_ctx_mu);
+  if (!g_ctx[dev]) {
+    std::unique_ptr<Context> c(new Context());
+    c->device = dev;
+    cudaDeviceProp prop;
+    MANN_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    c->num_sms = prop.multiProcessorCount;
+    c->cc_major = prop.major;
+    c->cc_minor = prop.minor;
+    c->smem_optin = prop.sharedMemPerBlockOptin;
+    if (c->cc_major != 10)
+      return fail(MANN_ENODEV, "libmanngpu is built for sm_103a (GB300); device " +
+                                   std::to_string(dev) + " is sm_" + std::to_string(prop.major) +
+                                   std::to_string(prop.minor));
+    MANN_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    MANN_CUDA_TRY(cudaEventCreateWithFlags(&c->last_use, cudaEventDisableTiming));
+    g_ctx[dev] = std::move(c);
+  }
+  *out = g_ctx[dev].get();
+  return MANN_OK;
+}
+
+CallScope::CallScope(Context* ctx, cudaStream_t s) : ctx_(ctx), s_(s), lock_(ctx->mu) {
+  // scratch written by the previous call (possibly on another stream) must be
+  // free before this call's kernels touch it
+  cudaStreamWaitEvent(s_, ctx_->last_use, 0);
+}
+
+CallScope::~CallScope() { cudaEventRecord(ctx_->last_use, s_); }
+
+}  // namespace mann

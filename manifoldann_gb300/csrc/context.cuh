@@ -1,0 +1,82 @@
+// context.cuh -- per-device state of libmanngpu: stream, grow-only scratch
+// buffers, device properties and the autotune cache.
+#pragma once
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+
+namespace mann {
+
+// Named scratch slots.  Each slot is one grow-only device allocation that is
+// reused by every call on the device; calls are serialised by Context::mu and
+// ordered on the GPU through Context::last_use.
+enum ScratchSlot : int {
+  SLOT_BASE = 0,      // host-pointer calls: device copy of the points
+  SLOT_QUERIES,       // host-pointer calls: device copy of the queries
+  SLOT_OUT_IDS,       // host-pointer calls: device ids
+  SLOT_OUT_DISTS,     // host-pointer calls: device distances
+  SLOT_PARTIAL,       // per-split top-k lists (uint64 keys)
+  SLOT_KEYS,          // merged top-k lists (uint64 keys)
+  SLOT_NORMS_Q,       // per-row squared norms of the queries
+  SLOT_NORMS_B,       // per-row squared norms of the points
+  SLOT_BF16_Q,        // BF16 copy of the (centred) queries
+  SLOT_BF16_B,        // BF16 copy of the (centred) points
+  SLOT_ROWINFO_Q,     // per-row bound terms of the queries
+  SLOT_ROWINFO_B,     // per-row bound terms of the points
+  SLOT_CENTRE,        // per-dimension centre (float) + reduction partials
+  SLOT_CAND,          // candidate lists of the reduced-precision forms
+  SLOT_FALLBACK,      // rows that need the exact FP32 scan
+  SLOT_FALLBACK_KEYS, // their FP32 top-k lists
+  SLOT_COUNTERS,      // small counters (report, status words)
+  SLOT_MISC0,
+  SLOT_MISC1,
+  SLOT_MISC2,
+  SLOT_MISC3,
+  SLOT_COUNT
+};
+
+struct Context {
+  int device = 0;
+  int num_sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+  std::mutex mu;
+  cudaStream_t stream = nullptr;   // used by the host-pointer entry points
+  cudaEvent_t last_use = nullptr;  // recorded after every call that used scratch
+  void* slot_ptr[SLOT_COUNT] = {};
+  size_t slot_bytes[SLOT_COUNT] = {};
+  // autotune cache: shape class -> chosen configuration word
+  std::unordered_map<uint64_t, uint64_t> tune;
+
+  // Device buffer of at least `bytes` for `slot`.  Grows by reallocation
+  // (cudaFree synchronises the device, so no kernel still uses the old one).
+  mann_status scratch(int slot, size_t bytes, void** out);
+  template <typename T>
+  mann_status scratch_t(int slot, size_t count, T** out) {
+    void* p = nullptr;
+    mann_status s = scratch(slot, count * sizeof(T), &p);
+    *out = static_cast<T*>(p);
+    return s;
+  }
+};
+
+// The context of the current device (created on first use).
+mann_status get_context(Context** out);
+
+// Scope guard for one entry-point call: locks the context, orders the call's
+// stream after the previous call's use of scratch, and records the new use.
+class CallScope {
+ public:
+  CallScope(Context* ctx, cudaStream_t s);
+  ~CallScope();
+  cudaStream_t stream() const { return s_; }
+
+ private:
+  Context* ctx_;
+  cudaStream_t s_;
+  std::unique_lock<std::mutex> lock_;
+};
+
+}  // namespace mann

@@ -1,0 +1,33 @@
+// kernels.cuh -- internal launchers shared by the entry points.
+#pragma once
+#include "context.cuh"
+
+namespace mann {
+
+// Squared norms of n rows of d floats (sequential fused multiply-add over the
+// dimensions, the same order as every FP32 distance in this library).
+mann_status launch_row_sqnorm(const float* x, int64_t n, int d, float* out, cudaStream_t s);
+
+// Exact FP32 top-kk of every query (difference-form distances, fused top-k).
+// Result: sorted (distance, id) keys [nq][kk] in `out_keys` (device scratch
+// owned by the context, valid until the next call).  `rows` optionally maps
+// result row i to query row rows[i] (nq entries); NULL = identity.  Cosine
+// needs the squared row norms of the points (bn) and of the query matrix (qn,
+// indexed by query row).
+mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
+                          const float* qs, int64_t nq, int d, int metric, int kk,
+                          const int32_t* rows, const float* qn, const float* bn,
+                          uint64_t** out_keys, int slot_partial, int slot_keys);
+
+// Keys [nq][kk] -> ids/dists [*][kout].  Key row i goes to output row
+// rows[i] (identity when rows is NULL).  With graph_self >= 0 the query of
+// output row r is point (graph_self + r) and is dropped wherever it appears
+// (_prepare_neighbors, src/graphs/knn_graph.jl:105-130); entries without a key
+// become id -1 / +inf.
+mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, int64_t graph_self,
+                          const int32_t* rows, int32_t* ids, float* dists, cudaStream_t s);
+
+// Largest k handled by the fused top-k kernels.
+constexpr int KMAX_FUSED = 256;
+
+}  // namespace mann

@@ -1,0 +1,495 @@
+// knn_fp32.cu -- exact FP32 kNN with fused per-row top-k (the plain form).
+//
+// Replaces the per-query scan of src/indices/bruteforce.jl:59-65 (one
+// Distances.jl evaluation per point, then partialsortperm) and the batch loop
+// of src/ann_index.jl:91-98.  One CTA owns BQ queries and a contiguous split
+// of the points; it walks the split in tiles of 128 points, computes the
+// BQ x 128 distance tile in registers (difference form, one fused
+// multiply-add per dimension in order 0..d-1 -- bit-identical to the oracle's
+// sequential sum), stages it in shared memory and folds it into per-row
+// sorted top-k lists that live in the registers of the warp owning the row.
+// Splits are merged by a second kernel.  Order: (distance, id) as
+// partialsortperm (bruteforce.jl:65).
+#include <algorithm>
+
+#include "kernels.cuh"
+
+namespace mann {
+
+namespace {
+
+constexpr int K1_THREADS = 256;
+constexpr int K1_BN = 128;  // points per tile
+constexpr int K1_DK = 16;   // dimensions per shared-memory stage
+constexpr unsigned FULL = 0xFFFFFFFFu;
+
+__global__ void row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
+                                  float* __restrict__ out) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = x + i * (int64_t)d;
+  float s = 0.0f;
+  for (int j = 0; j < d; ++j) s = __fmaf_rn(r[j], r[j], s);
+  out[i] = s;
+}
+
+// ---- warp-distributed sorted list: entry e lives in slot e/32 of lane e%32
+template <int KW>
+__device__ __forceinline__ void list_insert(uint64_t (&L)[KW], uint64_t c, int lane) {
+  int pos = 0;
+#pragma unroll
+  for (int s = 0; s < KW; ++s) pos += __popc(__ballot_sync(FULL, L[s] < c));
+  uint64_t up[KW], last[KW];
+#pragma unroll
+  for (int s = 0; s < KW; ++s) {
+    up[s] = __shfl_up_sync(FULL, L[s], 1);
+    last[s] = __shfl_sync(FULL, L[s], 31);
+  }
+#pragma unroll
+  for (int s = 0; s < KW; ++s) {
+    const int e = s * 32 + lane;
+    uint64_t shifted = up[s];
+    if (lane == 0) shifted = (s == 0) ? KEY_NONE : last[s > 0 ? s - 1 : 0];
+    if (e > pos) L[s] = shifted;
+    else if (e == pos) L[s] = c;
+  }
+}
+
+template <int KW>
+__device__ __forceinline__ uint64_t list_get(const uint64_t (&L)[KW], int e) {
+  const int slot = e >> 5, ln = e & 31;
+  uint64_t v = L[0];
+#pragma unroll
+  for (int s = 1; s < KW; ++s)
+    if (slot == s) v = L[s];
+  return __shfl_sync(FULL, v, ln);
+}
+
+// Thread-tile row/column maps.  TQ rows per thread: 8 -> {ty*4+i, 64+ty*4+i},
+// 4 -> ty*4+i, 2 -> ty*2+i.  Eight columns per thread: {tx*4+j, 64+tx*4+j}.
+template <int TQ>
+__device__ __forceinline__ int tile_row(int ty, int i) {
+  if constexpr (TQ == 8) return (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+  else if constexpr (TQ == 4) return ty * 4 + i;
+  else return ty * 2 + i;
+}
+__device__ __forceinline__ int tile_col(int tx, int j) {
+  return (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
+}
+
+template <int TQ>
+__device__ __forceinline__ void load_q_frag(const float* p, int ty, float (&v)[TQ]) {
+  if constexpr (TQ == 8) {
+    float4 a = *reinterpret_cast<const float4*>(p + ty * 4);
+    float4 b = *reinterpret_cast<const float4*>(p + 64 + ty * 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else if constexpr (TQ == 4) {
+    float4 a = *reinterpret_cast<const float4*>(p + ty * 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  } else {
+    float2 a = *reinterpret_cast<const float2*>(p + ty * 2);
+    v[0] = a.x; v[1] = a.y;
+  }
+}
+
+__device__ __forceinline__ void load_b_frag(const float* p, int tx, float (&v)[8]) {
+  float4 a = *reinterpret_cast<const float4*>(p + tx * 4);
+  float4 b = *reinterpret_cast<const float4*>(p + 64 + tx * 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// Stage loader: rows [r0, r0+R) x dims [c0, c0+16) of a row-major [*][d]
+// matrix into registers (VEC: float4 per thread-slot, else scalars).
+template <int R, bool VEC>
+struct StageLoader {
+  static constexpr int NV = VEC ? (R * 4 + K1_THREADS - 1) / K1_THREADS
+                                : (R * 16 + K1_THREADS - 1) / K1_THREADS;
+  float4 v4[VEC ? NV : 1];
+  float v1[VEC ? 1 : NV];
+
+  __device__ __forceinline__ void load(const float* __restrict__ src, const int32_t* rows,
+                                       int64_t r0, int64_t rend, int d, int c0, int tid) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if constexpr (VEC) {
+        const int e = tid + i * K1_THREADS;
+        float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (e < R * 4) {
+          const int r = e >> 2, c = c0 + (e & 3) * 4;
+          const int64_t gr = r0 + r;
+          if (gr < rend && c < d) {
+            const int64_t row = rows ? (int64_t)rows[gr] : gr;
+            val = __ldg(reinterpret_cast<const float4*>(src + row * (int64_t)d + c));
+          }
+        }
+        v4[i] = val;
+      } else {
+        const int e = tid + i * K1_THREADS;
+        float val = 0.f;
+        if (e < R * 16) {
+          const int r = e >> 4, c = c0 + (e & 15);
+          const int64_t gr = r0 + r;
+          if (gr < rend && c < d) {
+            const int64_t row = rows ? (int64_t)rows[gr] : gr;
+            val = __ldg(src + row * (int64_t)d + c);
+          }
+        }
+        v1[i] = val;
+      }
+    }
+  }
+
+  // transpose into dst[dim][row] (row stride `str`)
+  __device__ __forceinline__ void store(float* dst, int str, int tid) const {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if constexpr (VEC) {
+        const int e = tid + i * K1_THREADS;
+        if (e < R * 4) {
+          const int r = e >> 2, c = (e & 3) * 4;
+          dst[(c + 0) * str + r] = v4[i].x;
+          dst[(c + 1) * str + r] = v4[i].y;
+          dst[(c + 2) * str + r] = v4[i].z;
+          dst[(c + 3) * str + r] = v4[i].w;
+        }
+      } else {
+        const int e = tid + i * K1_THREADS;
+        if (e < R * 16) dst[(e & 15) * str + (e >> 4)] = v1[i];
+      }
+    }
+  }
+};
+
+template <int METRIC, int BQ, int KW, bool VEC>
+__global__ void __launch_bounds__(K1_THREADS, 1)
+    k1_tile_topk(const float* __restrict__ base, int64_t n, const float* __restrict__ qs,
+                 const int32_t* __restrict__ qrows, int64_t nq, int d,
+                 const float* __restrict__ qnorm, const float* __restrict__ bnorm, int k,
+                 int64_t split_len, int nsplit, uint64_t* __restrict__ partial) {
+  constexpr int TQ = BQ / 16;
+  constexpr int TN = 8;
+  constexpr int RPW = BQ / 8;
+  constexpr int QSTR = BQ + 4;
+  constexpr int BSTR = K1_BN + 4;
+  extern __shared__ float4 k1_smem[];
+  float* Qs = reinterpret_cast<float*>(k1_smem);  // [2][DK][QSTR]
+  float* Bs = Qs + 2 * K1_DK * QSTR;               // [2][DK][BSTR]
+  float* Dt = Bs + 2 * K1_DK * BSTR;               // [BQ][BSTR]
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ty = tid >> 4, tx = tid & 15;
+  const int64_t q0 = (int64_t)blockIdx.x * BQ;
+  const int split = blockIdx.y;
+  const int64_t nb0 = (int64_t)split * split_len;
+  const int64_t nb1 = min(n, nb0 + split_len);
+  const int nchunks = (d + K1_DK - 1) / K1_DK;
+
+  uint64_t L[RPW][KW];
+#pragma unroll
+  for (int r = 0; r < RPW; ++r)
+#pragma unroll
+    for (int s = 0; s < KW; ++s) L[r][s] = KEY_NONE;
+
+  StageLoader<BQ, VEC> qload;
+  StageLoader<K1_BN, VEC> bload;
+
+  for (int64_t t0 = nb0; t0 < nb1; t0 += K1_BN) {
+    const int64_t tend = min(nb1, t0 + K1_BN);
+    float acc[TQ][TN];
+#pragma unroll
+    for (int i = 0; i < TQ; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = 0.0f;
+
+    qload.load(qs, qrows, q0, nq, d, 0, tid);
+    bload.load(base, nullptr, t0, tend, d, 0, tid);
+    qload.store(Qs, QSTR, tid);
+    bload.store(Bs, BSTR, tid);
+    __syncthreads();
+
+    for (int c = 0; c < nchunks; ++c) {
+      const int buf = c & 1;
+      const bool more = (c + 1) < nchunks;
+      if (more) {
+        qload.load(qs, qrows, q0, nq, d, (c + 1) * K1_DK, tid);
+        bload.load(base, nullptr, t0, tend, d, (c + 1) * K1_DK, tid);
+      }
+      const float* qsb = Qs + buf * K1_DK * QSTR;
+      const float* bsb = Bs + buf * K1_DK * BSTR;
+#pragma unroll
+      for (int kk = 0; kk < K1_DK; ++kk) {
+        float qv[TQ], bv[TN];
+        load_q_frag<TQ>(qsb + kk * QSTR, ty, qv);
+        load_b_frag(bsb + kk * BSTR, tx, bv);
+#pragma unroll
+        for (int i = 0; i < TQ; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) {
+            if constexpr (METRIC == MANN_METRIC_COSINE) {
+              acc[i][j] = __fmaf_rn(qv[i], bv[j], acc[i][j]);
+            } else {
+              const float t = __fsub_rn(qv[i], bv[j]);
+              acc[i][j] = __fmaf_rn(t, t, acc[i][j]);
+            }
+          }
+      }
+      if (more) {
+        qload.store(Qs + (buf ^ 1) * K1_DK * QSTR, QSTR, tid);
+        bload.store(Bs + (buf ^ 1) * K1_DK * BSTR, BSTR, tid);
+      }
+      __syncthreads();
+    }
+
+    // finish the metric and stage the tile
+#pragma unroll
+    for (int i = 0; i < TQ; ++i) {
+      const int r = tile_row<TQ>(ty, i);
+      float qn = 0.f;
+      if constexpr (METRIC == MANN_METRIC_COSINE) {
+        const int64_t gq = q0 + r;
+        qn = (gq < nq) ? qnorm[qrows ? qrows[gq] : gq] : 1.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        float v = acc[i][j];
+        if constexpr (METRIC == MANN_METRIC_EUCLIDEAN) {
+          v = __fsqrt_rn(v);
+        } else if constexpr (METRIC == MANN_METRIC_COSINE) {
+          const int64_t gb = t0 + tile_col(tx, j);
+          const float bn = (gb < tend) ? bnorm[gb] : 1.0f;
+          const float den = __fmul_rn(__fsqrt_rn(qn), __fsqrt_rn(bn));
+          v = __fsub_rn(1.0f, __fdiv_rn(v, den));
+          if (v < 0.0f) v = 0.0f;
+        }
+        acc[i][j] = v;
+      }
+      float* drow = Dt + r * BSTR;
+      *reinterpret_cast<float4*>(drow + tx * 4) =
+          make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+      *reinterpret_cast<float4*>(drow + 64 + tx * 4) =
+          make_float4(acc[i][4], acc[i][5], acc[i][6], acc[i][7]);
+    }
+    __syncthreads();
+
+    // fold the tile into the per-row lists (warp `warp` owns RPW rows)
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) {
+      const int row = warp * RPW + r;
+      const float* drow = Dt + row * BSTR;
+      uint64_t thr = list_get<KW>(L[r], k - 1);
+      uint64_t key[4];
+      unsigned pend = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int col = lane + 32 * j;
+        const int64_t gid = t0 + col;
+        key[j] = (gid < tend) ? make_key(drow[col], (uint32_t)gid) : KEY_NONE;
+        if (key[j] < thr) pend |= 1u << j;
+      }
+      for (;;) {
+        const unsigned any = __ballot_sync(FULL, pend != 0);
+        if (!any) break;
+        const int src = __ffs(any) - 1;
+        uint64_t mine = KEY_NONE;
+        if (pend) {
+          const int j = __ffs(pend) - 1;
+          mine = (j == 0) ? key[0] : (j == 1) ? key[1] : (j == 2) ? key[2] : key[3];
+        }
+        const uint64_t cnd = __shfl_sync(FULL, mine, src);
+        if (lane == src) pend &= pend - 1;
+        if (cnd < thr) {
+          list_insert<KW>(L[r], cnd, lane);
+          thr = list_get<KW>(L[r], k - 1);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (!(key[j] < thr)) pend &= ~(1u << j);
+      }
+    }
+    __syncthreads();
+  }
+
+  // write this split's lists
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) {
+    const int64_t gq = q0 + warp * RPW + r;
+    if (gq >= nq) continue;
+    uint64_t* dst = partial + (gq * nsplit + split) * (int64_t)k;
+#pragma unroll
+    for (int s = 0; s < KW; ++s) {
+      const int e = s * 32 + lane;
+      if (e < k) dst[e] = L[r][s];
+    }
+  }
+}
+
+// Merge nsplit sorted lists of k keys per query into one sorted list of k.
+// One warp per query; lane s walks list s (and s+32, ...).
+__global__ void merge_lists_kernel(const uint64_t* __restrict__ partial, int64_t nq, int nsplit,
+                                   int k, uint64_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (q >= nq) return;
+  const uint64_t* src = partial + q * (int64_t)nsplit * k;
+  constexpr int MAXL = 4;  // lists per lane (nsplit <= 128)
+  int head[MAXL];
+  uint64_t cur[MAXL];
+#pragma unroll
+  for (int t = 0; t < MAXL; ++t) {
+    const int s = lane + 32 * t;
+    head[t] = 0;
+    cur[t] = (s < nsplit) ? src[(int64_t)s * k] : KEY_NONE;
+  }
+  for (int e = 0; e < k; ++e) {
+    uint64_t m = cur[0];
+#pragma unroll
+    for (int t = 1; t < MAXL; ++t) m = min(m, cur[t]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = min(m, (uint64_t)__shfl_xor_sync(FULL, m, o));
+    if (lane == 0) out[q * k + e] = m;
+    if (m == KEY_NONE) continue;
+#pragma unroll
+    for (int t = 0; t < MAXL; ++t) {
+      if (cur[t] == m) {  // keys are unique (ids differ), so exactly one owner
+        const int s = lane + 32 * t;
+        ++head[t];
+        cur[t] = head[t] < k ? src[(int64_t)s * k + head[t]] : KEY_NONE;
+      }
+    }
+  }
+}
+
+__global__ void finish_kernel(const uint64_t* __restrict__ keys, int64_t nq, int kk, int kout,
+                              int64_t graph_self, const int32_t* __restrict__ rows,
+                              int32_t* __restrict__ ids, float* __restrict__ dists) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const uint64_t* src = keys + q * (int64_t)kk;
+  const int64_t orow = rows ? (int64_t)rows[q] : q;  // output row (and query id)
+  int32_t* oid = ids + orow * kout;
+  float* odist = dists + orow * kout;
+  int m = 0;
+  for (int e = 0; e < kk && m < kout; ++e) {
+    const uint64_t key = src[e];
+    if (key == KEY_NONE) break;
+    if (graph_self >= 0 && (int64_t)key_id(key) == graph_self + orow) continue;
+    oid[m] = key_id(key);
+    odist[m] = key_dist(key);
+    ++m;
+  }
+  for (; m < kout; ++m) {
+    oid[m] = -1;
+    odist[m] = __int_as_float(0x7F800000);
+  }
+}
+
+template <int METRIC, int BQ, int KW, bool VEC>
+mann_status launch_k1(const float* base, int64_t n, const float* qs, const int32_t* rows,
+                      int64_t nq, int d, const float* qn, const float* bn, int k,
+                      int64_t split_len, int nsplit, uint64_t* partial, cudaStream_t s) {
+  constexpr int QSTR = BQ + 4, BSTR = K1_BN + 4;
+  const size_t smem = sizeof(float) * (2 * K1_DK * QSTR + 2 * K1_DK * BSTR + BQ * BSTR);
+  auto kern = k1_tile_topk<METRIC, BQ, KW, VEC>;
+  MANN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)ceil_div(nq, BQ), (unsigned)nsplit);
+  kern<<<grid, K1_THREADS, smem, s>>>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+                                      partial);
+  MANN_CUDA_TRY(cudaGetLastError());
+  return MANN_OK;
+}
+
+template <int METRIC, bool VEC>
+mann_status dispatch_k1(int k, const float* base, int64_t n, const float* qs, const int32_t* rows,
+                        int64_t nq, int d, const float* qn, const float* bn, int64_t split_len,
+                        int nsplit, uint64_t* partial, cudaStream_t s) {
+  if (k <= 32)
+    return launch_k1<METRIC, 128, 1, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+                                          partial, s);
+  if (k <= 64)
+    return launch_k1<METRIC, 128, 2, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+                                          partial, s);
+  if (k <= 128)
+    return launch_k1<METRIC, 64, 4, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+                                         partial, s);
+  return launch_k1<METRIC, 32, 8, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+                                       partial, s);
+}
+
+}  // namespace
+
+mann_status launch_row_sqnorm(const float* x, int64_t n, int d, float* out, cudaStream_t s) {
+  if (n <= 0) return MANN_OK;
+  row_sqnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, d, out);
+  MANN_CUDA_TRY(cudaGetLastError());
+  return MANN_OK;
+}
+
+mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, int64_t graph_self,
+                          const int32_t* rows, int32_t* ids, float* dists, cudaStream_t s) {
+  if (nq <= 0 || kout <= 0) return MANN_OK;
+  finish_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(keys, nq, kk, kout, graph_self, rows,
+                                                           ids, dists);
+  MANN_CUDA_TRY(cudaGetLastError());
+  return MANN_OK;
+}
+
+mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
+                          const float* qs, int64_t nq, int d, int metric, int kk,
+                          const int32_t* rows, const float* qn, const float* bn,
+                          uint64_t** out_keys, int slot_partial, int slot_keys) {
+  if (kk < 1 || kk > KMAX_FUSED)
+    return fail(MANN_EINVAL_ARG, "fused top-k supports 1 <= k <= " + std::to_string(KMAX_FUSED));
+  if (nq <= 0) return MANN_OK;
+  if (metric == MANN_METRIC_COSINE && (qn == nullptr || bn == nullptr))
+    return fail(MANN_EINVAL_ARG, "cosine search needs row norms");
+  const int bq = kk <= 64 ? 128 : (kk <= 128 ? 64 : 32);
+  const int64_t qblocks = ceil_div(nq, bq);
+  const int64_t tiles = ceil_div(n, K1_BN);
+  // Split the points so that the grid covers the SMs at least once.
+  int64_t want = std::max<int64_t>(1, ceil_div(ctx->num_sms, qblocks));
+  want = std::min<int64_t>(want, std::min<int64_t>(tiles, 128));
+  const int64_t tiles_per = ceil_div(tiles, want);
+  const int nsplit = (int)ceil_div(tiles, tiles_per);
+  const int64_t split_len = tiles_per * K1_BN;
+
+  uint64_t* partial = nullptr;
+  MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * nsplit * kk, &partial));
+  const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0) &&
+                   ((reinterpret_cast<uintptr_t>(qs) & 15) == 0);
+  mann_status st;
+  switch (metric) {
+    case MANN_METRIC_EUCLIDEAN:
+      st = vec ? dispatch_k1<MANN_METRIC_EUCLIDEAN, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+                                                          split_len, nsplit, partial, s)
+               : dispatch_k1<MANN_METRIC_EUCLIDEAN, false>(kk, base, n, qs, rows, nq, d, qn, bn,
+                                                           split_len, nsplit, partial, s);
+      break;
+    case MANN_METRIC_SQEUCLIDEAN:
+      st = vec ? dispatch_k1<MANN_METRIC_SQEUCLIDEAN, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+                                                            split_len, nsplit, partial, s)
+               : dispatch_k1<MANN_METRIC_SQEUCLIDEAN, false>(kk, base, n, qs, rows, nq, d, qn,
+                                                             bn, split_len, nsplit, partial, s);
+      break;
+    default:
+      st = vec ? dispatch_k1<MANN_METRIC_COSINE, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+                                                       split_len, nsplit, partial, s)
+               : dispatch_k1<MANN_METRIC_COSINE, false>(kk, base, n, qs, rows, nq, d, qn, bn,
+                                                        split_len, nsplit, partial, s);
+      break;
+  }
+  MANN_TRY(st);
+  if (nsplit == 1) {
+    *out_keys = partial;
+    return MANN_OK;
+  }
+  uint64_t* keys = nullptr;
+  MANN_TRY(ctx->scratch_t(slot_keys, (size_t)nq * kk, &keys));
+  merge_lists_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, nsplit, kk, keys);
+  MANN_CUDA_TRY(cudaGetLastError());
+  *out_keys = keys;
+  return MANN_OK;
+}
+
+}  // namespace mann
