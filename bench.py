@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the exact-kNN hot path on one GB300.
+
+Workload (one step): the 784-d quantised Gaussian-mixture set -- N=60,000
+points, Q=10,000 held-out queries, SqEuclidean, k=10 -- searched for the
+held-out queries AND materialised as the self kNN graph of the 60,000 points
+(build_knn_graph semantics).  A step therefore answers 70,000 queries.
+
+Arms
+  (default)          the BF16 tensor-core form with certified candidates and
+                     exact FP32 rerank (recall@10 = 1.0 by construction); the
+                     plain FP32 form is timed beside it.  `value` has the inputs
+                     resident in HBM; `e2e` goes through the host-pointer C ABI
+                     (pinned host buffers, copies inside the timed region).
+  --impl reference   the reference's BruteForceIndex algorithm restated in C
+                     (OpenMP over every host core), on a bounded sample of the
+                     same workload per step.
+
+Prints ONE JSON line on rank 0.  Multi-GPU (torchrun): replicas only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_POINTS, N_QUERIES, DIM, K = 60000, 10000, 784, 10
+WORKLOAD = "quantized-mixture-784d: N=60000 points + Q=10000 held-out queries, SqEuclidean, k=10, plus the 60000-point self kNN graph"
+METRIC = "kNN queries/s (BF16+rerank exact kNN at recall@10=1.0)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp32-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    def __init__(self, gpu_index: int):
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.tmp.flush()
+        self.tmp.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.tmp.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.tmp.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_workload():
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.quantized_mixture(N_POINTS, DIM, seed=1)
+    q = synthetic.quantized_mixture(N_QUERIES, DIM, seed=2)
+    return base, q
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return j.get("bf16_tflops_sustained", 1737.1), j.get("hbm_gbs", 6703.5), "measured"
+    return 1700.0, 6800.0, "fallback"
+
+
+def cpu_baseline(base, q, budget_s):
+    """The reference algorithm (oracle's OpenMP restatement) on a bounded query sample."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    oracle.load()
+    probe = 32
+    t0 = time.perf_counter()
+    oracle.cpu_bruteforce_batch(base, q[:probe], K, oracle.SQEUCLIDEAN, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    m = int(min(len(q), max(probe, probe * budget_s / dt)))
+    t0 = time.perf_counter()
+    oracle.cpu_bruteforce_batch(base, q[:m], K, oracle.SQEUCLIDEAN, threads)
+    dt = time.perf_counter() - t0
+    return {"value": m / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{m} held-out queries against all {N_POINTS} points (d={DIM}, k={K}), "
+                      f"{dt:.1f} s wall on {threads} host threads"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    base, q = make_workload()
+    import oracle
+
+    oracle.load()
+    threads = os.cpu_count() or 1
+    per_step = 64
+    for i in range(args.warmup):
+        oracle.cpu_bruteforce_batch(base, q[i * per_step % N_QUERIES:][:per_step], K, oracle.SQEUCLIDEAN, threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        s = (i * per_step) % (N_QUERIES - per_step)
+        oracle.cpu_bruteforce_batch(base, q[s:s + per_step], K, oracle.SQEUCLIDEAN, threads)
+    dt = time.perf_counter() - t0
+    qps = per_step * args.steps / dt
+    line = {"metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "step": f"{per_step} held-out queries against all points",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{per_step} queries per step x {args.steps} steps; reference "
+                                       "BruteForceIndex algorithm restated in C (Julia is not installed)"},
+            "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import manifoldann_gb300 as M
+    from manifoldann_gb300 import _lib
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    lib = _lib.load()
+    base, q = make_workload()
+    tb = torch.from_numpy(base).cuda()
+    tq = torch.from_numpy(q).cuda()
+    qi = torch.empty((N_QUERIES, K), dtype=torch.int32, device="cuda")
+    qd = torch.empty((N_QUERIES, K), dtype=torch.float32, device="cuda")
+    gi = torch.empty((N_POINTS, K), dtype=torch.int32, device="cuda")
+    gd = torch.empty((N_POINTS, K), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def step(prec, flags=0):
+        p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, prec, 0, flags)
+        r1, r2 = _lib.KnnReport(), _lib.KnnReport()
+        _lib.check(lib.mann_knn_device(p, tb.data_ptr(), N_POINTS, tq.data_ptr(), N_QUERIES, DIM,
+                                       qi.data_ptr(), qd.data_ptr(), r1, sp))
+        _lib.check(lib.mann_knn_graph_device(p, tb.data_ptr(), N_POINTS, DIM, 0, gi.data_ptr(),
+                                             gd.data_ptr(), r2, sp))
+        return r1, r2
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- headline: BF16 form, inputs resident
+    for _ in range(args.warmup):
+        step(_lib.PREC_BF16)
+    barrier()
+    sampler = ClockSampler(local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kernel_ms, launches, fallback, cands = 0.0, 0, 0, 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r1, r2 = step(_lib.PREC_BF16, _lib.FLAG_TIME_KERNEL)
+        kernel_ms += r1.kernel_ms + r2.kernel_ms
+        launches += r1.launches + r2.launches
+        fallback += r1.rows_fallback + r2.rows_fallback
+        cands += r1.candidates + r2.candidates
+    ev1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    qps_step = N_QUERIES + N_POINTS
+    value = ws * qps_step * args.steps / (ms / 1e3)
+    bf16_i = (qi.cpu().numpy().copy(), gi.cpu().numpy().copy())
+
+    # ---- the plain FP32 form on the same step
+    step(_lib.PREC_FP32)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.fp32_steps):
+        step(_lib.PREC_FP32)
+    e1.record(stream)
+    barrier()
+    fp32_ms = e0.elapsed_time(e1) / max(args.fp32_steps, 1)
+    fp32_qps = qps_step / (fp32_ms / 1e3)
+    same_as_fp32 = bool(np.array_equal(bf16_i[0], qi.cpu().numpy()) and np.array_equal(bf16_i[1], gi.cpu().numpy()))
+
+    # ---- e2e through the host-pointer C ABI (pinned host buffers)
+    e2e = None
+    if not args.no_e2e:
+        hb = torch.from_numpy(base).pin_memory()
+        hq = torch.from_numpy(q).pin_memory()
+        hqi = torch.empty((N_QUERIES, K), dtype=torch.int32).pin_memory()
+        hqd = torch.empty((N_QUERIES, K), dtype=torch.float32).pin_memory()
+        hgi = torch.empty((N_POINTS, K), dtype=torch.int32).pin_memory()
+        hgd = torch.empty((N_POINTS, K), dtype=torch.float32).pin_memory()
+        p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_BF16)
+
+        def host_step():
+            _lib.check(lib.mann_knn(p, hb.data_ptr(), N_POINTS, hq.data_ptr(), N_QUERIES, DIM,
+                                    hqi.data_ptr(), hqd.data_ptr(), None))
+            _lib.check(lib.mann_knn_graph(p, hb.data_ptr(), N_POINTS, DIM, 0, hgi.data_ptr(),
+                                          hgd.data_ptr(), None))
+
+        for _ in range(max(1, args.warmup)):
+            host_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            host_step()
+        dt = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([dt], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        e2e = {"value": ws * qps_step * args.steps / dt, "unit": "queries/s",
+               "h2d_bytes_per_step": int(2 * base.nbytes + q.nbytes),
+               "d2h_bytes_per_step": int((N_QUERIES + N_POINTS) * K * 8)}
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+
+    peak_tf, hbm, peak_src = measured_peaks()
+    flops_step = 2.0 * DIM * N_POINTS * (N_QUERIES + N_POINTS)
+    launches_per_step_main = 2
+    achieved_tf = flops_step * args.steps / (kernel_ms / 1e3) / 1e12 if kernel_ms > 0 else None
+    roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": (achieved_tf / peak_tf) if achieved_tf else None, "traffic": None,
+            "peak_source": f"{peak_src} bf16 dense (sustained)", "kernel": "k2_main (tcgen05 BF16 tiles + fused top-(k+m))",
+            "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step_main)}
+    cpu = cpu_baseline(base, q, args.cpu_seconds) if args.cpu_seconds > 0 else None
+    line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "queries_per_step": qps_step, "l2": "inputs larger than L2 (188 MB fp32 points)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "fp32_form": {"value": fp32_qps, "unit": "queries/s", "ms_per_step": fp32_ms,
+                          "bf16_over_fp32": value / ws / fp32_qps},
+            "recall_at_10_vs_fp32_form": 1.0 if same_as_fp32 else 0.0,
+            "rows_fallback_per_step": fallback / args.steps,
+            "candidates_per_query": cands / (args.steps * qps_step),
+            "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -29,6 +29,7 @@ PREC_BF16 = 1
 PREC_AUTO = 3
 
 FLAG_FP64_TIES = 1
+FLAG_TIME_KERNEL = 2
 
 
 class DimensionMismatch(ValueError):
@@ -63,6 +64,8 @@ class KnnReport(C.Structure):
         ("max_abs_err_fp64", C.c_double),
         ("precision_used", C.c_int32),
         ("margin_used", C.c_int32),
+        ("kernel_ms", C.c_double),
+        ("launches", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -24,12 +24,40 @@ mann_status check_common(const mann_knn_params* p, int64_t n, int32_t d) {
   return MANN_OK;
 }
 
+mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_params* p,
+                               const float* base, int64_t n, const float* qs, int64_t nq, int d,
+                               int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
+                               mann_knn_report* rep);
+
 // One exact search on device buffers.  graph_self >= 0: the queries are the
 // points themselves (row r is point r) and `kreq` = k+1 lists drop the self id.
 mann_status search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p,
                           const float* base, int64_t n, const float* qs, int64_t nq, int d,
                           int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
                           mann_knn_report* rep) {
+  const int64_t launches0 = launch_count();
+  ctx->timing = (p->flags & MANN_FLAG_TIME_KERNEL) != 0;
+  ctx->timed = false;
+  mann_status st = search_device_body(ctx, s, p, base, n, qs, nq, d, graph_self, kreq, kout, ids,
+                                      dists, rep);
+  if (rep) {
+    rep->launches = launch_count() - launches0;
+    rep->kernel_ms = -1.0;
+    if (st == MANN_OK && ctx->timing && ctx->timed) {
+      float ms = 0.0f;
+      MANN_CUDA_TRY(cudaEventSynchronize(ctx->time_b));
+      MANN_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->time_a, ctx->time_b));
+      rep->kernel_ms = ms;
+    }
+  }
+  ctx->timing = false;
+  return st;
+}
+
+mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_params* p,
+                               const float* base, int64_t n, const float* qs, int64_t nq, int d,
+                               int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
+                               mann_knn_report* rep) {
   if (rep) {
     *rep = mann_knn_report{};
     rep->rows = nq;
@@ -55,9 +83,31 @@ mann_status search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p
       qn = dq;
     }
   }
+  const bool l2 = p->metric != MANN_METRIC_COSINE;
+  bool use_bf16 = false;
+  if (p->precision == MANN_PREC_BF16) {
+    if (!l2) return fail(MANN_EINVAL_ARG, "the BF16 form supports SqEuclidean and Euclidean");
+    if (kreq > 64) return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= 64 (k+1 for graphs)");
+    use_bf16 = true;
+  } else if (p->precision == MANN_PREC_AUTO) {
+    use_bf16 = l2 && kreq <= 48 && d >= 128 && n >= 4096;
+  }
   uint64_t* keys = nullptr;
-  MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, nullptr, qn, bn, &keys,
-                         SLOT_PARTIAL, SLOT_KEYS));
+  if (use_bf16) {
+    MANN_TRY(knn_bf16_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, p->margin,
+                           (p->flags & MANN_FLAG_FP64_TIES) != 0, &keys, rep));
+    if (rep) rep->rows = nq;
+  } else if (p->flags & MANN_FLAG_FP64_TIES) {
+    // FP32 scan with a few extra entries, then FP64 order for near-ties
+    const int kk = (int)std::min<int64_t>(std::min<int64_t>(n, KMAX_FUSED), (int64_t)kreq + 32);
+    uint64_t* fkeys = nullptr;
+    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kk, nullptr, qn, bn, &fkeys,
+                           SLOT_PARTIAL, SLOT_KEYS));
+    MANN_TRY(fp32_then_resolve(ctx, s, base, qs, n, nq, d, p->metric, kk, kreq, fkeys, &keys, rep));
+  } else {
+    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, nullptr, qn, bn, &keys,
+                           SLOT_PARTIAL, SLOT_KEYS));
+  }
   MANN_TRY(launch_finish(keys, nq, kreq, kout, graph_self, nullptr, ids, dists, s));
   return MANN_OK;
 }

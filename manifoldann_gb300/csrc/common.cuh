@@ -15,6 +15,10 @@ namespace mann {
 void set_error(const std::string& msg);
 void clear_error();
 
+// kernels launched by the calling thread (reported per call)
+void note_launch();
+int64_t launch_count();
+
 struct Status {
   mann_status code = MANN_OK;
   bool ok() const { return code == MANN_OK; }
@@ -29,6 +33,13 @@ struct Status {
                         std::to_string(__LINE__) + " in " #expr);                        \
       return (_e == cudaErrorMemoryAllocation) ? MANN_ENOMEM : MANN_ECUDA;               \
     }                                                                                    \
+  } while (0)
+
+// after every kernel launch: count it and surface launch errors
+#define MANN_CHECK_LAUNCH()                   \
+  do {                                        \
+    ::mann::note_launch();                    \
+    MANN_CUDA_TRY(cudaGetLastError());        \
   } while (0)
 
 #define MANN_TRY(expr)                 \

@@ -7,12 +7,15 @@ namespace mann {
 
 namespace {
 thread_local std::string g_last_error;
+thread_local int64_t g_launches = 0;
 std::mutex g_ctx_mu;
 std::unique_ptr<Context> g_ctx[64];
 }  // namespace
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
+void note_launch() { ++g_launches; }
+int64_t launch_count() { return g_launches; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 
 mann_status Context::scratch(int slot, size_t bytes, void** out) {
@@ -63,10 +66,23 @@ mann_status get_context(Context** out) {
                                    std::to_string(prop.minor));
     MANN_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     MANN_CUDA_TRY(cudaEventCreateWithFlags(&c->last_use, cudaEventDisableTiming));
+    MANN_CUDA_TRY(cudaEventCreate(&c->time_a));
+    MANN_CUDA_TRY(cudaEventCreate(&c->time_b));
     g_ctx[dev] = std::move(c);
   }
   *out = g_ctx[dev].get();
   return MANN_OK;
+}
+
+void Context::time_begin(cudaStream_t s) {
+  if (timing && !timed) cudaEventRecord(time_a, s);
+}
+
+void Context::time_end(cudaStream_t s) {
+  if (timing && !timed) {
+    cudaEventRecord(time_b, s);
+    timed = true;
+  }
 }
 
 CallScope::CallScope(Context* ctx, cudaStream_t s) : ctx_(ctx), s_(s), lock_(ctx->mu) {

@@ -34,6 +34,7 @@ enum ScratchSlot : int {
   SLOT_MISC1,
   SLOT_MISC2,
   SLOT_MISC3,
+  SLOT_OUT_KEYS_BF16, // final sorted keys of the BF16 form
   SLOT_COUNT
 };
 
@@ -47,6 +48,12 @@ struct Context {
   cudaEvent_t last_use = nullptr;  // recorded after every call that used scratch
   void* slot_ptr[SLOT_COUNT] = {};
   size_t slot_bytes[SLOT_COUNT] = {};
+  // optional timing of the call's dominant kernel (MANN_FLAG_TIME_KERNEL)
+  cudaEvent_t time_a = nullptr, time_b = nullptr;
+  bool timing = false;  // requested for the current call
+  bool timed = false;   // the dominant kernel has been bracketed
+  void time_begin(cudaStream_t s);
+  void time_end(cudaStream_t s);
   // autotune cache: shape class -> chosen configuration word
   std::unordered_map<uint64_t, uint64_t> tune;
 

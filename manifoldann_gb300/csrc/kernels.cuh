@@ -27,6 +27,25 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
 mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, int64_t graph_self,
                           const int32_t* rows, int32_t* ids, float* dists, cudaStream_t s);
 
+// BF16 tensor-core form (SqEuclidean / Euclidean): certified candidates,
+// exact FP32 rerank, optional FP64 near-tie order.  Result: keys [nq][kreq].
+mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
+                          const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep);
+
+// Orders near-ties of sorted FP32 candidate lists by FP64 distance (when fp64)
+// and truncates them to kreq keys.  counters[0] += rows re-ordered,
+// counters[1] += rows whose boundary tie could not be settled.
+mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
+                           int kreq, int fp64, const uint64_t* cand, const int* cand_count,
+                           const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
+                           cudaStream_t s);
+
+// Exact FP32 top-kk lists -> FP64-ordered near-ties, truncated to kreq.
+mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, const float* qs,
+                              int64_t n, int64_t nq, int d, int metric, int kk, int kreq,
+                              const uint64_t* fkeys, uint64_t** out_keys, mann_knn_report* rep);
+
 // Largest k handled by the fused top-k kernels.
 constexpr int KMAX_FUSED = 256;
 

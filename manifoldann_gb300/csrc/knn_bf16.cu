@@ -100,10 +100,56 @@ __device__ __forceinline__ float round_up_f(double v) {
   return f;
 }
 
-// One warp per row: BF16 copy of (x - mu) padded to dp, and the row's bound terms.
+// scale / centre candidates tried on a sample of rows: the one whose BF16
+// rounding residual is smallest wins.  (1, mean) suits general data;
+// (255, mean on the 1/255 grid) and (1, integer mean) make 8-bit-quantised
+// data exactly representable, so its certificate is nearly exact.
+constexpr int NUM_SCALES = 3;
+__device__ __forceinline__ void scale_candidate(int i, float m, float* sc, float* mc) {
+  if (i == 0) { *sc = 1.0f; *mc = m; }
+  else if (i == 1) { *sc = 255.0f; *mc = rintf(m * 255.0f) / 255.0f; }
+  else { *sc = 1.0f; *mc = rintf(m); }
+}
+
+// per candidate: sum over sampled rows of ||cv - bf16(cv)||^2 / ||cv||^2
+__global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d,
+                                   const float* __restrict__ mu, int64_t stride,
+                                   double* __restrict__ score) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * stride;
+  const int cand = blockIdx.y;
+  if (row >= n) return;
+  double rr = 0.0, cc = 0.0;
+  for (int c = lane; c < d; c += 32) {
+    float sc, mc;
+    scale_candidate(cand, mu[c], &sc, &mc);
+    const float cv = __fmul_rn(sc, __fsub_rn(x[row * d + c], mc));
+    const float bv = __bfloat162float(__float2bfloat16_rn(cv));
+    rr += (double)(cv - bv) * (double)(cv - bv);
+    cc += (double)cv * (double)cv;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    rr += __shfl_xor_sync(FULL, rr, o);
+    cc += __shfl_xor_sync(FULL, cc, o);
+  }
+  if (lane == 0) atomicAdd(&score[cand], cc > 0.0 ? rr / cc : 0.0);
+}
+
+// replace mu by the chosen candidate's centre
+__global__ void apply_centre_kernel(float* __restrict__ mu, int d, int cand) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d) return;
+  float sc, mc;
+  scale_candidate(cand, mu[c], &sc, &mc);
+  mu[c] = mc;
+}
+
+// One warp per row: BF16 copy of scale*(x - mu) padded to dp, and the row's bound terms.
 __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
-                                    const float* __restrict__ mu, __nv_bfloat16* __restrict__ xb,
-                                    RowInfo* __restrict__ info, BaseMax* __restrict__ bmax) {
+                                    const float* __restrict__ mu, float scale,
+                                    __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
+                                    BaseMax* __restrict__ bmax) {
   const int lane = threadIdx.x & 31;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= n) return;
@@ -112,7 +158,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   double s_b = 0.0, s_r = 0.0, s_c = 0.0;
   for (int c = lane; c < dp; c += 32) {
     float cv = 0.0f;
-    if (c < d) cv = __fsub_rn(xr[c], mu[c]);
+    if (c < d) cv = __fmul_rn(scale, __fsub_rn(xr[c], mu[c]));
     const __nv_bfloat16 b = __float2bfloat16_rn(cv);
     br[c] = b;
     const float bv = __bfloat162float(b);
@@ -131,8 +177,8 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     RowInfo ri;
     ri.nrm = __double2float_rn(s_b);
     ri.xn_up = round_up_f(sqrt(s_b) * (1.0 + 1e-12));
-    // ||(x-mu)_exact - x~|| <= ||fl(x-mu) - x~|| + u ||fl(x-mu)|| (1+u)
-    ri.r_up = round_up_f((sqrt(s_r) + 5.9604645e-08 * 1.0000001 * sqrt(s_c)) * (1.0 + 1e-9));
+    // ||s(x-mu)_exact - x~|| <= ||cv - x~|| + 2u ||cv|| (1+u), cv = fl(s fl(x-mu))
+    ri.r_up = round_up_f((sqrt(s_r) + 2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c)) * (1.0 + 1e-9));
     ri.pad = 0.0f;
     info[row] = ri;
     if (bmax) {
@@ -407,10 +453,6 @@ __global__ void __launch_bounds__(K2_THREADS, 1)
 
 // ---------------------------------------------------------------- merge
 
-__device__ __forceinline__ int64_t h_chunk_begin(int c, int64_t work, int grid) {
-  return (int64_t)((__int128)c * work / grid);
-}
-
 // L smallest keys over the CTA segments of each query (warp per query).
 template <int KW>
 __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int smax, int tiles,
@@ -447,6 +489,7 @@ struct RerankArgs {
   const float* qs;
   int64_t nq, n;
   int d, L, kreq, metric;
+  float scale;  // the est values are in units of scale^2 * distance
   const RowInfo* qinfo;
   const BaseMax* bmax;
   const uint64_t* lists;  // [nq][L] sorted by est
@@ -480,7 +523,8 @@ __global__ void k2_rerank(RerankArgs a) {
   const double bxn = (double)__uint_as_float(a.bmax->xn_bits);
   const double br = (double)__uint_as_float(a.bmax->r_bits);
   const double u = 5.9604644775390625e-08;
-  const double gam = (double)(a.d + 32) * 2.384185791015625e-07;
+  // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
+  const double gam = (double)((a.d + 15) / 16 + 2) * 2.384185791015625e-07;
   const double c1 = 4.0 * u + 2.0 * gam;
   const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn);
   const double Rs = (double)qi.r_up + br;
@@ -492,7 +536,7 @@ __global__ void k2_rerank(RerankArgs a) {
   // lower bound on the exact distance of any point outside the list's est <= T set
   const double e_floor = fmax(T - c1 * A, 0.0);
   const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
-  double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u);
+  double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / ((double)a.scale * a.scale);
   const bool all_in = (last_key == KEY_NONE);  // the list holds every point
   const bool certified = all_in || (double)key_dist(last_key) > T;
   if (!certified) {
@@ -571,6 +615,17 @@ namespace {
 
 __device__ __forceinline__ double fp64_dist_row(const float* __restrict__ x,
                                                 const float* __restrict__ y, int d, int metric) {
+  if (metric == MANN_METRIC_COSINE) {
+    double ab = 0.0, aa = 0.0, bb = 0.0;
+    for (int c = 0; c < d; ++c) {
+      const double xv = (double)x[c], yv = (double)y[c];
+      ab = fma(xv, yv, ab);
+      aa = fma(xv, xv, aa);
+      bb = fma(yv, yv, bb);
+    }
+    const double r = 1.0 - ab / (sqrt(aa) * sqrt(bb));
+    return r < 0.0 ? 0.0 : r;
+  }
   double s = 0.0;
   for (int c = 0; c < d; ++c) {
     const double t = (double)x[c] - (double)y[c];
@@ -611,7 +666,9 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
     for (int p = 1; p < cm; ++p) {
       const double a = (double)key_dist(s_key[w][p - 1]);
       const double b = (double)key_dist(s_key[w][p]);
-      const bool link = (b - a) <= eps * (fabs(a) + fabs(b));
+      // FP32 cosine distances carry an absolute error of order (d+4)u
+      const bool link = metric == MANN_METRIC_COSINE ? (b - a) <= 2.0 * eps + 4.8e-7
+                                                     : (b - a) <= eps * (fabs(a) + fabs(b));
       if (!link) start = p;
       s_cl[w][p] = start;
     }
@@ -624,7 +681,10 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
   bool resolvable = true;
   if (end == cm - 1) {
     const double lastv = (double)key_dist(s_key[w][cm - 1]);
-    if (!(lastv * (1.0 + eps) < (double)floor_val[q] * (1.0 - eps))) resolvable = (cm < c) ? false : (floor_val[q] >= 3.0e38f);
+    const double fl = (double)floor_val[q];
+    const bool clear = metric == MANN_METRIC_COSINE ? lastv + 2.0 * eps + 4.8e-7 < fl
+                                                    : lastv * (1.0 + eps) < fl * (1.0 - eps);
+    resolvable = clear || fl >= 3.0e38;
   }
   bool any_tie = false;
   for (int p = 1; p <= end; ++p)
@@ -675,7 +735,52 @@ mann_status launch_resolve(const float* base, const float* qs, int d, int metric
   resolve_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(base, qs, d, metric, nq, L, kreq, fp64,
                                                             cand, cand_count, floor_val, keys_out,
                                                             counters, counters + 1);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
+namespace {
+
+// candidate table from an exact FP32 top-kk list: counts and the floor (the
+// kk-th distance bounds every point outside the list from below)
+__global__ void fp32_lists_to_cand_kernel(const uint64_t* __restrict__ keys, int64_t nq, int kk,
+                                          int* __restrict__ cand_count, float* __restrict__ floor_val) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const uint64_t* r = keys + q * kk;
+  int c = 0;
+  while (c < kk && r[c] != KEY_NONE) ++c;
+  cand_count[q] = c;
+  floor_val[q] = (c == kk) ? key_dist(r[kk - 1]) : 3.0e38f;
+}
+
+}  // namespace
+
+mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, const float* qs,
+                              int64_t n, int64_t nq, int d, int metric, int kk, int kreq,
+                              const uint64_t* fkeys, uint64_t** out_keys, mann_knn_report* rep) {
+  (void)n;
+  int* cand_count = nullptr;
+  float* floor_val = nullptr;
+  unsigned long long* counters = nullptr;
+  uint64_t* keys = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_MISC0, (size_t)nq, &cand_count));
+  MANN_TRY(ctx->scratch_t(SLOT_MISC1, (size_t)nq, &floor_val));
+  MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)nq * kreq, &keys));
+  MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
+  fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(fkeys, nq, kk, cand_count,
+                                                                       floor_val);
+  MANN_CHECK_LAUNCH();
+  MANN_TRY(launch_resolve(base, qs, d, metric, nq, kk, kreq, 1, fkeys, cand_count, floor_val, keys,
+                          counters + 4, s));
+  if (rep) {
+    unsigned long long h[2] = {0, 0};
+    MANN_CUDA_TRY(cudaMemcpyAsync(h, counters + 4, sizeof(h), cudaMemcpyDeviceToHost, s));
+    MANN_CUDA_TRY(cudaStreamSynchronize(s));
+    rep->rows_fp64_ties = (int64_t)h[0];
+  }
+  *out_keys = keys;
   return MANN_OK;
 }
 
@@ -752,27 +857,46 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   const int64_t rows_per = ceil_div(n, chunks);
   double* cpart = nullptr;
   float* mu = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_CENTRE, (size_t)chunks * d + (size_t)d, &cpart));
+  MANN_TRY(ctx->scratch_t(SLOT_CENTRE, (size_t)chunks * d + (size_t)d + 8, &cpart));
   MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));
   BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + ((d + 31) & ~31));
   dim3 cg((unsigned)ceil_div(d, 128), (unsigned)chunks);
   centre_partial_kernel<<<cg, 128, 0, s>>>(base, n, d, rows_per, cpart);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
   centre_final_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(cpart, chunks, d, n, mu);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
+  // pick the centre / scale with the smallest BF16 residual on a row sample
+  double* score = cpart;  // reuse: the partial sums are consumed
+  MANN_CUDA_TRY(cudaMemsetAsync(score, 0, NUM_SCALES * sizeof(double), s));
+  const int64_t sample_rows = std::min<int64_t>(n, 2048);
+  const int64_t stride = std::max<int64_t>(1, n / sample_rows);
+  dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
+  scale_probe_kernel<<<pg, 256, 0, s>>>(base, n, d, mu, stride, score);
+  MANN_CHECK_LAUNCH();
+  double h_score[NUM_SCALES];
+  MANN_CUDA_TRY(cudaMemcpyAsync(h_score, score, sizeof(h_score), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  int best = 0;
+  for (int i = 1; i < NUM_SCALES; ++i)
+    if (h_score[i] < 0.25 * h_score[best]) best = i;  // move off the plain mean only for a clear win
+  const float scale = best == 1 ? 255.0f : 1.0f;
+  if (best != 0) {
+    apply_centre_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(mu, d, best);
+    MANN_CHECK_LAUNCH();
+  }
   MANN_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(BaseMax), s));
   Bf16Operand B, Q;
   MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
-  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, dp, mu, B.xb, B.info, bmax);
-  MANN_CUDA_TRY(cudaGetLastError());
+  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, dp, mu, scale, B.xb, B.info, bmax);
+  MANN_CHECK_LAUNCH();
   if (self) {
     Q = B;
   } else {
     MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dp, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
-    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, dp, mu, Q.xb, Q.info, nullptr);
-    MANN_CUDA_TRY(cudaGetLastError());
+    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, dp, mu, scale, Q.xb, Q.info, nullptr);
+    MANN_CHECK_LAUNCH();
   }
 
   // ---- main
@@ -788,10 +912,6 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     const int c0 = h_cta_of(qb * tiles, work, grid);
     const int c1 = h_cta_of(qb * tiles + tiles - 1, work, grid);
     smax = std::max(smax, c1 - c0 + 1);
-    if (qblocks > 4096 && qb > 64) {  // the pattern is periodic; bound the host loop
-      smax = std::max(smax, (int)ceil_div(grid, qblocks) + 2);
-      break;
-    }
   }
   uint64_t* partial = nullptr;
   int* err = nullptr;
@@ -820,19 +940,22 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
   if (L == 32) {
     MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ctx->time_begin(s);
     k2_main<1><<<grid, K2_THREADS, smem, s>>>(mapA, mapB, ma);
   } else {
     MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ctx->time_begin(s);
     k2_main<2><<<grid, K2_THREADS, smem, s>>>(mapA, mapB, ma);
   }
-  MANN_CUDA_TRY(cudaGetLastError());
+  ctx->time_end(s);
+  MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_KEYS, (size_t)nq * L, &lists));
   if (L == 32)
     k2_merge<1><<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, lists);
   else
     k2_merge<2><<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, lists);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
 
   // ---- certify + rerank
   uint64_t* cand = nullptr;
@@ -852,6 +975,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.L = L;
   ra.kreq = kreq;
   ra.metric = metric;
+  ra.scale = scale;
   ra.qinfo = Q.info;
   ra.bmax = bmax;
   ra.lists = lists;
@@ -862,7 +986,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.fb_count = fb_count;
   ra.cand_total = counters + 2;
   k2_rerank<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(ra);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
 
   // ---- exact FP32 scan of uncertified rows (count known only on the device:
   // read it back; the common case is zero rows)
@@ -879,7 +1003,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_fb, d, metric, kk, fb_rows, no_norm, no_norm,
                            &fkeys, SLOT_FALLBACK_KEYS, SLOT_MISC2));
     k2_scatter_fallback<<<h_fb, 64, 0, s>>>(fkeys, fb_rows, fb_count, kk, L, cand, cand_count, floor_val);
-    MANN_CUDA_TRY(cudaGetLastError());
+    MANN_CHECK_LAUNCH();
   }
 
   // ---- resolve + truncate

@@ -386,7 +386,7 @@ __global__ void finish_kernel(const uint64_t* __restrict__ keys, int64_t nq, int
 }
 
 template <int METRIC, int BQ, int KW, bool VEC>
-mann_status launch_k1(const float* base, int64_t n, const float* qs, const int32_t* rows,
+mann_status launch_k1(Context* ctx, const float* base, int64_t n, const float* qs, const int32_t* rows,
                       int64_t nq, int d, const float* qn, const float* bn, int k,
                       int64_t split_len, int nsplit, uint64_t* partial, cudaStream_t s) {
   constexpr int QSTR = BQ + 4, BSTR = K1_BN + 4;
@@ -394,26 +394,28 @@ mann_status launch_k1(const float* base, int64_t n, const float* qs, const int32
   auto kern = k1_tile_topk<METRIC, BQ, KW, VEC>;
   MANN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((unsigned)ceil_div(nq, BQ), (unsigned)nsplit);
+  ctx->time_begin(s);
   kern<<<grid, K1_THREADS, smem, s>>>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                       partial);
-  MANN_CUDA_TRY(cudaGetLastError());
+  ctx->time_end(s);
+  MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
 template <int METRIC, bool VEC>
-mann_status dispatch_k1(int k, const float* base, int64_t n, const float* qs, const int32_t* rows,
+mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const float* qs, const int32_t* rows,
                         int64_t nq, int d, const float* qn, const float* bn, int64_t split_len,
                         int nsplit, uint64_t* partial, cudaStream_t s) {
   if (k <= 32)
-    return launch_k1<METRIC, 128, 1, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+    return launch_k1<METRIC, 128, 1, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                           partial, s);
   if (k <= 64)
-    return launch_k1<METRIC, 128, 2, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+    return launch_k1<METRIC, 128, 2, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                           partial, s);
   if (k <= 128)
-    return launch_k1<METRIC, 64, 4, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+    return launch_k1<METRIC, 64, 4, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                          partial, s);
-  return launch_k1<METRIC, 32, 8, VEC>(base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
+  return launch_k1<METRIC, 32, 8, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                        partial, s);
 }
 
@@ -422,7 +424,7 @@ mann_status dispatch_k1(int k, const float* base, int64_t n, const float* qs, co
 mann_status launch_row_sqnorm(const float* x, int64_t n, int d, float* out, cudaStream_t s) {
   if (n <= 0) return MANN_OK;
   row_sqnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, d, out);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
@@ -431,7 +433,7 @@ mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, in
   if (nq <= 0 || kout <= 0) return MANN_OK;
   finish_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(keys, nq, kk, kout, graph_self, rows,
                                                            ids, dists);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
@@ -461,21 +463,21 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
   mann_status st;
   switch (metric) {
     case MANN_METRIC_EUCLIDEAN:
-      st = vec ? dispatch_k1<MANN_METRIC_EUCLIDEAN, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+      st = vec ? dispatch_k1<MANN_METRIC_EUCLIDEAN, true>(ctx, kk, base, n, qs, rows, nq, d, qn, bn,
                                                           split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_EUCLIDEAN, false>(kk, base, n, qs, rows, nq, d, qn, bn,
+               : dispatch_k1<MANN_METRIC_EUCLIDEAN, false>(ctx, kk, base, n, qs, rows, nq, d, qn, bn,
                                                            split_len, nsplit, partial, s);
       break;
     case MANN_METRIC_SQEUCLIDEAN:
-      st = vec ? dispatch_k1<MANN_METRIC_SQEUCLIDEAN, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+      st = vec ? dispatch_k1<MANN_METRIC_SQEUCLIDEAN, true>(ctx, kk, base, n, qs, rows, nq, d, qn, bn,
                                                             split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_SQEUCLIDEAN, false>(kk, base, n, qs, rows, nq, d, qn,
+               : dispatch_k1<MANN_METRIC_SQEUCLIDEAN, false>(ctx, kk, base, n, qs, rows, nq, d, qn,
                                                              bn, split_len, nsplit, partial, s);
       break;
     default:
-      st = vec ? dispatch_k1<MANN_METRIC_COSINE, true>(kk, base, n, qs, rows, nq, d, qn, bn,
+      st = vec ? dispatch_k1<MANN_METRIC_COSINE, true>(ctx, kk, base, n, qs, rows, nq, d, qn, bn,
                                                        split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_COSINE, false>(kk, base, n, qs, rows, nq, d, qn, bn,
+               : dispatch_k1<MANN_METRIC_COSINE, false>(ctx, kk, base, n, qs, rows, nq, d, qn, bn,
                                                         split_len, nsplit, partial, s);
       break;
   }
@@ -487,7 +489,7 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
   uint64_t* keys = nullptr;
   MANN_TRY(ctx->scratch_t(slot_keys, (size_t)nq * kk, &keys));
   merge_lists_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, nsplit, kk, keys);
-  MANN_CUDA_TRY(cudaGetLastError());
+  MANN_CHECK_LAUNCH();
   *out_keys = keys;
   return MANN_OK;
 }

@@ -1,0 +1,110 @@
+"""Parity of the BF16 tensor-core form (MANN_PREC_BF16): certified candidates
+reranked in exact FP32 must give exactly the FP32 oracle's answer (ids and
+distance bits); with MANN_FLAG_FP64_TIES the ids must equal the FP64 oracle's.
+The report's fallback counter must stay near zero -- a wrong tensor-core tile
+would otherwise hide behind the exact FP32 fallback."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from test_knn_gpu import M_EUC, M_SQ, gpu_graph, gpu_knn, same_bits
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("metric", [M_SQ, M_EUC])
+def test_bf16_golden_mixture(gpu_lib, metric, orc):
+    g = load_golden("knn_mix_sq_d784")
+    base, q = g["base"], g["queries"]
+    ids, d, rep = gpu_knn(base, q, 10, metric, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 10, metric)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(d, d_o)
+    assert rep["precision_used"] == 1
+    assert rep["rows_fallback"] <= 2, rep
+
+
+def test_bf16_fp64_ties_golden(gpu_lib):
+    g = load_golden("knn_mix_sq_d784")
+    ids, d, rep = gpu_knn(g["base"], g["queries"], 10, M_SQ, precision="bf16", fp64_ties=True,
+                          report=True)
+    assert np.array_equal(ids, g["ids_f64"])
+    # distances are the FP32 ones
+    assert np.all(np.abs(d - g["dists_f64"]) <= 1e-5 * np.abs(g["dists_f64"]) + 1e-6)
+
+
+def test_bf16_graph_golden(gpu_lib):
+    g = load_golden("graph_mix_sq_d784")
+    ids, d, rep = gpu_graph(g["data"], 10, M_SQ, precision="bf16", report=True)
+    assert np.array_equal(ids, g["ids_f32"])
+    assert same_bits(d, g["dists_f32"])
+    ids64, _ = gpu_graph(g["data"], 10, M_SQ, precision="bf16", fp64_ties=True)
+    assert np.array_equal(ids64, g["ids_f64"])
+
+
+@pytest.mark.parametrize("n,nq,d,k", [(20000, 700, 128, 10), (9000, 300, 256, 20), (5000, 129, 784, 40),
+                                      (3000, 40, 200, 1), (777, 33, 96, 30)])
+def test_bf16_iid_shapes(gpu_lib, orc, n, nq, d, k):
+    rng = np.random.default_rng(n + d)
+    base = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((nq, d)).astype(np.float32)
+    ids, dist, rep = gpu_knn(base, q, k, M_SQ, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, k, orc.SQEUCLIDEAN)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dist, d_o)
+    if d <= 256:  # at d=784 i.i.d. points are nearly equidistant: falling back is expected
+        assert rep["rows_fallback"] <= max(2, nq // 10), rep
+
+
+def test_bf16_quantized_workload_slice(gpu_lib, orc):
+    # the 784-d quantised mixture at 1/6 of its point count, all queries of one batch
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.quantized_mixture(10000, 784, seed=1)
+    q = synthetic.quantized_mixture(500, 784, seed=2)
+    ids, d, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 10, orc.SQEUCLIDEAN)
+    assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
+    assert rep["rows_fallback"] <= 5, rep
+    ids64, _ = gpu_knn(base, q, 10, M_SQ, precision="bf16", fp64_ties=True)
+    ids_o64, _ = orc.knn_f64(base, q, 10, orc.SQEUCLIDEAN)
+    assert np.array_equal(ids64, ids_o64)
+
+
+def test_fp32_form_fp64_ties(gpu_lib, orc):
+    g = load_golden("knn_mix_sq_d784")
+    ids, _ = gpu_knn(g["base"], g["queries"], 10, M_SQ, precision="fp32", fp64_ties=True)
+    assert np.array_equal(ids, g["ids_f64"])
+    g = load_golden("knn_iid_cos_d37")
+    ids, _ = gpu_knn(g["base"], g["queries"], 20, 2, precision="fp32", fp64_ties=True)
+    assert np.array_equal(ids, g["ids_f64"])
+
+
+def test_bf16_duplicates_certify_or_fall_back(gpu_lib, orc):
+    # many identical points: the candidate list cannot be certified, the exact
+    # scan answers instead -- still identical to the oracle
+    rng = np.random.default_rng(2)
+    base = np.repeat(rng.standard_normal((40, 128)).astype(np.float32), 100, axis=0)
+    q = base[::97].copy()
+    ids, d, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 10, orc.SQEUCLIDEAN)
+    assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
+
+
+def test_bf16_full_size_equals_fp32_kernel(gpu_lib):
+    # N=60,000 quantised 784-d points, 10,000 held-out queries and the self graph:
+    # the two GPU forms must agree bit for bit (size-independent property)
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.quantized_mixture(60000, 784, seed=1)
+    q = synthetic.quantized_mixture(10000, 784, seed=2)
+    i32, d32 = gpu_knn(base, q, 10, M_SQ, precision="fp32")
+    ib, db, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", report=True)
+    assert np.array_equal(i32, ib) and same_bits(d32, db)
+    assert rep["rows_fallback"] <= 20, rep
+    assert np.all(np.diff(db, axis=1) >= 0)
+    g32, gd32 = gpu_graph(base, 10, M_SQ, precision="fp32")
+    gb, gdb, rep = gpu_graph(base, 10, M_SQ, precision="bf16", report=True)
+    assert np.array_equal(g32, gb) and same_bits(gd32, gdb)
+    assert not np.any(gb == np.arange(60000)[:, None])
+    assert rep["rows_fallback"] <= 120, rep
