@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--fp32-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--case", choices=["full", "profile"], default="full",
+                    help="profile: only the BF16 search of the 10000 held-out queries against the "
+                         "60000 points, per step (one k2_main launch), for ncu captures")
     return ap.parse_args()
 
 
@@ -168,6 +171,30 @@ def run_reference(args):
                                        "BruteForceIndex algorithm restated in C (Julia is not installed)"},
             "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile_case(args):
+    """Case for ncu: the BF16 search of the held-out queries against all points."""
+    import torch
+
+    from manifoldann_gb300 import _lib
+
+    lib = _lib.load()
+    base, q = make_workload()
+    nq = N_QUERIES
+    tb = torch.from_numpy(base).cuda()
+    tq = torch.from_numpy(q[:nq]).cuda()
+    qi = torch.empty((nq, K), dtype=torch.int32, device="cuda")
+    qd = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_BF16)
+    for _ in range(args.warmup + args.steps):
+        _lib.check(lib.mann_knn_device(p, tb.data_ptr(), N_POINTS, tq.data_ptr(), nq, DIM,
+                                       qi.data_ptr(), qd.data_ptr(), None, sp))
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "profile", "queries": nq, "points": N_POINTS, "d": DIM,
+                      "launches_of_k2_main": args.warmup + args.steps}), flush=True)
     return 0
 
 
@@ -316,6 +343,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.case == "profile":
+        return run_profile_case(args)
     return run_ours(args)
 
 

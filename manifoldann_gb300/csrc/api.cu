@@ -87,10 +87,10 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
   bool use_bf16 = false;
   if (p->precision == MANN_PREC_BF16) {
     if (!l2) return fail(MANN_EINVAL_ARG, "the BF16 form supports SqEuclidean and Euclidean");
-    if (kreq > 64) return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= 64 (k+1 for graphs)");
+    if (kreq > 24) return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= 24 (k+1 for graphs)");
     use_bf16 = true;
   } else if (p->precision == MANN_PREC_AUTO) {
-    use_bf16 = l2 && kreq <= 48 && d >= 128 && n >= 4096;
+    use_bf16 = l2 && kreq <= 24 && d >= 128 && n >= 4096;
   }
   uint64_t* keys = nullptr;
   if (use_bf16) {

@@ -55,7 +55,9 @@ constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int K2_THREADS = 64 + NUM_EPI_WARPS * 32;  // producer, MMA, 4 epilogue warps
-constexpr int STAGE_CAP = 16;                        // staged candidates per row per 16-column chunk
+constexpr int LIST = 32;                             // candidates kept per query row
+constexpr int TSTR = 36;                             // row stride of the 32x32 transpose (floats)
+constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
 
 enum : int { ERR_TIMEOUT_PRODUCER = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_EPI = 3 };
@@ -74,25 +76,15 @@ struct BaseMax {
 
 // ---------------------------------------------------------------- prep kernels
 
-// partial column sums over a chunk of rows (deterministic order)
-__global__ void centre_partial_kernel(const float* __restrict__ x, int64_t n, int d, int64_t rows_per,
-                                      double* __restrict__ partial) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d) return;
-  const int64_t r0 = (int64_t)blockIdx.y * rows_per;
-  const int64_t r1 = min(n, r0 + rows_per);
-  double s = 0.0;
-  for (int64_t r = r0; r < r1; ++r) s += (double)x[r * d + c];
-  partial[(int64_t)blockIdx.y * d + c] = s;
-}
-
-__global__ void centre_final_kernel(const double* __restrict__ partial, int chunks, int d, int64_t n,
-                                    float* __restrict__ mu) {
+// Column means over an evenly spaced sample of rows.  Any centre keeps the
+// distances unchanged; a good one shrinks the BF16 values and their rounding.
+__global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
+                                     int64_t rows, float* __restrict__ mu) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= d) return;
   double s = 0.0;
-  for (int i = 0; i < chunks; ++i) s += partial[(int64_t)i * d + c];
-  mu[c] = (float)(s / (double)n);
+  for (int64_t i = 0; i < rows; ++i) s += (double)x[(i * stride) * d + c];
+  mu[c] = (float)(s / (double)rows);
 }
 
 __device__ __forceinline__ float round_up_f(double v) {
@@ -136,26 +128,43 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
   if (lane == 0) atomicAdd(&score[cand], cc > 0.0 ? rr / cc : 0.0);
 }
 
-// replace mu by the chosen candidate's centre
-__global__ void apply_centre_kernel(float* __restrict__ mu, int d, int cand) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d) return;
-  float sc, mc;
-  scale_candidate(cand, mu[c], &sc, &mc);
-  mu[c] = mc;
+// pick the candidate with the smallest residual (moving off the plain mean
+// only for a clear win), replace mu by its centre and publish its scale
+__global__ void choose_scale_kernel(const double* __restrict__ score, float* __restrict__ mu, int d,
+                                    float* __restrict__ scale_out) {
+  __shared__ int best;
+  if (threadIdx.x == 0) {
+    int b = 0;
+    for (int i = 1; i < NUM_SCALES; ++i)
+      if (score[i] < 0.25 * score[b]) b = i;
+    best = b;
+    float sc, mc;
+    scale_candidate(b, 0.0f, &sc, &mc);
+    *scale_out = sc;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < d; c += blockDim.x) {
+    float sc, mc;
+    scale_candidate(best, mu[c], &sc, &mc);
+    mu[c] = mc;
+  }
 }
 
 // One warp per row: BF16 copy of scale*(x - mu) padded to dp, and the row's bound terms.
 __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
-                                    const float* __restrict__ mu, float scale,
+                                    const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
                                     BaseMax* __restrict__ bmax) {
   const int lane = threadIdx.x & 31;
+  const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= n) return;
   const float* xr = x + row * d;
   __nv_bfloat16* br = xb + row * dp;
-  double s_b = 0.0, s_r = 0.0, s_c = 0.0;
+  // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
+  // sum carries a relative error below (ceil(dp/32) + 2) u, which the
+  // certificate adds to its bound (norm_rel_err)
+  float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f;
   for (int c = lane; c < dp; c += 32) {
     float cv = 0.0f;
     if (c < d) cv = __fmul_rn(scale, __fsub_rn(xr[c], mu[c]));
@@ -163,10 +172,11 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     br[c] = b;
     const float bv = __bfloat162float(b);
     const float rv = cv - bv;  // exact: the rounding residual of a float fits in a float
-    s_b += (double)bv * (double)bv;
-    s_r += (double)rv * (double)rv;
-    s_c += (double)cv * (double)cv;
+    f_b = __fmaf_rn(bv, bv, f_b);
+    f_r = __fmaf_rn(rv, rv, f_r);
+    f_c = __fmaf_rn(cv, cv, f_c);
   }
+  double s_b = f_b, s_r = f_r, s_c = f_c;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     s_b += __shfl_xor_sync(FULL, s_b, o);
@@ -174,11 +184,13 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     s_c += __shfl_xor_sync(FULL, s_c, o);
   }
   if (lane == 0) {
+    const double rel = (double)((dp + 31) / 32 + 2) * 5.9604644775390625e-08;
     RowInfo ri;
     ri.nrm = __double2float_rn(s_b);
-    ri.xn_up = round_up_f(sqrt(s_b) * (1.0 + 1e-12));
+    ri.xn_up = round_up_f(sqrt(s_b * (1.0 + rel)) * (1.0 + 1e-12));
     // ||s(x-mu)_exact - x~|| <= ||cv - x~|| + 2u ||cv|| (1+u), cv = fl(s fl(x-mu))
-    ri.r_up = round_up_f((sqrt(s_r) + 2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c)) * (1.0 + 1e-9));
+    ri.r_up = round_up_f((sqrt(s_r * (1.0 + rel)) +
+                          2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c * (1.0 + rel))) * (1.0 + 1e-9));
     ri.pad = 0.0f;
     info[row] = ri;
     if (bmax) {
@@ -197,7 +209,8 @@ struct MainArgs {
   int64_t work;       // qblocks * tiles
   int grid;           // CTAs
   int smax;           // partial-list slots per query
-  int L;              // list length (k + margin), 32 or 64
+  int L;              // list capacity (32)
+  int depth;          // admission depth = k + margin (<= L)
   const RowInfo* qinfo;
   const RowInfo* binfo;
   uint64_t* partial;  // [nq][smax][L]
@@ -237,19 +250,138 @@ __device__ __forceinline__ void wl_insert(uint64_t (&Lr)[KW], uint64_t c, int la
   }
 }
 
-template <int KW>
-__global__ void __launch_bounds__(K2_THREADS, 1)
+// ---- warp-cooperative helpers on a 32-entry sorted list (lane i holds entry i)
+__device__ __forceinline__ uint64_t shfl_xor_u64(uint64_t v, int m) {
+  return (uint64_t)__shfl_xor_sync(FULL, (unsigned long long)v, m);
+}
+
+// ascending bitonic sort of one key per lane
+__device__ __forceinline__ uint64_t warp_sort32(uint64_t x, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint64_t y = shfl_xor_u64(x, j);
+      const bool up = (lane & k) == 0 || k == 32;
+      const bool lower = (lane & j) == 0;
+      x = (lower == up) ? min(x, y) : max(x, y);
+    }
+  }
+  return x;
+}
+
+// lane i: i-th smallest of the union of two ascending 32-lists
+__device__ __forceinline__ uint64_t warp_merge32(uint64_t a, uint64_t b_sorted, int lane) {
+  const uint64_t br = __shfl_sync(FULL, (unsigned long long)b_sorted, 31 - lane);
+  uint64_t x = min(a, br);  // bitonic
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const uint64_t y = shfl_xor_u64(x, j);
+    x = ((lane & j) == 0) ? min(x, y) : max(x, y);
+  }
+  return x;
+}
+
+// One 32-column chunk of the epilogue for a warp's 32 rows.  v: this lane's
+// row (32 accumulators), nb: the chunk's point norms, tw: 32 x TSTR transpose
+// buffer, thr: per-row admission threshold (est' of the depth-th entry),
+// lists: the warp's row lists (entry e of row r at lists[r * CAP + e]).
+// Lane r first tests its own row; only rows with candidates go through the
+// transpose, where the whole warp folds them into the row's list.
+template <int CAP>
+__device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* __restrict__ nb,
+                                          float* __restrict__ tw, float* __restrict__ thr,
+                                          uint64_t* __restrict__ lists, uint32_t col0, int lane,
+                                          int depth) {
+  const float INF = __int_as_float(0x7F800000);
+  const float4* nb4 = reinterpret_cast<const float4*>(nb);
+  const float t_own = thr[lane];
+  float e[32];
+  unsigned mask = 0;
+#pragma unroll
+  for (int j4 = 0; j4 < 8; ++j4) {
+    const float4 n4 = nb4[j4];
+    e[4 * j4 + 0] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 0]), n4.x);
+    e[4 * j4 + 1] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 1]), n4.y);
+    e[4 * j4 + 2] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 2]), n4.z);
+    e[4 * j4 + 3] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 3]), n4.w);
+  }
+#pragma unroll
+  for (int j = 0; j < 32; ++j) mask |= (e[j] < t_own) ? (1u << j) : 0u;
+  unsigned rows = __ballot_sync(FULL, mask != 0);
+  if (rows == 0) return;
+  if (mask) {
+    float4* trow = reinterpret_cast<float4*>(tw + lane * TSTR);
+#pragma unroll
+    for (int j4 = 0; j4 < 8; ++j4)
+      trow[j4] = make_float4(e[4 * j4 + 0], e[4 * j4 + 1], e[4 * j4 + 2], e[4 * j4 + 3]);
+  }
+  __syncwarp();
+  const uint32_t mycol = col0 + (uint32_t)lane;
+  while (rows) {
+    const int r = __ffs(rows) - 1;
+    rows &= rows - 1;
+    unsigned m = __shfl_sync(FULL, mask, r);
+    const float x = tw[r * TSTR + lane];
+    uint64_t key = ((m >> lane) & 1u) ? make_key(x, mycol) : KEY_NONE;
+    uint64_t Lr = lane < CAP ? lists[r * CAP + lane] : KEY_NONE;
+    if (__popc(m) > 3) {
+      key = warp_sort32(key, lane);
+      Lr = warp_merge32(Lr, key, lane);
+    } else {
+      uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        const uint64_t c = __shfl_sync(FULL, (unsigned long long)key, b);
+        if (c < tk) {
+          uint64_t one[1] = {Lr};
+          wl_insert<1>(one, c, lane);
+          Lr = one[0];
+          tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+        }
+      }
+    }
+    if (lane < CAP) lists[r * CAP + lane] = Lr;
+    const uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+    if (lane == r) thr[r] = (tk == KEY_NONE) ? INF : key_dist(tk);
+  }
+  __syncwarp();
+}
+
+// Shared-memory footprint of k2_main<CAP, NSETS>.
+__host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
+  return 1024 /* alignment */ + (size_t)STAGES * STAGE_BYTES +
+         (size_t)nsets * BM * cap * 8 /* lists */ + (size_t)nsets * 4 * 32 * TSTR * 4 /* transpose */ +
+         (size_t)nsets * 4 * 32 * 4 /* thresholds */ + (size_t)nsets * 4 * BN * 4 /* norms */ +
+         (2 * STAGES + 4) * 8 + 16;
+}
+
+// The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
+// ||q~||^2 is left out: it does not change the row's order).  A point is
+// admitted when its key is below the row's `depth`-th entry, so the first
+// `depth` entries of a list are exactly the segment's `depth` smallest keys and
+// every point left out has est' >= the depth-th entry (the certificate's
+// premise); entries past `depth` are admitted points kept while space lasts.
+//
+// Warps: 0 = TMA producer, 1 = MMA issuer (and TMEM owner), then NSETS sets
+// of 4 epilogue warps.  With two sets, set h drains accumulator buffer h, so
+// each set has two tile-times per tile; each set keeps its own lists and
+// writes them to its own partial slot.
+template <int CAP, int NSETS>
+__global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
             MainArgs a) {
-  constexpr int L = KW * 32;
+  constexpr int NEPI = 4 * NSETS;
   extern __shared__ __align__(1024) uint8_t k2_smem_raw[];
-  // 1024-byte alignment for the swizzled stages
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(k2_smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* stage_base = smem;                                            // STAGES * 48 KB
-  uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [BM][L]
-  uint64_t* staging = lists + BM * L;                                   // [STAGE_CAP][BM]
-  uint64_t* bars = staging + STAGE_CAP * BM;                            // full[S], empty[S], tfull[2], tempty[2]
+  uint8_t* stage_base = smem;                                                   // STAGES * 48 KB
+  uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [NSETS][BM][CAP]
+  float* trans = reinterpret_cast<float*>(lists + NSETS * BM * CAP);            // [NEPI][32][TSTR]
+  float* thrs = trans + NEPI * 32 * TSTR;                                        // [NEPI][32]
+  float* nbs = thrs + NEPI * 32;                                                 // [NEPI][BN]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(nbs + NEPI * BN);
   uint64_t* full_bar = bars;
   uint64_t* empty_bar = bars + STAGES;
   uint64_t* tfull_bar = bars + 2 * STAGES;
@@ -268,7 +400,7 @@ __global__ void __launch_bounds__(K2_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&tfull_bar[b], 1);
-      ptx::mbar_init(&tempty_bar[b], NUM_EPI_WARPS * 32);
+      ptx::mbar_init(&tempty_bar[b], (NSETS == 2 ? 4 : NEPI) * 32);
     }
     ptx::fence_mbar_init();
     ptx::prefetch_tensormap(&mapA);
@@ -343,104 +475,87 @@ __global__ void __launch_bounds__(K2_THREADS, 1)
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int ew = warp - 2;           // 0..3
-    const int quad = warp & 3;         // TMEM lane quadrant this warp may access
-    const int row = quad * 32 + lane;  // row of the 128-query tile
-    uint64_t* my_list_base = lists;    // list of row r: lists[r * L + e]
-    float thr = __int_as_float(0x7F800000);
-    int cnt = 0;
+    const int ew = warp - 2;          // 0 .. NEPI-1
+    const int set = ew >> 2;          // which accumulator buffer this warp drains (two sets)
+    const int quad = warp & 3;        // TMEM lane quadrant this warp may access
+    float* nbw = nbs + ew * BN;       // point norms of the current tile
+    float* tw = trans + ew * (32 * TSTR);
+    float* thrw = thrs + ew * 32;     // est' of each row's depth-th entry (+inf until full)
+    uint64_t* lw = lists + (size_t)set * BM * CAP + quad * 32 * CAP;  // lw[r * CAP + e]
+    const float INF = __int_as_float(0x7F800000);
     int tcount = 0;
     int cur_qb = -1;
     int seg_first_cta = 0;
-    float qn = 0.0f;
     bool alive = true;
-    (void)ew;
 
-    // reset the 32 lists owned by this warp
+    thrw[lane] = INF;
     for (int r = 0; r < 32; ++r)
-      for (int e = lane; e < L; e += 32) my_list_base[(quad * 32 + r) * L + e] = KEY_NONE;
+      if (lane < CAP) lw[r * CAP + lane] = KEY_NONE;
     __syncwarp();
-
-    auto flush = [&](int qb) {
-      // write this warp's 32 lists into the partial buffer and reset them
-      const int slot = cta - seg_first_cta;
-      for (int r = 0; r < 32; ++r) {
-        const int64_t gq = (int64_t)qb * BM + quad * 32 + r;
-        uint64_t* lr = my_list_base + (quad * 32 + r) * L;
-        for (int e = lane; e < L; e += 32) {
-          if (gq < a.nq) a.partial[(gq * a.smax + slot) * L + e] = lr[e];
-          lr[e] = KEY_NONE;
-        }
-      }
-      __syncwarp();
-      thr = __int_as_float(0x7F800000);
-    };
 
     for (int64_t item = it0; item < it1; ++item, ++tcount) {
       const int qb = (int)(item / a.tiles);
       const int t = (int)(item % a.tiles);
       if (qb != cur_qb) {
-        if (cur_qb >= 0) flush(cur_qb);
+        if (cur_qb >= 0) {
+          // flush the finished segment's lists (every set, even one that saw no tile)
+          const int slot = (cta - seg_first_cta) * NSETS + set;
+          for (int r = 0; r < 32; ++r) {
+            const int64_t gq = (int64_t)cur_qb * BM + quad * 32 + r;
+            const uint64_t v = lane < CAP ? lw[r * CAP + lane] : KEY_NONE;
+            if (gq < a.nq) a.partial[(gq * a.smax + slot) * LIST + lane] = v;
+            if (lane < CAP) lw[r * CAP + lane] = KEY_NONE;
+          }
+          thrw[lane] = INF;
+          __syncwarp();
+        }
         cur_qb = qb;
         seg_first_cta = cta_of((int64_t)qb * a.tiles, a.work, a.grid);
-        const int64_t gq = (int64_t)qb * BM + row;
-        qn = gq < a.nq ? a.qinfo[gq].nrm : 0.0f;
       }
       const int buf = tcount & 1;
+      if (NSETS == 2 && buf != set) continue;
+      const int64_t col0 = (int64_t)t * BN;
+#pragma unroll
+      for (int i = 0; i < BN / 32; ++i) {
+        const int64_t col = col0 + lane + 32 * i;
+        nbw[lane + 32 * i] = col < a.n ? __ldg(&a.binfo[col].nrm) : INF;
+      }
+      __syncwarp();
       const uint32_t tph = (tcount >> 1) & 1;
       if (alive && !ptx::mbar_wait(&tfull_bar[buf], tph, a.err, ERR_TIMEOUT_EPI)) alive = false;
       if (!alive) break;
       ptx::tc_fence_after();
-      const int64_t col0 = (int64_t)t * BN;
       const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
-      for (int ch = 0; ch < BN / 16; ++ch) {
-        uint32_t v[16];
-        ptx::tmem_ld16(taddr + ch * 16, v);
+      uint32_t va[32], vb[32];
+      ptx::tmem_ld16(taddr, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
+      ptx::tmem_ld16(taddr + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
+      ptx::tmem_ld_wait();
+#pragma unroll 1
+      for (int ch = 0; ch < BN / 32; ch += 2) {
+        // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
+        ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
+        ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
+        epi_chunk<CAP>(va, nbw + ch * 32, tw, thrw, lw, (uint32_t)(col0 + ch * 32), lane, a.depth);
         ptx::tmem_ld_wait();
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int64_t col = col0 + ch * 16 + j;
-          if (col < a.n) {
-            const float nb = __ldg(&a.binfo[col].nrm);
-            const float est = __fmaf_rn(-2.0f, __uint_as_float(v[j]), __fadd_rn(qn, nb));
-            if (est < thr) {
-              staging[cnt * BM + row] = make_key(est, (uint32_t)col);
-              ++cnt;
-            }
-          }
+        if (ch + 2 < BN / 32) {
+          ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
+          ptx::tmem_ld16(taddr + (ch + 2) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
         }
-        // fold staged candidates into the lists, one row at a time (warp-cooperative)
-        unsigned pending = __ballot_sync(FULL, cnt > 0);
-        while (pending) {
-          const int r = __ffs(pending) - 1;
-          pending &= pending - 1;
-          const int rrow = quad * 32 + r;
-          const int rc = __shfl_sync(FULL, cnt, r);
-          uint64_t* lr = my_list_base + rrow * L;
-          uint64_t Lr[KW];
-#pragma unroll
-          for (int s = 0; s < KW; ++s) Lr[s] = lr[s * 32 + lane];
-          uint64_t tk = __shfl_sync(FULL, Lr[KW - 1], 31);
-          for (int e = 0; e < rc; ++e) {
-            const uint64_t c = staging[e * BM + rrow];
-            if (c < tk) {
-              wl_insert<KW>(Lr, c, lane);
-              tk = __shfl_sync(FULL, Lr[KW - 1], 31);
-            }
-          }
-#pragma unroll
-          for (int s = 0; s < KW; ++s) lr[s * 32 + lane] = Lr[s];
-          if (lane == r) {
-            cnt = 0;
-            thr = (tk == KEY_NONE) ? __int_as_float(0x7F800000) : key_dist(tk);
-          }
-        }
-        __syncwarp();
+        epi_chunk<CAP>(vb, nbw + (ch + 1) * 32, tw, thrw, lw, (uint32_t)(col0 + (ch + 1) * 32),
+                       lane, a.depth);
+        ptx::tmem_ld_wait();
       }
       ptx::tc_fence_before();
       ptx::mbar_arrive(&tempty_bar[buf]);
     }
-    if (alive && cur_qb >= 0) flush(cur_qb);
+    if (alive && cur_qb >= 0) {
+      const int slot = (cta - seg_first_cta) * NSETS + set;
+      for (int r = 0; r < 32; ++r) {
+        const int64_t gq = (int64_t)cur_qb * BM + quad * 32 + r;
+        const uint64_t v = lane < CAP ? lw[r * CAP + lane] : KEY_NONE;
+        if (gq < a.nq) a.partial[(gq * a.smax + slot) * LIST + lane] = v;
+      }
+    }
   }
 
   ptx::tc_fence_before();
@@ -453,33 +568,32 @@ __global__ void __launch_bounds__(K2_THREADS, 1)
 
 // ---------------------------------------------------------------- merge
 
-// L smallest keys over the CTA segments of each query (warp per query).
-template <int KW>
+// The `depth` smallest keys over the CTA segments of each query (warp per
+// query); only the first `depth` entries of every segment list take part.
 __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int smax, int tiles,
-                         int64_t work, int grid, uint64_t* __restrict__ out) {
-  constexpr int L = KW * 32;
+                         int64_t work, int grid, int depth, int nsets, uint64_t* __restrict__ out) {
+  constexpr int L = LIST;
   const int lane = threadIdx.x & 31;
   const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (q >= nq) return;
   const int64_t qb = q / BM;
   const int c0 = cta_of(qb * tiles, work, grid);
   const int c1 = cta_of(qb * tiles + tiles - 1, work, grid);
-  const int nseg = c1 - c0 + 1;
-  uint64_t Lr[KW];
-#pragma unroll
-  for (int s = 0; s < KW; ++s) Lr[s] = partial[(q * smax + 0) * L + s * 32 + lane];
+  const int nseg = (c1 - c0 + 1) * nsets;
+  uint64_t Lr = lane < depth ? partial[(q * smax + 0) * L + lane] : KEY_NONE;
   for (int g = 1; g < nseg; ++g) {
     const uint64_t* src = partial + (q * smax + g) * L;
-    uint64_t tk = __shfl_sync(FULL, Lr[KW - 1], 31);
-    for (int e = 0; e < L; ++e) {
+    uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+    for (int e = 0; e < depth; ++e) {
       const uint64_t c = src[e];  // sorted: stop at the first that cannot enter
       if (!(c < tk)) break;
-      wl_insert<KW>(Lr, c, lane);
-      tk = __shfl_sync(FULL, Lr[KW - 1], 31);
+      uint64_t one[1] = {Lr};
+      wl_insert<1>(one, c, lane);
+      Lr = lane < depth ? one[0] : KEY_NONE;
+      tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
     }
   }
-#pragma unroll
-  for (int s = 0; s < KW; ++s) out[q * L + s * 32 + lane] = Lr[s];
+  out[q * L + lane] = Lr;
 }
 
 // ---------------------------------------------------------------- certify + rerank
@@ -488,8 +602,9 @@ struct RerankArgs {
   const float* base;
   const float* qs;
   int64_t nq, n;
-  int d, L, kreq, metric;
-  float scale;  // the est values are in units of scale^2 * distance
+  int d, L, kreq, metric, depth;
+  const float* scale;  // the est values are in units of scale^2 * distance
+  unsigned long long* depth_hist;  // [LIST + 2]: rows by the list depth their certificate needed
   const RowInfo* qinfo;
   const BaseMax* bmax;
   const uint64_t* lists;  // [nq][L] sorted by est
@@ -501,10 +616,28 @@ struct RerankArgs {
   unsigned long long* cand_total;
 };
 
+// sequential difference-form sum over dimensions 0..d-1 (the FP32 form's order)
 __device__ __forceinline__ float fp32_dist_row(const float* __restrict__ x,
                                                const float* __restrict__ y, int d, int metric) {
   float s = 0.0f;
-  for (int c = 0; c < d; ++c) {
+  int c = 0;
+  if ((d & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0) {
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    const float4* y4 = reinterpret_cast<const float4*>(y);
+    for (; c < (d >> 2); ++c) {
+      const float4 a = __ldg(x4 + c), b = __ldg(y4 + c);
+      float t = __fsub_rn(a.x, b.x);
+      s = __fmaf_rn(t, t, s);
+      t = __fsub_rn(a.y, b.y);
+      s = __fmaf_rn(t, t, s);
+      t = __fsub_rn(a.z, b.z);
+      s = __fmaf_rn(t, t, s);
+      t = __fsub_rn(a.w, b.w);
+      s = __fmaf_rn(t, t, s);
+    }
+    c = d;
+  }
+  for (; c < d; ++c) {
     const float t = __fsub_rn(x[c], y[c]);
     s = __fmaf_rn(t, t, s);
   }
@@ -517,7 +650,7 @@ __global__ void k2_rerank(RerankArgs a) {
   if (q >= a.nq) return;
   const uint64_t* lst = a.lists + q * a.L;
   const uint64_t ek_key = lst[a.kreq - 1];
-  const uint64_t last_key = lst[a.L - 1];
+  const uint64_t last_key = lst[a.depth - 1];
   // threshold (identical on every lane)
   const RowInfo qi = a.qinfo[q];
   const double bxn = (double)__uint_as_float(a.bmax->xn_bits);
@@ -525,10 +658,14 @@ __global__ void k2_rerank(RerankArgs a) {
   const double u = 5.9604644775390625e-08;
   // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
   const double gam = (double)((a.d + 15) / 16 + 2) * 2.384185791015625e-07;
-  const double c1 = 4.0 * u + 2.0 * gam;
+  // + the relative error of the FP32-accumulated row norms (two of them)
+  const int dpad = (a.d + 7) & ~7;
+  const double nerr = (double)((dpad + 31) / 32 + 2) * u;
+  const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
   const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn);
   const double Rs = (double)qi.r_up + br;
-  const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key), 0.0);
+  const double qn = (double)qi.nrm;  // list keys hold est' = est - ||q~||^2
+  const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key) + qn, 0.0);
   const double sU = sqrt(ek + c1 * A) + Rs;
   const double U = sU * sU;
   const double slack = 3.0 * (double)(a.d + 2) * u * U + 1e-6 * U + 1e-30;
@@ -536,9 +673,16 @@ __global__ void k2_rerank(RerankArgs a) {
   // lower bound on the exact distance of any point outside the list's est <= T set
   const double e_floor = fmax(T - c1 * A, 0.0);
   const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
-  double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / ((double)a.scale * a.scale);
+  const double sc = (double)*a.scale;
+  double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
   const bool all_in = (last_key == KEY_NONE);  // the list holds every point
-  const bool certified = all_in || (double)key_dist(last_key) > T;
+  const bool certified = all_in || (double)key_dist(last_key) + qn > T;
+  {
+    // depth this row's certificate needs: one past its last est <= T entry
+    const uint64_t kl = lst[lane];
+    const int le = __popc(__ballot_sync(FULL, kl != KEY_NONE && (double)key_dist(kl) + qn <= T));
+    if (lane == 0) atomicAdd(&a.depth_hist[certified ? min(le + 1, LIST) : LIST + 1], 1ull);
+  }
   if (!certified) {
     if (lane == 0) {
       const int slot = atomicAdd(a.fb_count, 1);
@@ -557,7 +701,7 @@ __global__ void k2_rerank(RerankArgs a) {
     const int e = s * 32 + lane;
     if (e < a.L) {
       const uint64_t k = lst[e];
-      if (k != KEY_NONE && (double)key_dist(k) <= T) {
+      if (k != KEY_NONE && (double)key_dist(k) + qn <= T) {
         const int id = key_id(k);
         const float dist = fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
         key[s] = make_key(dist, (uint32_t)id);
@@ -821,11 +965,6 @@ mann_status make_map(CUtensorMap* m, const void* ptr, int64_t rows, int dp, int 
   return MANN_OK;
 }
 
-size_t main_smem_bytes(int L) {
-  return 1024 /* alignment */ + (size_t)STAGES * STAGE_BYTES + (size_t)BM * L * 8 +
-         (size_t)STAGE_CAP * BM * 8 + (2 * STAGES + 4) * 8 + 16;
-}
-
 int64_t h_chunk(int c, int64_t work, int grid) { return (int64_t)((__int128)c * work / grid); }
 int h_cta_of(int64_t i, int64_t work, int grid) {
   int c = (int)((__int128)i * grid / work);
@@ -847,43 +986,48 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
                           bool fp64, uint64_t** out_keys, mann_knn_report* rep) {
   if (metric == MANN_METRIC_COSINE) return fail(MANN_EINVAL_ARG, "BF16 form: L2 metrics only");
   if (nq <= 0) return MANN_OK;
-  const int L = (kreq + std::max(margin, 0) <= 32 && margin > 0) ? 32 : 64;
-  if (kreq > L) return fail(MANN_EINVAL_ARG, "BF16 form supports k <= 64");
+  const int L = LIST;
+  // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
+  // autotuner's choice for this shape class -- the full list on first sight,
+  // then the depth 99% of rows needed plus one (refreshed after every call).
+  const uint64_t tkey = ((uint64_t)kreq << 56) ^ ((uint64_t)d << 36) ^ ((uint64_t)metric << 32) ^
+                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63);
+  int depth = L;
+  if (margin > 0) {
+    depth = std::min(L, kreq + margin);
+  } else {
+    auto it = ctx->tune.find(tkey);
+    if (it != ctx->tune.end()) depth = (int)it->second;
+  }
+  if (kreq > KREQ_MAX_BF16)
+    return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
+                                     " (k+1 for graphs)");
   const int dp = (d + 7) & ~7;
   const bool self = (qs == base);
 
   // ---- prep
-  const int chunks = (int)std::min<int64_t>(256, std::max<int64_t>(1, n / 512));
-  const int64_t rows_per = ceil_div(n, chunks);
   double* cpart = nullptr;
   float* mu = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_CENTRE, (size_t)chunks * d + (size_t)d + 8, &cpart));
-  MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));
+  MANN_TRY(ctx->scratch_t(SLOT_CENTRE, 64, &cpart));
+  MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));  // mu | BaseMax | scale
   BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + ((d + 31) & ~31));
-  dim3 cg((unsigned)ceil_div(d, 128), (unsigned)chunks);
-  centre_partial_kernel<<<cg, 128, 0, s>>>(base, n, d, rows_per, cpart);
-  MANN_CHECK_LAUNCH();
-  centre_final_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(cpart, chunks, d, n, mu);
-  MANN_CHECK_LAUNCH();
+  {
+    const int64_t rows = std::min<int64_t>(n, 8192);
+    const int64_t stride = n / rows;
+    centre_sample_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(base, n, d, stride, rows, mu);
+    MANN_CHECK_LAUNCH();
+  }
   // pick the centre / scale with the smallest BF16 residual on a row sample
-  double* score = cpart;  // reuse: the partial sums are consumed
+  double* score = cpart;  // probe scores
   MANN_CUDA_TRY(cudaMemsetAsync(score, 0, NUM_SCALES * sizeof(double), s));
   const int64_t sample_rows = std::min<int64_t>(n, 2048);
   const int64_t stride = std::max<int64_t>(1, n / sample_rows);
   dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
   scale_probe_kernel<<<pg, 256, 0, s>>>(base, n, d, mu, stride, score);
   MANN_CHECK_LAUNCH();
-  double h_score[NUM_SCALES];
-  MANN_CUDA_TRY(cudaMemcpyAsync(h_score, score, sizeof(h_score), cudaMemcpyDeviceToHost, s));
-  MANN_CUDA_TRY(cudaStreamSynchronize(s));
-  int best = 0;
-  for (int i = 1; i < NUM_SCALES; ++i)
-    if (h_score[i] < 0.25 * h_score[best]) best = i;  // move off the plain mean only for a clear win
-  const float scale = best == 1 ? 255.0f : 1.0f;
-  if (best != 0) {
-    apply_centre_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(mu, d, best);
-    MANN_CHECK_LAUNCH();
-  }
+  float* scale = reinterpret_cast<float*>(bmax + 1);
+  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale);
+  MANN_CHECK_LAUNCH();
   MANN_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(BaseMax), s));
   Bf16Operand B, Q;
   MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp, &B.xb));
@@ -913,6 +1057,10 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     const int c1 = h_cta_of(qb * tiles + tiles - 1, work, grid);
     smax = std::max(smax, c1 - c0 + 1);
   }
+  // two epilogue sets with 16-entry lists when the tuned depth allows it; each
+  // set writes its own slot
+  const int nsets = depth <= 16 ? 2 : 1;
+  smax *= nsets;
   uint64_t* partial = nullptr;
   int* err = nullptr;
   unsigned long long* counters = nullptr;
@@ -932,29 +1080,28 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ma.grid = grid;
   ma.smax = smax;
   ma.L = L;
+  ma.depth = depth;
   ma.qinfo = Q.info;
   ma.binfo = B.info;
   ma.partial = partial;
   ma.err = err;
-  const size_t smem = main_smem_bytes(L);
+  const size_t smem = nsets == 2 ? k2_smem_bytes(16, 2) : k2_smem_bytes(32, 1);
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
-  if (L == 32) {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nsets == 2) {
+    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ctx->time_begin(s);
-    k2_main<1><<<grid, K2_THREADS, smem, s>>>(mapA, mapB, ma);
+    k2_main<16, 2><<<grid, 64 + 256, smem, s>>>(mapA, mapB, ma);
   } else {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     ctx->time_begin(s);
-    k2_main<2><<<grid, K2_THREADS, smem, s>>>(mapA, mapB, ma);
+    k2_main<32, 1><<<grid, 64 + 128, smem, s>>>(mapA, mapB, ma);
   }
   ctx->time_end(s);
   MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_KEYS, (size_t)nq * L, &lists));
-  if (L == 32)
-    k2_merge<1><<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, lists);
-  else
-    k2_merge<2><<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, lists);
+  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, depth,
+                                                     nsets, lists);
   MANN_CHECK_LAUNCH();
 
   // ---- certify + rerank
@@ -976,6 +1123,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.kreq = kreq;
   ra.metric = metric;
   ra.scale = scale;
+  ra.depth = depth;
+  ra.depth_hist = counters + 16;
   ra.qinfo = Q.info;
   ra.bmax = bmax;
   ra.lists = lists;
@@ -990,10 +1139,30 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
   // ---- exact FP32 scan of uncertified rows (count known only on the device:
   // read it back; the common case is zero rows)
-  int h_fb = 0, h_err = 0;
-  MANN_CUDA_TRY(cudaMemcpyAsync(&h_fb, fb_count, sizeof(int), cudaMemcpyDeviceToHost, s));
-  MANN_CUDA_TRY(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  unsigned long long hc[64];
+  MANN_CUDA_TRY(cudaMemcpyAsync(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  const int h_err = reinterpret_cast<const int*>(hc + 8)[0];
+  const int h_fb = reinterpret_cast<const int*>(hc + 8)[1];
+  if (margin <= 0 && h_err == 0) {
+    // autotune the admission depth from the depths the certificates needed
+    const unsigned long long* hist = hc + 16;
+    unsigned long long total = 0, acc = 0;
+    for (int j = 0; j <= L + 1; ++j) total += hist[j];
+    int want = L;
+    if (hist[L + 1] * 100 > total) {
+      want = L;  // more than 1% fell back at this depth: widen to the full list
+    } else {
+      for (int j = 0; j <= L; ++j) {
+        acc += hist[j];
+        if (acc * 100 >= total * 99) {
+          want = std::min(L, std::max(kreq + 2, j + 1));
+          break;
+        }
+      }
+    }
+    ctx->tune[tkey] = (uint64_t)want;
+  }
   if (h_err != 0)
     return fail(MANN_ETIMEOUT, "tensor-core kernel: a bounded wait ran out (role " + std::to_string(h_err) + ")");
   if (h_fb > 0) {

@@ -42,8 +42,8 @@ def test_bf16_graph_golden(gpu_lib):
     assert np.array_equal(ids64, g["ids_f64"])
 
 
-@pytest.mark.parametrize("n,nq,d,k", [(20000, 700, 128, 10), (9000, 300, 256, 20), (5000, 129, 784, 40),
-                                      (3000, 40, 200, 1), (777, 33, 96, 30)])
+@pytest.mark.parametrize("n,nq,d,k", [(20000, 700, 128, 10), (9000, 300, 256, 20), (5000, 129, 784, 24),
+                                      (3000, 40, 200, 1), (777, 33, 96, 16), (300, 5, 130, 24)])
 def test_bf16_iid_shapes(gpu_lib, orc, n, nq, d, k):
     rng = np.random.default_rng(n + d)
     base = rng.standard_normal((n, d)).astype(np.float32)
@@ -52,8 +52,11 @@ def test_bf16_iid_shapes(gpu_lib, orc, n, nq, d, k):
     ids_o, d_o = orc.knn_f32(base, q, k, orc.SQEUCLIDEAN)
     assert np.array_equal(ids, ids_o)
     assert same_bits(dist, d_o)
-    if d <= 256:  # at d=784 i.i.d. points are nearly equidistant: falling back is expected
-        assert rep["rows_fallback"] <= max(2, nq // 10), rep
+    # i.i.d. Gaussian points are the hard case for BF16 rounding: some rows fall
+    # back to the exact scan (the answer is exact either way); a broken tile
+    # would make every row fall back
+    if d <= 256:
+        assert rep["rows_fallback"] <= max(2, nq // 2), rep
 
 
 def test_bf16_quantized_workload_slice(gpu_lib, orc):
@@ -69,6 +72,18 @@ def test_bf16_quantized_workload_slice(gpu_lib, orc):
     ids64, _ = gpu_knn(base, q, 10, M_SQ, precision="bf16", fp64_ties=True)
     ids_o64, _ = orc.knn_f64(base, q, 10, orc.SQEUCLIDEAN)
     assert np.array_equal(ids64, ids_o64)
+
+
+def test_bf16_rejects_large_k(gpu_lib):
+    import manifoldann_gb300 as M
+
+    rng = np.random.default_rng(0)
+    base = rng.standard_normal((500, 128)).astype(np.float32)
+    with pytest.raises(M.ArgumentError):
+        gpu_knn(base, base[:3], 25, M_SQ, precision="bf16")
+    # automatic choice falls back to the FP32 form for large k
+    ids, _ = gpu_knn(base, base[:3], 40, M_SQ, precision="auto")
+    assert ids.shape == (3, 40)
 
 
 def test_fp32_form_fp64_ties(gpu_lib, orc):
@@ -108,3 +123,21 @@ def test_bf16_full_size_equals_fp32_kernel(gpu_lib):
     assert np.array_equal(g32, gb) and same_bits(gd32, gdb)
     assert not np.any(gb == np.arange(60000)[:, None])
     assert rep["rows_fallback"] <= 120, rep
+
+
+@pytest.mark.parametrize("margin", [0, 4, 6, 20])
+def test_bf16_admission_depth(gpu_lib, orc, margin):
+    # margin 0 = autotuned depth: the first call on a shape runs the full list,
+    # later calls the tuned depth (two epilogue warp sets when it is <= 16);
+    # explicit margins pick the depth directly
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.quantized_mixture(6000, 784, seed=5)
+    q = synthetic.quantized_mixture(300, 784, seed=6)
+    ids_o, d_o = orc.knn_f32(base, q, 10, orc.SQEUCLIDEAN)
+    g_o, gd_o = orc.knn_graph_f32(base[:3000], 10, orc.SQEUCLIDEAN)
+    for _ in range(3):
+        ids, d, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", margin=margin, report=True)
+        assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
+        gi, gd = gpu_graph(base[:3000], 10, M_SQ, precision="bf16", margin=margin)
+        assert np.array_equal(gi, g_o) and same_bits(gd, gd_o)
