@@ -50,8 +50,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--case", choices=["full", "profile"], default="full",
-                    help="profile: only the BF16 search of the 10000 held-out queries against the "
-                         "60000 points, per step (one k2_main launch), for ncu captures")
+                    help="profile: BF16 steps only (query batch + self graph, two k2_main "
+                         "launches per step), for ncu captures")
     return ap.parse_args()
 
 
@@ -175,26 +175,29 @@ def run_reference(args):
 
 
 def run_profile_case(args):
-    """Case for ncu: the BF16 search of the held-out queries against all points."""
+    """Case for ncu: BF16 steps only (the held-out queries, then the self graph)."""
     import torch
 
     from manifoldann_gb300 import _lib
 
     lib = _lib.load()
     base, q = make_workload()
-    nq = N_QUERIES
     tb = torch.from_numpy(base).cuda()
-    tq = torch.from_numpy(q[:nq]).cuda()
-    qi = torch.empty((nq, K), dtype=torch.int32, device="cuda")
-    qd = torch.empty((nq, K), dtype=torch.float32, device="cuda")
+    tq = torch.from_numpy(q).cuda()
+    qi = torch.empty((N_QUERIES, K), dtype=torch.int32, device="cuda")
+    qd = torch.empty((N_QUERIES, K), dtype=torch.float32, device="cuda")
+    gi = torch.empty((N_POINTS, K), dtype=torch.int32, device="cuda")
+    gd = torch.empty((N_POINTS, K), dtype=torch.float32, device="cuda")
     sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_BF16)
     for _ in range(args.warmup + args.steps):
-        _lib.check(lib.mann_knn_device(p, tb.data_ptr(), N_POINTS, tq.data_ptr(), nq, DIM,
+        _lib.check(lib.mann_knn_device(p, tb.data_ptr(), N_POINTS, tq.data_ptr(), N_QUERIES, DIM,
                                        qi.data_ptr(), qd.data_ptr(), None, sp))
+        _lib.check(lib.mann_knn_graph_device(p, tb.data_ptr(), N_POINTS, DIM, 0, gi.data_ptr(),
+                                             gd.data_ptr(), None, sp))
     torch.cuda.synchronize()
-    print(json.dumps({"case": "profile", "queries": nq, "points": N_POINTS, "d": DIM,
-                      "launches_of_k2_main": args.warmup + args.steps}), flush=True)
+    print(json.dumps({"case": "profile", "steps": args.warmup + args.steps,
+                      "k2_main_launches": 2 * (args.warmup + args.steps)}), flush=True)
     return 0
 
 

@@ -78,13 +78,22 @@ struct BaseMax {
 
 // Column means over an evenly spaced sample of rows.  Any centre keeps the
 // distances unchanged; a good one shrinks the BF16 values and their rounding.
+// Block (32 columns x 32 row groups): FP32 partial sums per thread, FP64 across groups.
 __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
                                      int64_t rows, float* __restrict__ mu) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= d) return;
-  double s = 0.0;
-  for (int64_t i = 0; i < rows; ++i) s += (double)x[(i * stride) * d + c];
-  mu[c] = (float)(s / (double)rows);
+  __shared__ double part[32][33];
+  const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + cl;
+  float s = 0.0f;
+  if (c < d)
+    for (int64_t i = g; i < rows; i += 32) s += x[(i * stride) * d + c];
+  part[g][cl] = (double)s;
+  __syncthreads();
+  if (g == 0 && c < d) {
+    double t = 0.0;
+    for (int i = 0; i < 32; ++i) t += part[i][cl];
+    mu[c] = (float)(t / (double)rows);
+  }
 }
 
 __device__ __forceinline__ float round_up_f(double v) {
@@ -250,54 +259,20 @@ __device__ __forceinline__ void wl_insert(uint64_t (&Lr)[KW], uint64_t c, int la
   }
 }
 
-// ---- warp-cooperative helpers on a 32-entry sorted list (lane i holds entry i)
-__device__ __forceinline__ uint64_t shfl_xor_u64(uint64_t v, int m) {
-  return (uint64_t)__shfl_xor_sync(FULL, (unsigned long long)v, m);
-}
-
-// ascending bitonic sort of one key per lane
-__device__ __forceinline__ uint64_t warp_sort32(uint64_t x, int lane) {
-#pragma unroll
-  for (int k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const uint64_t y = shfl_xor_u64(x, j);
-      const bool up = (lane & k) == 0 || k == 32;
-      const bool lower = (lane & j) == 0;
-      x = (lower == up) ? min(x, y) : max(x, y);
-    }
-  }
-  return x;
-}
-
-// lane i: i-th smallest of the union of two ascending 32-lists
-__device__ __forceinline__ uint64_t warp_merge32(uint64_t a, uint64_t b_sorted, int lane) {
-  const uint64_t br = __shfl_sync(FULL, (unsigned long long)b_sorted, 31 - lane);
-  uint64_t x = min(a, br);  // bitonic
-#pragma unroll
-  for (int j = 16; j > 0; j >>= 1) {
-    const uint64_t y = shfl_xor_u64(x, j);
-    x = ((lane & j) == 0) ? min(x, y) : max(x, y);
-  }
-  return x;
-}
-
-// One 32-column chunk of the epilogue for a warp's 32 rows.  v: this lane's
-// row (32 accumulators), nb: the chunk's point norms, tw: 32 x TSTR transpose
-// buffer, thr: per-row admission threshold (est' of the depth-th entry),
-// lists: the warp's row lists (entry e of row r at lists[r * CAP + e]).
-// Lane r first tests its own row; only rows with candidates go through the
-// transpose, where the whole warp folds them into the row's list.
-template <int CAP>
+// One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
+// rows: v holds the row's 32 accumulators of the chunk, nb the chunk's point
+// norms.  The row's list lives in shared memory, entry e at mylist[e * BM],
+// sorted by key; thr_key is its depth-th entry (KEY_NONE until full) and
+// thr_est that entry's est'.  The common case -- no column of any row below
+// its threshold -- costs one FMA and one min per value and one vote; a lane
+// with candidates stashes its row in trow and inserts them one by one.
 __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* __restrict__ nb,
-                                          float* __restrict__ tw, float* __restrict__ thr,
-                                          uint64_t* __restrict__ lists, uint32_t col0, int lane,
+                                          float* __restrict__ trow, uint64_t* __restrict__ mylist,
+                                          uint64_t& thr_key, float& thr_est, uint32_t col0,
                                           int depth) {
-  const float INF = __int_as_float(0x7F800000);
   const float4* nb4 = reinterpret_cast<const float4*>(nb);
-  const float t_own = thr[lane];
   float e[32];
-  unsigned mask = 0;
+  float mn = __int_as_float(0x7F800000);
 #pragma unroll
   for (int j4 = 0; j4 < 8; ++j4) {
     const float4 n4 = nb4[j4];
@@ -305,56 +280,44 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* 
     e[4 * j4 + 1] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 1]), n4.y);
     e[4 * j4 + 2] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 2]), n4.z);
     e[4 * j4 + 3] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 3]), n4.w);
+    mn = fminf(mn, fminf(fminf(e[4 * j4 + 0], e[4 * j4 + 1]), fminf(e[4 * j4 + 2], e[4 * j4 + 3])));
   }
+  if (!__any_sync(FULL, mn < thr_est)) return;
+  if (mn < thr_est) {
+    unsigned mask = 0;
+    float4* t4 = reinterpret_cast<float4*>(trow);
 #pragma unroll
-  for (int j = 0; j < 32; ++j) mask |= (e[j] < t_own) ? (1u << j) : 0u;
-  unsigned rows = __ballot_sync(FULL, mask != 0);
-  if (rows == 0) return;
-  if (mask) {
-    float4* trow = reinterpret_cast<float4*>(tw + lane * TSTR);
+    for (int j4 = 0; j4 < 8; ++j4) {
+      t4[j4] = make_float4(e[4 * j4 + 0], e[4 * j4 + 1], e[4 * j4 + 2], e[4 * j4 + 3]);
 #pragma unroll
-    for (int j4 = 0; j4 < 8; ++j4)
-      trow[j4] = make_float4(e[4 * j4 + 0], e[4 * j4 + 1], e[4 * j4 + 2], e[4 * j4 + 3]);
-  }
-  __syncwarp();
-  const uint32_t mycol = col0 + (uint32_t)lane;
-  while (rows) {
-    const int r = __ffs(rows) - 1;
-    rows &= rows - 1;
-    unsigned m = __shfl_sync(FULL, mask, r);
-    const float x = tw[r * TSTR + lane];
-    uint64_t key = ((m >> lane) & 1u) ? make_key(x, mycol) : KEY_NONE;
-    uint64_t Lr = lane < CAP ? lists[r * CAP + lane] : KEY_NONE;
-    if (__popc(m) > 3) {
-      key = warp_sort32(key, lane);
-      Lr = warp_merge32(Lr, key, lane);
-    } else {
-      uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
-      while (m) {
-        const int b = __ffs(m) - 1;
-        m &= m - 1;
-        const uint64_t c = __shfl_sync(FULL, (unsigned long long)key, b);
-        if (c < tk) {
-          uint64_t one[1] = {Lr};
-          wl_insert<1>(one, c, lane);
-          Lr = one[0];
-          tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+      for (int u = 0; u < 4; ++u) mask |= (e[4 * j4 + u] < thr_est ? 1u : 0u) << (4 * j4 + u);
+    }
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const uint64_t c = make_key(trow[j], col0 + (uint32_t)j);
+      if (c < thr_key) {
+        // sorted insertion from the end; the depth-th entry drops out
+        int p = depth - 1;
+        while (p > 0) {
+          const uint64_t prev = mylist[(p - 1) * BM];
+          if (prev < c) break;
+          mylist[p * BM] = prev;
+          --p;
         }
+        mylist[p * BM] = c;
+        thr_key = mylist[(depth - 1) * BM];
+        thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
       }
     }
-    if (lane < CAP) lists[r * CAP + lane] = Lr;
-    const uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
-    if (lane == r) thr[r] = (tk == KEY_NONE) ? INF : key_dist(tk);
   }
-  __syncwarp();
 }
 
 // Shared-memory footprint of k2_main<CAP, NSETS>.
 __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
   return 1024 /* alignment */ + (size_t)STAGES * STAGE_BYTES +
-         (size_t)nsets * BM * cap * 8 /* lists */ + (size_t)nsets * 4 * 32 * TSTR * 4 /* transpose */ +
-         (size_t)nsets * 4 * 32 * 4 /* thresholds */ + (size_t)nsets * 4 * BN * 4 /* norms */ +
-         (2 * STAGES + 4) * 8 + 16;
+         (size_t)nsets * BM * cap * 8 /* lists */ + (size_t)nsets * 4 * 32 * TSTR * 4 /* row buffers */ +
+         (size_t)nsets * 4 * BN * 4 /* norms */ + (2 * STAGES + 4) * 8 + 16;
 }
 
 // The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
@@ -377,10 +340,9 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(k2_smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* stage_base = smem;                                                   // STAGES * 48 KB
-  uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [NSETS][BM][CAP]
+  uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [NSETS][CAP][BM]
   float* trans = reinterpret_cast<float*>(lists + NSETS * BM * CAP);            // [NEPI][32][TSTR]
-  float* thrs = trans + NEPI * 32 * TSTR;                                        // [NEPI][32]
-  float* nbs = thrs + NEPI * 32;                                                 // [NEPI][BN]
+  float* nbs = trans + NEPI * 32 * TSTR;                                         // [NEPI][BN]
   uint64_t* bars = reinterpret_cast<uint64_t*>(nbs + NEPI * BN);
   uint64_t* full_bar = bars;
   uint64_t* empty_bar = bars + STAGES;
@@ -478,36 +440,35 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     const int ew = warp - 2;          // 0 .. NEPI-1
     const int set = ew >> 2;          // which accumulator buffer this warp drains (two sets)
     const int quad = warp & 3;        // TMEM lane quadrant this warp may access
+    const int row = quad * 32 + lane; // this lane's row of the 128-query tile
     float* nbw = nbs + ew * BN;       // point norms of the current tile
-    float* tw = trans + ew * (32 * TSTR);
-    float* thrw = thrs + ew * 32;     // est' of each row's depth-th entry (+inf until full)
-    uint64_t* lw = lists + (size_t)set * BM * CAP + quad * 32 * CAP;  // lw[r * CAP + e]
+    float* trow = trans + (ew * 32 + lane) * TSTR;            // this lane's row buffer
+    uint64_t* mylist = lists + (size_t)set * CAP * BM + row;  // entry e at mylist[e * BM]
     const float INF = __int_as_float(0x7F800000);
+    uint64_t thr_key = KEY_NONE;
+    float thr_est = INF;
     int tcount = 0;
     int cur_qb = -1;
     int seg_first_cta = 0;
     bool alive = true;
 
-    thrw[lane] = INF;
-    for (int r = 0; r < 32; ++r)
-      if (lane < CAP) lw[r * CAP + lane] = KEY_NONE;
-    __syncwarp();
+    for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
 
     for (int64_t item = it0; item < it1; ++item, ++tcount) {
       const int qb = (int)(item / a.tiles);
       const int t = (int)(item % a.tiles);
       if (qb != cur_qb) {
         if (cur_qb >= 0) {
-          // flush the finished segment's lists (every set, even one that saw no tile)
+          // flush the finished segment's list (every set, even one that saw no tile)
           const int slot = (cta - seg_first_cta) * NSETS + set;
-          for (int r = 0; r < 32; ++r) {
-            const int64_t gq = (int64_t)cur_qb * BM + quad * 32 + r;
-            const uint64_t v = lane < CAP ? lw[r * CAP + lane] : KEY_NONE;
-            if (gq < a.nq) a.partial[(gq * a.smax + slot) * LIST + lane] = v;
-            if (lane < CAP) lw[r * CAP + lane] = KEY_NONE;
+          const int64_t gq = (int64_t)cur_qb * BM + row;
+          uint64_t* dst = a.partial + (gq * a.smax + slot) * LIST;
+          for (int e = 0; e < CAP; ++e) {
+            if (gq < a.nq) dst[e] = mylist[e * BM];
+            mylist[e * BM] = KEY_NONE;
           }
-          thrw[lane] = INF;
-          __syncwarp();
+          thr_key = KEY_NONE;
+          thr_est = INF;
         }
         cur_qb = qb;
         seg_first_cta = cta_of((int64_t)qb * a.tiles, a.work, a.grid);
@@ -515,6 +476,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       const int buf = tcount & 1;
       if (NSETS == 2 && buf != set) continue;
       const int64_t col0 = (int64_t)t * BN;
+      __syncwarp();
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) {
         const int64_t col = col0 + lane + 32 * i;
@@ -535,14 +497,15 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        epi_chunk<CAP>(va, nbw + ch * 32, tw, thrw, lw, (uint32_t)(col0 + ch * 32), lane, a.depth);
+        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, (uint32_t)(col0 + ch * 32),
+                  a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < BN / 32) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
           ptx::tmem_ld16(taddr + (ch + 2) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
         }
-        epi_chunk<CAP>(vb, nbw + (ch + 1) * 32, tw, thrw, lw, (uint32_t)(col0 + (ch + 1) * 32),
-                       lane, a.depth);
+        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est,
+                  (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
       ptx::tc_fence_before();
@@ -550,11 +513,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     }
     if (alive && cur_qb >= 0) {
       const int slot = (cta - seg_first_cta) * NSETS + set;
-      for (int r = 0; r < 32; ++r) {
-        const int64_t gq = (int64_t)cur_qb * BM + quad * 32 + r;
-        const uint64_t v = lane < CAP ? lw[r * CAP + lane] : KEY_NONE;
-        if (gq < a.nq) a.partial[(gq * a.smax + slot) * LIST + lane] = v;
-      }
+      const int64_t gq = (int64_t)cur_qb * BM + row;
+      uint64_t* dst = a.partial + (gq * a.smax + slot) * LIST;
+      if (gq < a.nq)
+        for (int e = 0; e < CAP; ++e) dst[e] = mylist[e * BM];
     }
   }
 
@@ -1012,15 +974,15 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));  // mu | BaseMax | scale
   BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + ((d + 31) & ~31));
   {
-    const int64_t rows = std::min<int64_t>(n, 8192);
+    const int64_t rows = std::min<int64_t>(n, 4096);
     const int64_t stride = n / rows;
-    centre_sample_kernel<<<(unsigned)ceil_div(d, 128), 128, 0, s>>>(base, n, d, stride, rows, mu);
+    centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(base, n, d, stride, rows, mu);
     MANN_CHECK_LAUNCH();
   }
   // pick the centre / scale with the smallest BF16 residual on a row sample
   double* score = cpart;  // probe scores
   MANN_CUDA_TRY(cudaMemsetAsync(score, 0, NUM_SCALES * sizeof(double), s));
-  const int64_t sample_rows = std::min<int64_t>(n, 2048);
+  const int64_t sample_rows = std::min<int64_t>(n, 1024);
   const int64_t stride = std::max<int64_t>(1, n / sample_rows);
   dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
   scale_probe_kernel<<<pg, 256, 0, s>>>(base, n, d, mu, stride, score);
@@ -1150,13 +1112,16 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     unsigned long long total = 0, acc = 0;
     for (int j = 0; j <= L + 1; ++j) total += hist[j];
     int want = L;
-    if (hist[L + 1] * 100 > total) {
-      want = L;  // more than 1% fell back at this depth: widen to the full list
+    if (hist[L + 1] * 1000 > total) {
+      want = L;  // more than 0.1% fell back at this depth: widen to the full list
     } else {
       for (int j = 0; j <= L; ++j) {
         acc += hist[j];
-        if (acc * 100 >= total * 99) {
+        if (acc * 1000 >= total * 999) {
+          // the 99.9th percentile + 1; anything up to 16 runs the 16-entry
+          // two-set kernel, so take all 16 there (fewer exact-scan fallbacks)
           want = std::min(L, std::max(kreq + 2, j + 1));
+          if (want <= 16) want = 16;
           break;
         }
       }

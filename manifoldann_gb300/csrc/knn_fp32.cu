@@ -406,6 +406,13 @@ template <int METRIC, bool VEC>
 mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const float* qs, const int32_t* rows,
                         int64_t nq, int d, const float* qn, const float* bn, int64_t split_len,
                         int nsplit, uint64_t* partial, cudaStream_t s) {
+  if (nq <= 32) {  // a handful of queries (e.g. rows re-run by the exact scan): narrow tiles
+    if (k <= 32)
+      return launch_k1<METRIC, 32, 1, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len,
+                                           nsplit, partial, s);
+    return launch_k1<METRIC, 32, 8, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len,
+                                         nsplit, partial, s);
+  }
   if (k <= 32)
     return launch_k1<METRIC, 128, 1, VEC>(ctx, base, n, qs, rows, nq, d, qn, bn, k, split_len, nsplit,
                                           partial, s);
@@ -446,7 +453,7 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (nq <= 0) return MANN_OK;
   if (metric == MANN_METRIC_COSINE && (qn == nullptr || bn == nullptr))
     return fail(MANN_EINVAL_ARG, "cosine search needs row norms");
-  const int bq = kk <= 64 ? 128 : (kk <= 128 ? 64 : 32);
+  const int bq = nq <= 32 ? 32 : (kk <= 64 ? 128 : (kk <= 128 ? 64 : 32));
   const int64_t qblocks = ceil_div(nq, bq);
   const int64_t tiles = ceil_div(n, K1_BN);
   // Split the points so that the grid covers the SMs at least once.
