@@ -35,6 +35,9 @@ enum ScratchSlot : int {
   SLOT_MISC2,
   SLOT_MISC3,
   SLOT_OUT_KEYS_BF16, // final sorted keys of the BF16 form
+  SLOT_SEED_PARTIAL,  // seed pass: per-CTA lists
+  SLOT_SEED_LISTS,    // seed pass: merged lists
+  SLOT_SEED,          // per-query admission seeds
   SLOT_COUNT
 };
 

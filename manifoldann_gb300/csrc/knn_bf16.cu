@@ -56,7 +56,8 @@ constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int K2_THREADS = 64 + NUM_EPI_WARPS * 32;  // producer, MMA, 4 epilogue warps
 constexpr int LIST = 32;                             // candidates kept per query row
-constexpr int TSTR = 36;                             // row stride of the 32x32 transpose (floats)
+constexpr int TSTR = 36;                             // row stride of the per-lane row buffers (floats)
+constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
 
@@ -222,6 +223,8 @@ struct MainArgs {
   int depth;          // admission depth = k + margin (<= L)
   const RowInfo* qinfo;
   const RowInfo* binfo;
+  int64_t bstride;    // point p of this launch is row p * bstride of binfo (sampled passes)
+  const float* seed;  // per query: admit only est' below this (NULL = no seed)
   uint64_t* partial;  // [nq][smax][L]
   int* err;
 };
@@ -262,14 +265,14 @@ __device__ __forceinline__ void wl_insert(uint64_t (&Lr)[KW], uint64_t c, int la
 // One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
 // rows: v holds the row's 32 accumulators of the chunk, nb the chunk's point
 // norms.  The row's list lives in shared memory, entry e at mylist[e * BM],
-// sorted by key; thr_key is its depth-th entry (KEY_NONE until full) and
-// thr_est that entry's est'.  The common case -- no column of any row below
+// sorted by key; thr_key is its depth-th entry, or the row's seed key
+// (seed est', id 0) until the list is full, and thr_est that key's est'.  The common case -- no column of any row below
 // its threshold -- costs one FMA and one min per value and one vote; a lane
 // with candidates stashes its row in trow and inserts them one by one.
 __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* __restrict__ nb,
                                           float* __restrict__ trow, uint64_t* __restrict__ mylist,
-                                          uint64_t& thr_key, float& thr_est, uint32_t col0,
-                                          int depth) {
+                                          uint64_t& thr_key, float& thr_est, uint64_t seed_key,
+                                          uint32_t col0, int depth) {
   const float4* nb4 = reinterpret_cast<const float4*>(nb);
   float e[32];
   float mn = __int_as_float(0x7F800000);
@@ -306,7 +309,8 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* 
           --p;
         }
         mylist[p * BM] = c;
-        thr_key = mylist[(depth - 1) * BM];
+        const uint64_t last = mylist[(depth - 1) * BM];
+        thr_key = last == KEY_NONE ? seed_key : last;
         thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
       }
     }
@@ -445,6 +449,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     float* trow = trans + (ew * 32 + lane) * TSTR;            // this lane's row buffer
     uint64_t* mylist = lists + (size_t)set * CAP * BM + row;  // entry e at mylist[e * BM]
     const float INF = __int_as_float(0x7F800000);
+    uint64_t seed_key = KEY_NONE;
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
     int tcount = 0;
@@ -467,11 +472,13 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             if (gq < a.nq) dst[e] = mylist[e * BM];
             mylist[e * BM] = KEY_NONE;
           }
-          thr_key = KEY_NONE;
-          thr_est = INF;
         }
         cur_qb = qb;
         seg_first_cta = cta_of((int64_t)qb * a.tiles, a.work, a.grid);
+        const int64_t gq = (int64_t)qb * BM + row;
+        seed_key = (a.seed != nullptr && gq < a.nq) ? make_key(a.seed[gq], 0u) : KEY_NONE;
+        thr_key = seed_key;
+        thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
       }
       const int buf = tcount & 1;
       if (NSETS == 2 && buf != set) continue;
@@ -480,7 +487,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) {
         const int64_t col = col0 + lane + 32 * i;
-        nbw[lane + 32 * i] = col < a.n ? __ldg(&a.binfo[col].nrm) : INF;
+        nbw[lane + 32 * i] = col < a.n ? __ldg(&a.binfo[col * a.bstride].nrm) : INF;
       }
       __syncwarp();
       const uint32_t tph = (tcount >> 1) & 1;
@@ -497,14 +504,14 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, (uint32_t)(col0 + ch * 32),
-                  a.depth);
+        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, seed_key,
+                  (uint32_t)(col0 + ch * 32), a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < BN / 32) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
           ptx::tmem_ld16(taddr + (ch + 2) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
         }
-        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est,
+        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est, seed_key,
                   (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
@@ -565,6 +572,7 @@ struct RerankArgs {
   const float* qs;
   int64_t nq, n;
   int d, L, kreq, metric, depth;
+  const float* seed;   // per query admission seed of the main pass (NULL = none)
   const float* scale;  // the est values are in units of scale^2 * distance
   unsigned long long* depth_hist;  // [LIST + 2]: rows by the list depth their certificate needed
   const RowInfo* qinfo;
@@ -637,8 +645,14 @@ __global__ void k2_rerank(RerankArgs a) {
   const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
   const double sc = (double)*a.scale;
   double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
-  const bool all_in = (last_key == KEY_NONE);  // the list holds every point
-  const bool certified = all_in || (double)key_dist(last_key) + qn > T;
+  // Every point outside the merged list has est' >= its depth-th entry, or >=
+  // the seed when the list is not full; with neither, the list holds every point.
+  const float sd = a.seed ? a.seed[q] : __int_as_float(0x7F800000);
+  const bool all_in = (last_key == KEY_NONE) && !(sd < 3.0e38f);
+  const double beyond = last_key != KEY_NONE ? (double)key_dist(last_key) : (double)sd;
+  // without the row's k-th estimate (fewer than k points admitted below the
+  // seed) the threshold is unknown: the row is not certified
+  const bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
   {
     // depth this row's certificate needs: one past its last est <= T entry
     const uint64_t kl = lst[lane];
@@ -913,11 +927,13 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-mann_status make_map(CUtensorMap* m, const void* ptr, int64_t rows, int dp, int box_rows) {
+// rows of dp BF16 values; row r of the map is row r * row_step of the buffer
+mann_status make_map(CUtensorMap* m, const void* ptr, int64_t rows, int dp, int box_rows,
+                     int64_t row_step = 1) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return fail(MANN_ECUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[2] = {(cuuint64_t)dp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)dp * 2};
+  cuuint64_t strides[1] = {(cuuint64_t)dp * 2 * (cuuint64_t)row_step};
   cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
   CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box,
@@ -933,6 +949,77 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
   while (c + 1 < grid && h_chunk(c + 1, work, grid) <= i) ++c;
   while (c > 0 && h_chunk(c, work, grid) > i) --c;
   return c;
+}
+
+// One tensor-core pass (k2_main + k2_merge): the `depth` smallest est' of
+// every query over n points (binfo row p * bstride), as sorted lists [nq][LIST].
+mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
+                          const CUtensorMap& mapB, const RowInfo* qinfo, const RowInfo* binfo,
+                          int64_t bstride, int64_t n, int64_t nq, int d, int dp, int depth,
+                          const float* seed, int* err, int slot_partial, int slot_lists, bool timed,
+                          uint64_t** lists_out) {
+  const int64_t qblocks = ceil_div(nq, BM);
+  const int tiles = (int)ceil_div(n, BN);
+  const int64_t work = qblocks * tiles;
+  const int grid = (int)std::min<int64_t>(ctx->num_sms, work);
+  int smax = 1;
+  for (int64_t qb = 0; qb < qblocks; ++qb) {
+    const int c0 = h_cta_of(qb * tiles, work, grid);
+    const int c1 = h_cta_of(qb * tiles + tiles - 1, work, grid);
+    smax = std::max(smax, c1 - c0 + 1);
+  }
+  // two epilogue sets with 16-entry lists when the depth allows it; each set
+  // writes its own slot
+  const int nsets = depth <= 16 ? 2 : 1;
+  smax *= nsets;
+  uint64_t* partial = nullptr;
+  MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * smax * LIST, &partial));
+  MainArgs ma;
+  ma.nq = nq;
+  ma.n = n;
+  ma.d = d;
+  ma.dp = dp;
+  ma.nkb = (int)ceil_div(dp, BK);
+  ma.tiles = tiles;
+  ma.work = work;
+  ma.grid = grid;
+  ma.smax = smax;
+  ma.L = LIST;
+  ma.depth = depth;
+  ma.qinfo = qinfo;
+  ma.binfo = binfo;
+  ma.bstride = bstride;
+  ma.seed = seed;
+  ma.partial = partial;
+  ma.err = err;
+  const size_t smem = nsets == 2 ? k2_smem_bytes(16, 2) : k2_smem_bytes(32, 1);
+  if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
+  if (nsets == 2) {
+    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (timed) ctx->time_begin(s);
+    k2_main<16, 2><<<grid, 64 + 256, smem, s>>>(mapA, mapB, ma);
+  } else {
+    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (timed) ctx->time_begin(s);
+    k2_main<32, 1><<<grid, 64 + 128, smem, s>>>(mapA, mapB, ma);
+  }
+  if (timed) ctx->time_end(s);
+  MANN_CHECK_LAUNCH();
+  uint64_t* lists = nullptr;
+  MANN_TRY(ctx->scratch_t(slot_lists, (size_t)nq * LIST, &lists));
+  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, depth,
+                                                     nsets, lists);
+  MANN_CHECK_LAUNCH();
+  *lists_out = lists;
+  return MANN_OK;
+}
+
+__global__ void seed_from_lists_kernel(const uint64_t* __restrict__ lists, int64_t nq, int e,
+                                       float* __restrict__ seed) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  const uint64_t k = lists[q * LIST + e];
+  seed[q] = k == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(k);
 }
 
 }  // namespace
@@ -1005,66 +1092,40 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     MANN_CHECK_LAUNCH();
   }
 
-  // ---- main
-  CUtensorMap mapA, mapB;
-  MANN_TRY(make_map(&mapA, Q.xb, nq, dp, BM));
-  MANN_TRY(make_map(&mapB, B.xb, n, dp, BN));
-  const int64_t qblocks = ceil_div(nq, BM);
-  const int tiles = (int)ceil_div(n, BN);
-  const int64_t work = qblocks * tiles;
-  const int grid = (int)std::min<int64_t>(ctx->num_sms, work);
-  int smax = 1;
-  for (int64_t qb = 0; qb < qblocks; ++qb) {
-    const int c0 = h_cta_of(qb * tiles, work, grid);
-    const int c1 = h_cta_of(qb * tiles + tiles - 1, work, grid);
-    smax = std::max(smax, c1 - c0 + 1);
-  }
-  // two epilogue sets with 16-entry lists when the tuned depth allows it; each
-  // set writes its own slot
-  const int nsets = depth <= 16 ? 2 : 1;
-  smax *= nsets;
-  uint64_t* partial = nullptr;
-  int* err = nullptr;
+  // ---- counters: [2] candidates, [4..5] resolve, [8] error word + fallback
+  // count (as ints), [16..49] depth histogram
   unsigned long long* counters = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_PARTIAL, (size_t)nq * smax * L, &partial));
   MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
-  err = reinterpret_cast<int*>(counters + 8);
+  int* err = reinterpret_cast<int*>(counters + 8);
   int* fb_count = err + 1;
   MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
-  MainArgs ma;
-  ma.nq = nq;
-  ma.n = n;
-  ma.d = d;
-  ma.dp = dp;
-  ma.nkb = (int)ceil_div(dp, BK);
-  ma.tiles = tiles;
-  ma.work = work;
-  ma.grid = grid;
-  ma.smax = smax;
-  ma.L = L;
-  ma.depth = depth;
-  ma.qinfo = Q.info;
-  ma.binfo = B.info;
-  ma.partial = partial;
-  ma.err = err;
-  const size_t smem = nsets == 2 ? k2_smem_bytes(16, 2) : k2_smem_bytes(32, 1);
-  if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
-  if (nsets == 2) {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ctx->time_begin(s);
-    k2_main<16, 2><<<grid, 64 + 256, smem, s>>>(mapA, mapB, ma);
-  } else {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ctx->time_begin(s);
-    k2_main<32, 1><<<grid, 64 + 128, smem, s>>>(mapA, mapB, ma);
+
+  CUtensorMap mapA;
+  MANN_TRY(make_map(&mapA, Q.xb, nq, dp, BM));
+
+  // ---- seed pass: the 5th smallest est' of each query over an evenly spaced
+  // sample of SEED_SAMPLE points becomes its admission seed in the main pass
+  // (roughly its 5n/SEED_SAMPLE-th neighbour), which spares most insertions.
+  // A seed below the row's k-th estimate leaves the row uncertified.
+  float* seed = nullptr;
+  if (n >= 16 * SEED_SAMPLE) {
+    const int64_t bstride = n / SEED_SAMPLE;
+    CUtensorMap mapS;
+    MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dp, BN, bstride));
+    uint64_t* slists = nullptr;
+    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, bstride, SEED_SAMPLE, nq, d, dp, 5,
+                           nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists));
+    MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
+    seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, 4, seed);
+    MANN_CHECK_LAUNCH();
   }
-  ctx->time_end(s);
-  MANN_CHECK_LAUNCH();
+
+  // ---- main pass over every point
+  CUtensorMap mapB;
+  MANN_TRY(make_map(&mapB, B.xb, n, dp, BN));
   uint64_t* lists = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_KEYS, (size_t)nq * L, &lists));
-  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, depth,
-                                                     nsets, lists);
-  MANN_CHECK_LAUNCH();
+  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, 1, n, nq, d, dp, depth, seed, err,
+                         SLOT_PARTIAL, SLOT_KEYS, true, &lists));
 
   // ---- certify + rerank
   uint64_t* cand = nullptr;
@@ -1086,6 +1147,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.metric = metric;
   ra.scale = scale;
   ra.depth = depth;
+  ra.seed = seed;
   ra.depth_hist = counters + 16;
   ra.qinfo = Q.info;
   ra.bmax = bmax;
@@ -1153,7 +1215,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     rep->candidates = (int64_t)h[2];
     rep->rows_fp64_ties = (int64_t)h[4];
     rep->precision_used = MANN_PREC_BF16;
-    rep->margin_used = L - kreq;
+    rep->margin_used = depth - kreq;
   }
   *out_keys = keys;
   return MANN_OK;

@@ -141,3 +141,15 @@ def test_bf16_admission_depth(gpu_lib, orc, margin):
         assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
         gi, gd = gpu_graph(base[:3000], 10, M_SQ, precision="bf16", margin=margin)
         assert np.array_equal(gi, g_o) and same_bits(gd, gd_o)
+
+
+def test_bf16_seeded_pass(gpu_lib, orc):
+    # n >= 32768 points switches on the sampled seed pass; the answer must not change
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.anisotropic_clusters(40000, 128, seed=3, clusters=256)
+    q = synthetic.anisotropic_clusters(300, 128, seed=4, clusters=256)
+    ids_o, d_o = orc.knn_f32(base, q, 10, orc.SQEUCLIDEAN)
+    for _ in range(3):
+        ids, d, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", report=True)
+        assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
