@@ -108,6 +108,23 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
                                   int32_t d, int32_t include_self, int32_t* out_ids,
                                   float* out_dists, mann_knn_report* report, void* stream);
 
+/* Exact kNN in the FP32 form for callers that cannot allocate device memory.
+ * No counterpart in the reference: it is an addition of this library for
+ * hosts that own all device memory through their own pool (a Julia or Python
+ * runtime that reserved the GPU's memory), code that must not stall the
+ * device with cudaMalloc/cudaFree (both synchronise it), and callers that
+ * must not run out of memory mid-job.  Arguments as mann_knn_device (device
+ * pointers; precision FP32 or AUTO, no MANN_FLAG_FP64_TIES).  It allocates
+ * nothing: its scratch is one 16 MiB array the library holds on every device
+ * it is loaded on until exit; a search that needs more is rejected with
+ * MANN_EINVAL_ARG (pass fewer queries per call).  The first call on a device
+ * looks up that array's address and should come before any stream capture.
+ * All calls on a device share the array, so calls that overlap on the GPU
+ * race: serialise them. */
+mann_status mann_knn_device_noalloc(const mann_knn_params* p, const float* base, int64_t n,
+                                    const float* queries, int64_t q, int32_t d, int32_t* out_ids,
+                                    float* out_dists, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

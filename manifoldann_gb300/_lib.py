@@ -89,6 +89,7 @@ SIGNATURES = {
     "mann_knn_graph": (_I32, [C.POINTER(KnnParams), _P, _I64, _I32, _I32, _P, _P, C.POINTER(KnnReport)]),
     "mann_knn_graph_device": (_I32, [C.POINTER(KnnParams), _P, _I64, _I32, _I32, _P, _P,
                                      C.POINTER(KnnReport), _P]),
+    "mann_knn_device_noalloc": (_I32, [C.POINTER(KnnParams), _P, _I64, _P, _I64, _I32, _P, _P, _P]),
 }
 
 _lib = None

@@ -46,6 +46,14 @@ mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, c
                               int64_t n, int64_t nq, int d, int metric, int kk, int kreq,
                               const uint64_t* fkeys, uint64_t** out_keys, mann_knn_report* rep);
 
+// Plan and scratch-free variant of knn_fp32_keys (caller supplies `words`
+// uint64 of device scratch).
+void knn_fp32_plan(int num_sms, int64_t n, int64_t nq, int kk, int* nsplit_out, size_t* words_out);
+mann_status knn_fp32_keys_on(int num_sms, cudaStream_t s, const float* base, int64_t n,
+                             const float* qs, int64_t nq, int d, int metric, int kk,
+                             const float* qn, const float* bn, uint64_t* scratch, size_t words,
+                             uint64_t** out_keys);
+
 // Largest k handled by the fused top-k kernels.
 constexpr int KMAX_FUSED = 256;
 
