@@ -43,7 +43,7 @@ METRIC = "kNN queries/s (BF16+rerank exact kNN at recall@10=1.0)"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp32-steps", type=int, default=2)
@@ -121,6 +121,16 @@ def measured_peaks():
         j = json.loads(p.read_text())
         return j.get("bf16_tflops_sustained", 1737.1), j.get("hbm_gbs", 6703.5), "measured"
     return 1700.0, 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per k2_main main-pass launch from the committed ncu summary."""
+    p = ROOT / "profiles" / "k2_main_bf16_knn_60k_784.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1].split()[0])
+    return None
 
 
 def cpu_baseline(base, q, budget_s):
@@ -316,11 +326,12 @@ def run_ours(args):
         return 0
 
     peak_tf, hbm, peak_src = measured_peaks()
+    traffic = profiled_traffic()
     flops_step = 2.0 * DIM * N_POINTS * (N_QUERIES + N_POINTS)
     launches_per_step_main = 2
     achieved_tf = flops_step * args.steps / (kernel_ms / 1e3) / 1e12 if kernel_ms > 0 else None
     roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-            "frac": (achieved_tf / peak_tf) if achieved_tf else None, "traffic": None,
+            "frac": (achieved_tf / peak_tf) if achieved_tf else None, "traffic": traffic,
             "peak_source": f"{peak_src} bf16 dense (sustained)", "kernel": "k2_main (tcgen05 BF16 tiles + fused top-(k+m))",
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step_main)}
     cpu = cpu_baseline(base, q, args.cpu_seconds) if args.cpu_seconds > 0 else None

@@ -108,6 +108,45 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
                                   int32_t d, int32_t include_self, int32_t* out_ids,
                                   float* out_dists, mann_knn_report* report, void* stream);
 
+/* ------------------------------------------------------------ KMeans (KMeansTransform) */
+
+typedef struct {
+  int32_t k;          /* clusters */
+  int32_t metric;     /* MANN_METRIC_EUCLIDEAN or MANN_METRIC_SQEUCLIDEAN */
+  int32_t init;       /* 0 random points, 1 k-means++ */
+  int32_t max_iters;  /* Lloyd iterations (> 0) */
+  double tol;         /* stop when the largest centroid movement is below tol */
+  int64_t subsample;  /* > 0 and < n: Lloyd on that many random points, then a full assignment */
+  uint64_t seed;      /* seed of the library's own generator (Julia's streams are not reproduced) */
+} mann_kmeans_params;
+
+/* D[n][k] = dist(X[i], C[j]) -- pairwise_distances! (src/transforms/kmeans/distance.jl:28-165).
+ * Julia's k x n matrix D has the same bytes as this [n][k] array. */
+mann_status mann_pairwise_distances(const float* X, int64_t n, const float* C, int32_t k, int32_t d,
+                                    int32_t metric, float* D);
+
+/* Nearest centroid of every point -- assign_clusters! on pairwise distances
+ * (distance.jl:287-310): the exact arg-min (near-ties ordered in FP64, lowest
+ * centroid id on exact ties), 0-based; out_dist (nullable) = its distance. */
+mann_status mann_kmeans_assign(const float* X, int64_t n, const float* C, int32_t k, int32_t d,
+                               int32_t metric, int32_t* out_assign, float* out_dist);
+
+/* k-means++ seeding with the caller's randomness -- init_kmeans_plus_plus
+ * (src/transforms/kmeans/init.jl:56-102): first = first point, u[i] in [0,1)
+ * the i-th draw (u[0] unused).  out_idx[k] = chosen point indices. */
+mann_status mann_kmeanspp(const float* X, int64_t n, int32_t d, int32_t k, int64_t first,
+                          const double* u, int64_t* out_idx);
+
+/* lloyd! (src/transforms/kmeans/lloyd.jl:36-134) from the given centroids
+ * [k][d] (updated in place); out_assign[n] 0-based; *out_iters = iterations. */
+mann_status mann_kmeans_lloyd(const float* X, int64_t n, int32_t d, int32_t k, float* centroids,
+                              int32_t max_iters, double tol, int32_t metric, int32_t* out_assign,
+                              int32_t* out_iters);
+
+/* fit! of KMeansTransform (src/transforms/KMeansTransform.jl:106-161). */
+mann_status mann_kmeans_fit(const mann_kmeans_params* p, const float* X, int64_t n, int32_t d,
+                            float* out_centroids, int32_t* out_assign, int32_t* out_iters);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python

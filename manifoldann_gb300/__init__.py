@@ -11,6 +11,9 @@ from .distances import (CosineDist, Euclidean, SqEuclidean, cosine_distance, def
 from .eval_utils import recall_at_k
 from .graphs import (KNNGraph, build_knn_graph, graph_metadata, has_metadata, knn_graph_arrays,
                      node_metadata)
+from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, assign_arrays,
+                         assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
+                         pairwise_distances, take_pending_assignments, transform)
 from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
                       index_distance, insert, knn_arrays, neighbor_ids, query, supports_mutation)
 
@@ -23,4 +26,7 @@ __all__ = [
     "node_metadata",
     "AbstractANNIndex", "BruteForceIndex", "Neighbor", "build_index", "configured_k",
     "index_distance", "insert", "knn_arrays", "neighbor_ids", "query", "supports_mutation",
+    "KMeansAssignment", "KMeansTransform", "TransformResult", "assign_arrays", "assign_clusters", "fit",
+    "get_bucket_assignment", "init_kmeans_plus_plus", "lloyd", "pairwise_distances",
+    "take_pending_assignments", "transform",
 ]

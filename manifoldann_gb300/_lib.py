@@ -72,6 +72,18 @@ class KnnReport(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class KmeansParams(C.Structure):
+    _fields_ = [
+        ("k", C.c_int32),
+        ("metric", C.c_int32),
+        ("init", C.c_int32),
+        ("max_iters", C.c_int32),
+        ("tol", C.c_double),
+        ("subsample", C.c_int64),
+        ("seed", C.c_uint64),
+    ]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -90,6 +102,11 @@ SIGNATURES = {
     "mann_knn_graph_device": (_I32, [C.POINTER(KnnParams), _P, _I64, _I32, _I32, _P, _P,
                                      C.POINTER(KnnReport), _P]),
     "mann_knn_device_noalloc": (_I32, [C.POINTER(KnnParams), _P, _I64, _P, _I64, _I32, _P, _P, _P]),
+    "mann_pairwise_distances": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P]),
+    "mann_kmeans_assign": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P, _P]),
+    "mann_kmeanspp": (_I32, [_P, _I64, _I32, _I32, _I64, _P, _P]),
+    "mann_kmeans_lloyd": (_I32, [_P, _I64, _I32, _I32, _P, _I32, C.c_double, _I32, _P, _P]),
+    "mann_kmeans_fit": (_I32, [C.POINTER(KmeansParams), _P, _I64, _I32, _P, _P, _P]),
 }
 
 _lib = None

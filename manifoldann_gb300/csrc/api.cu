@@ -178,6 +178,14 @@ mann_status graph_impl(const mann_knn_params* p, const float* data, int64_t n, i
 }
 
 }  // namespace
+
+mann_status exact_search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p,
+                                const float* base, int64_t n, const float* qs, int64_t nq, int d,
+                                int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
+                                mann_knn_report* rep) {
+  return search_device(ctx, s, p, base, n, qs, nq, d, graph_self, kreq, kout, ids, dists, rep);
+}
+
 }  // namespace mann
 
 using namespace mann;

@@ -38,6 +38,20 @@ enum ScratchSlot : int {
   SLOT_SEED_PARTIAL,  // seed pass: per-CTA lists
   SLOT_SEED_LISTS,    // seed pass: merged lists
   SLOT_SEED,          // per-query admission seeds
+  SLOT_KM_A,          // KMeans work buffers (k-means++ / Lloyd)
+  SLOT_KM_B,
+  SLOT_KM_C,
+  SLOT_KM_D,
+  SLOT_KM_E,
+  SLOT_KM_F,
+  SLOT_KM_G,
+  SLOT_KM_H,
+  SLOT_KM_I,
+  SLOT_KM_J,
+  SLOT_KM_DIST,       // assignment distances
+  SLOT_KM_X,          // host-pointer KMeans calls: points
+  SLOT_KM_CENT,       // centroids
+  SLOT_KM_ASSIGN,     // assignments
   SLOT_COUNT
 };
 

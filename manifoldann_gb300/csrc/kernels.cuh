@@ -54,6 +54,13 @@ mann_status knn_fp32_keys_on(int num_sms, cudaStream_t s, const float* base, int
                              const float* qn, const float* bn, uint64_t* scratch, size_t words,
                              uint64_t** out_keys);
 
+// The exact search of mann_knn_device / mann_knn_graph_device on device
+// buffers, inside a caller's CallScope (ids/dists [nq][kout]).
+mann_status exact_search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p,
+                                const float* base, int64_t n, const float* qs, int64_t nq, int d,
+                                int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
+                                mann_knn_report* rep);
+
 // Largest k handled by the fused top-k kernels.
 constexpr int KMAX_FUSED = 256;
 

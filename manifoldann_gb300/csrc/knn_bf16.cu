@@ -54,7 +54,6 @@ constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 constexpr int NUM_EPI_WARPS = 4;
-constexpr int K2_THREADS = 64 + NUM_EPI_WARPS * 32;  // producer, MMA, 4 epilogue warps
 constexpr int LIST = 32;                             // candidates kept per query row
 constexpr int TSTR = 36;                             // row stride of the per-lane row buffers (floats)
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
@@ -164,7 +163,7 @@ __global__ void choose_scale_kernel(const double* __restrict__ score, float* __r
 __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
                                     const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
-                                    BaseMax* __restrict__ bmax) {
+                                    float* __restrict__ norms, BaseMax* __restrict__ bmax) {
   const int lane = threadIdx.x & 31;
   const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -203,6 +202,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
                           2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c * (1.0 + rel))) * (1.0 + 1e-9));
     ri.pad = 0.0f;
     info[row] = ri;
+    if (norms) norms[row] = ri.nrm;
     if (bmax) {
       atomicMax(&bmax->xn_bits, __float_as_uint(ri.xn_up));
       atomicMax(&bmax->r_bits, __float_as_uint(ri.r_up));
@@ -223,7 +223,8 @@ struct MainArgs {
   int depth;          // admission depth = k + margin (<= L)
   const RowInfo* qinfo;
   const RowInfo* binfo;
-  int64_t bstride;    // point p of this launch is row p * bstride of binfo (sampled passes)
+  const float* bnorm; // ||p~||^2 of the points, contiguous
+  int64_t bstride;    // point p of this launch is row p * bstride of binfo / bnorm (sampled passes)
   const float* seed;  // per query: admit only est' below this (NULL = no seed)
   uint64_t* partial;  // [nq][smax][L]
   int* err;
@@ -231,6 +232,17 @@ struct MainArgs {
 
 __device__ __forceinline__ int64_t chunk_begin(int c, int64_t work, int grid) {
   return (int64_t)((__int128)c * work / grid);
+}
+
+// Step s of CTA c's walk over its range [b0, b1) of (query block, point tile)
+// items.  The walk starts at the range's first item of tile 0 and wraps, so
+// all CTAs stream the same point tiles at the same time (L2 reuse); each query
+// block's items stay contiguous in the walk.
+__device__ __forceinline__ int64_t walk_item(int64_t b0, int64_t b1, int tiles, int64_t s) {
+  const int64_t f = ((b0 + tiles - 1) / tiles) * tiles;
+  if (f >= b1 || f == b0) return b0 + s;
+  const int64_t head = b1 - f;
+  return s < head ? f + s : b0 + (s - head);
 }
 
 // the CTA whose work range contains item i
@@ -386,7 +398,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     if (lane == 0) {
       uint32_t it = 0;
       bool ok = true;
-      for (int64_t item = it0; item < it1 && ok; ++item) {
+      for (int64_t st = 0; st < it1 - it0 && ok; ++st) {
+        const int64_t item = walk_item(it0, it1, a.tiles, st);
         const int qb = (int)(item / a.tiles);
         const int t = (int)(item % a.tiles);
         for (int kb = 0; kb < a.nkb; ++kb, ++it) {
@@ -411,7 +424,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       uint32_t it = 0;
       int tcount = 0;
       bool ok = true;
-      for (int64_t item = it0; item < it1 && ok; ++item, ++tcount) {
+      for (int64_t st = 0; st < it1 - it0 && ok; ++st, ++tcount) {
         const int buf = tcount & 1;
         const uint32_t tph = (tcount >> 1) & 1;
         if (!ptx::mbar_wait(&tempty_bar[buf], tph ^ 1, a.err, ERR_TIMEOUT_MMA)) break;
@@ -459,7 +472,20 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 
     for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
 
-    for (int64_t item = it0; item < it1; ++item, ++tcount) {
+    // norms of this set's first tile; later tiles' norms are fetched one tile ahead
+    float nbn[BN / 32];
+    auto fetch_norms = [&](int64_t st_) {
+      const int64_t item_ = walk_item(it0, it1, a.tiles, st_);
+      const int64_t c0 = (int64_t)(item_ % a.tiles) * BN;
+#pragma unroll
+      for (int i = 0; i < BN / 32; ++i) {
+        const int64_t col = c0 + lane + 32 * i;
+        nbn[i] = col < a.n ? __ldg(&a.bnorm[col * a.bstride]) : INF;
+      }
+    };
+    if (set < it1 - it0) fetch_norms(set);
+    for (int64_t st = 0; st < it1 - it0; ++st, ++tcount) {
+      const int64_t item = walk_item(it0, it1, a.tiles, st);
       const int qb = (int)(item / a.tiles);
       const int t = (int)(item % a.tiles);
       if (qb != cur_qb) {
@@ -485,11 +511,9 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       const int64_t col0 = (int64_t)t * BN;
       __syncwarp();
 #pragma unroll
-      for (int i = 0; i < BN / 32; ++i) {
-        const int64_t col = col0 + lane + 32 * i;
-        nbw[lane + 32 * i] = col < a.n ? __ldg(&a.binfo[col * a.bstride].nrm) : INF;
-      }
+      for (int i = 0; i < BN / 32; ++i) nbw[lane + 32 * i] = nbn[i];
       __syncwarp();
+      if (st + NSETS < it1 - it0) fetch_norms(st + NSETS);
       const uint32_t tph = (tcount >> 1) & 1;
       if (alive && !ptx::mbar_wait(&tfull_bar[buf], tph, a.err, ERR_TIMEOUT_EPI)) alive = false;
       if (!alive) break;
@@ -955,7 +979,7 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
 // every query over n points (binfo row p * bstride), as sorted lists [nq][LIST].
 mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
                           const CUtensorMap& mapB, const RowInfo* qinfo, const RowInfo* binfo,
-                          int64_t bstride, int64_t n, int64_t nq, int d, int dp, int depth,
+                          const float* bnorm, int64_t bstride, int64_t n, int64_t nq, int d, int dp, int depth,
                           const float* seed, int* err, int slot_partial, int slot_lists, bool timed,
                           uint64_t** lists_out) {
   const int64_t qblocks = ceil_div(nq, BM);
@@ -988,6 +1012,7 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.depth = depth;
   ma.qinfo = qinfo;
   ma.binfo = binfo;
+  ma.bnorm = bnorm;
   ma.bstride = bstride;
   ma.seed = seed;
   ma.partial = partial;
@@ -1028,6 +1053,7 @@ __global__ void seed_from_lists_kernel(const uint64_t* __restrict__ lists, int64
 struct Bf16Operand {
   __nv_bfloat16* xb = nullptr;
   RowInfo* info = nullptr;
+  float* norms = nullptr;  // contiguous ||x~||^2 (points only)
 };
 
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
@@ -1081,14 +1107,17 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   Bf16Operand B, Q;
   MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
-  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, dp, mu, scale, B.xb, B.info, bmax);
+  MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
+  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, dp, mu, scale, B.xb, B.info,
+                                                              B.norms, bmax);
   MANN_CHECK_LAUNCH();
   if (self) {
     Q = B;
   } else {
     MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dp, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
-    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, dp, mu, scale, Q.xb, Q.info, nullptr);
+    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, dp, mu, scale, Q.xb, Q.info,
+                                                                  nullptr, nullptr);
     MANN_CHECK_LAUNCH();
   }
 
@@ -1113,7 +1142,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     CUtensorMap mapS;
     MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dp, BN, bstride));
     uint64_t* slists = nullptr;
-    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, bstride, SEED_SAMPLE, nq, d, dp, 5,
+    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dp, 5,
                            nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
     seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, 4, seed);
@@ -1124,7 +1153,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   CUtensorMap mapB;
   MANN_TRY(make_map(&mapB, B.xb, n, dp, BN));
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, 1, n, nq, d, dp, depth, seed, err,
+  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, B.norms, 1, n, nq, d, dp, depth, seed, err,
                          SLOT_PARTIAL, SLOT_KEYS, true, &lists));
 
   // ---- certify + rerank

@@ -34,6 +34,8 @@ _SIGS = {
     "orc_ivf_query_f32": (_I32, [_P, _I32, _P, _P, _I32, _P, _P, _P, _I64, _I32, _I32, _I32, _I32,
                                  _P, _P, _I32]),
     "cpu_bruteforce_batch": (_I32, [_P, _I64, _P, _I64, _I32, _I32, _I32, _P, _P, _I32]),
+    "orc_kmeanspp": (_I32, [_P, _I64, _I32, _I32, _I64, _P, _P]),
+    "orc_kmeans_lloyd": (_I32, [_P, _I64, _I32, _I32, _P, _I32, C.c_double, _I32, _P, _P, _I32]),
     "orc_max_threads": (_I32, []),
 }
 
@@ -172,6 +174,25 @@ def cpu_bruteforce_batch(base, queries, k, metric, threads=0):
                                        base.shape[1], k, metric, ids.ctypes.data, d.ctypes.data,
                                        threads))
     return ids, d
+
+
+def kmeanspp(X, k, first, u):
+    X = _f32(X)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.empty(k, np.int64)
+    _check(load().orc_kmeanspp(X.ctypes.data, X.shape[0], X.shape[1], k, int(first), u.ctypes.data,
+                               out.ctypes.data))
+    return out
+
+
+def kmeans_lloyd(X, C0, max_iters, tol, metric, threads=0):
+    X = _f32(X)
+    C_ = np.array(C0, dtype=np.float32, copy=True, order="C")
+    a = np.empty(X.shape[0], np.int32)
+    it = np.zeros(1, np.int32)
+    _check(load().orc_kmeans_lloyd(X.ctypes.data, X.shape[0], X.shape[1], C_.shape[0], C_.ctypes.data,
+                                   max_iters, tol, metric, a.ctypes.data, it.ctypes.data, threads))
+    return C_, a, int(it[0])
 
 
 def max_threads() -> int:

@@ -330,6 +330,112 @@ int orc_kmeans_assign_f64(const float* X, int64_t n, const float* C, int32_t nli
   return 0;
 }
 
+/* ------------------------------------------------------------ k-means++ */
+
+#define ORC_SCAN_BLOCK 1024
+
+int orc_kmeanspp(const float* X, int64_t n, int32_t d, int32_t k, int64_t first, const double* u,
+                 int64_t* out_idx) {
+  if (n <= 0 || d <= 0 || k <= 0 || k > n) return 2;
+  float* mind = (float*)malloc(sizeof(float) * (size_t)n);
+  int64_t nb = (n + ORC_SCAN_BLOCK - 1) / ORC_SCAN_BLOCK;
+  double* bsum = (double*)malloc(sizeof(double) * (size_t)nb);
+  for (int64_t j = 0; j < n; ++j) mind[j] = INFINITY;
+  out_idx[0] = first;
+  for (int32_t i = 1; i < k; ++i) {
+    const float* c = X + out_idx[i - 1] * (int64_t)d;
+    for (int64_t j = 0; j < n; ++j) {
+      float v = orc_dist_f32(X + j * (int64_t)d, c, d, ORC_SQEUCLIDEAN);
+      if (v < mind[j]) mind[j] = v;
+    }
+    for (int64_t b = 0; b < nb; ++b) {
+      double s = 0.0;
+      int64_t e = (b + 1) * ORC_SCAN_BLOCK < n ? (b + 1) * ORC_SCAN_BLOCK : n;
+      for (int64_t j = b * ORC_SCAN_BLOCK; j < e; ++j) s += (double)mind[j];
+      bsum[b] = s;
+    }
+    double total = 0.0;
+    for (int64_t b = 0; b < nb; ++b) total += bsum[b];
+    const double thr = u[i] * total;
+    double acc = 0.0;
+    int64_t pick = n - 1;
+    for (int64_t b = 0; b < nb; ++b) {
+      if (acc + bsum[b] >= thr) {
+        int64_t e = (b + 1) * ORC_SCAN_BLOCK < n ? (b + 1) * ORC_SCAN_BLOCK : n;
+        double a2 = acc;
+        for (int64_t j = b * ORC_SCAN_BLOCK; j < e; ++j) {
+          a2 += (double)mind[j];
+          if (a2 >= thr) {
+            pick = j;
+            break;
+          }
+        }
+        break;
+      }
+      acc += bsum[b];
+    }
+    out_idx[i] = pick;
+  }
+  free(mind);
+  free(bsum);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ Lloyd */
+
+int orc_kmeans_lloyd(const float* X, int64_t n, int32_t d, int32_t k, float* C, int32_t max_iters,
+                     double tol, int32_t metric, int32_t* assign, int32_t* iters, int32_t nthreads) {
+  if (n <= 0 || d <= 0 || k <= 0) return 2;
+  double* dist = (double*)malloc(sizeof(double) * (size_t)n);
+  float* nc = (float*)malloc(sizeof(float) * (size_t)k * d);
+  int64_t* cnt = (int64_t*)malloc(sizeof(int64_t) * (size_t)k);
+  const int32_t am = metric == ORC_EUCLIDEAN ? ORC_EUCLIDEAN : ORC_SQEUCLIDEAN;
+  int32_t it = 0;
+  for (int32_t step = 1; step <= max_iters; ++step) {
+    it = step;
+    orc_kmeans_assign_f64(X, n, C, k, d, am, assign, dist, nthreads);
+    memset(nc, 0, sizeof(float) * (size_t)k * d);
+    memset(cnt, 0, sizeof(int64_t) * (size_t)k);
+    for (int64_t j = 0; j < n; ++j) {
+      float* dst = nc + (int64_t)assign[j] * d;
+      const float* x = X + j * (int64_t)d;
+      for (int32_t r = 0; r < d; ++r) dst[r] += x[r];
+      cnt[assign[j]] += 1;
+    }
+    for (int32_t c = 0; c < k; ++c) {
+      float* dst = nc + (int64_t)c * d;
+      if (cnt[c] == 0) {
+        double best = -INFINITY;
+        int64_t far = 0;
+        for (int64_t j = 0; j < n; ++j)
+          if (dist[j] > best) {
+            best = dist[j];
+            far = j;
+          }
+        memcpy(dst, X + far * (int64_t)d, sizeof(float) * (size_t)d);
+        cnt[c] = 1;
+        dist[far] = -INFINITY;
+      } else {
+        const float cf = (float)cnt[c];
+        for (int32_t r = 0; r < d; ++r) dst[r] = dst[r] / cf;
+      }
+    }
+    double move = 0.0;
+    for (int32_t c = 0; c < k; ++c) {
+      double m = (double)orc_dist_f32(C + (int64_t)c * d, nc + (int64_t)c * d, d, am);
+      if (m > move) move = m;
+    }
+    memcpy(C, nc, sizeof(float) * (size_t)k * d);
+    if (move < tol) break;
+  }
+  orc_kmeans_assign_f64(X, n, C, k, d, am, assign, dist, nthreads);
+  *iters = it;
+  free(dist);
+  free(nc);
+  free(cnt);
+  return 0;
+}
+
 /* ------------------------------------------------------------- routing */
 
 int32_t orc_topk_route(const float* dists, int32_t n_dist, int32_t n_children, int32_t k,

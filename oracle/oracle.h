@@ -62,6 +62,26 @@ int orc_kmeans_assign_gemm_f32(const float* X, int64_t n, const float* C, int32_
 int orc_kmeans_assign_f64(const float* X, int64_t n, const float* C, int32_t nlist, int32_t d,
                           int32_t metric, int32_t* assign, double* out_dist, int32_t nthreads);
 
+/* k-means++ seeding (src/transforms/kmeans/init.jl:56-102) with the
+ * randomness supplied: first = index of the first centroid, u[i] uniform in
+ * [0,1) for the i-th draw (i = 1..k-1).  D^2 is the FP32 difference form; the
+ * running sums are FP64 over blocks of 1024 points (block sums sequential,
+ * then a sequential prefix over blocks) -- the same order as the GPU.  The
+ * next centroid is the first point whose cumulative D^2 reaches u*total
+ * (searchsortedfirst).  out_idx[0..k-1] = chosen point indices. */
+int orc_kmeanspp(const float* X, int64_t n, int32_t d, int32_t k, int64_t first, const double* u,
+                 int64_t* out_idx);
+
+/* Lloyd iterations (src/transforms/kmeans/lloyd.jl:36-134) from the given
+ * centroids C [k][d] (updated in place): exact assignment (FP64 difference
+ * form, strict <), per-cluster FP32 sums in point order, division by the
+ * count, empty clusters refilled with the point farthest from its assigned
+ * centroid (first maximum; a chosen point is marked -inf), stop when the
+ * largest centroid movement (metric) is below tol; final assignment.
+ * Returns the iterations run in *iters. */
+int orc_kmeans_lloyd(const float* X, int64_t n, int32_t d, int32_t k, float* C, int32_t max_iters,
+                     double tol, int32_t metric, int32_t* assign, int32_t* iters, int32_t nthreads);
+
 /* select_indices(::TopKRouting, ::KMeansAssignment, domain)
  * (src/indices/multilevel/routing.jl:94-118).  Writes up to k 0-based
  * positions; returns the count, or -2 for the ArgumentError case (no
