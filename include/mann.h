@@ -147,6 +147,51 @@ mann_status mann_kmeans_lloyd(const float* X, int64_t n, int32_t d, int32_t k, f
 mann_status mann_kmeans_fit(const mann_kmeans_params* p, const float* X, int64_t n, int32_t d,
                             float* out_centroids, int32_t* out_assign, int32_t* out_iters);
 
+/* ---------------------------------------------------------------- IVF-Flat
+ * build_index(IVFFlatIndex, ...) and query (src/indices/ivf_flat.jl:30-93,
+ * :135-168).  Lists are CSR: list c holds list_ids[list_offsets[c] ..
+ * list_offsets[c+1]) (0-based point ids, ascending within a list, as the
+ * reference's counting pass leaves them); points stay the caller's [n][d]. */
+typedef struct {
+  int32_t nlist;
+  int32_t centroid_metric;   /* MANN_METRIC_EUCLIDEAN (default) or _SQEUCLIDEAN */
+  int32_t kmeans_max_iters;  /* <= 0: 25 */
+  int32_t reserved;
+  double kmeans_tol;         /* <= 0: 1e-4 */
+  int64_t kmeans_subsample;  /* Lloyd sample; the reference's default is max(256 nlist, 32768) */
+  uint64_t seed;
+} mann_ivf_build_params;
+
+/* KMeans (k-means++, Lloyd on the subsample, full assignment) + inverted lists.
+ * out_centroids[nlist][d], out_offsets[nlist+1], out_ids[n]. */
+mann_status mann_ivf_build(const mann_ivf_build_params* p, const float* data, int64_t n, int32_t d,
+                           float* out_centroids, int64_t* out_offsets, int32_t* out_ids,
+                           int32_t* out_iters);
+
+/* query of IVFFlatIndex for q queries: route each query to its nprobe
+ * (clamped to nlist) nearest centroids by exact centroid_metric distance,
+ * scan those lists with p->metric (Euclidean / SqEuclidean, FP32 form), keep
+ * the top p->k (1..64) by (distance, id).  Rows with fewer candidates than k
+ * are padded with -1 / +inf (the reference returns the shorter list). */
+mann_status mann_ivf_search(const mann_knn_params* p, int32_t nprobe, int32_t centroid_metric,
+                            const float* data, int64_t n, int32_t d, const float* centroids,
+                            int32_t nlist, const int64_t* list_offsets, const int32_t* list_ids,
+                            const float* queries, int64_t q, int32_t* out_ids, float* out_dists);
+/* Same with device pointers, ordered on `stream`. */
+mann_status mann_ivf_search_device(const mann_knn_params* p, int32_t nprobe, int32_t centroid_metric,
+                                   const float* data, int64_t n, int32_t d, const float* centroids,
+                                   int32_t nlist, const int64_t* list_offsets,
+                                   const int32_t* list_ids, const float* queries, int64_t q,
+                                   int32_t* out_ids, float* out_dists, void* stream);
+/* The list scan alone for a routing chosen by the caller (select_indices of
+ * any routing policy, src/indices/multilevel/routing.jl): probes[q][nprobe]
+ * (device) holds distinct list ids per query, -1 = unused slot. */
+mann_status mann_ivf_scan_device(const mann_knn_params* p, const int32_t* probes, int32_t nprobe,
+                                 const float* data, int64_t n, int32_t d, int32_t nlist,
+                                 const int64_t* list_offsets, const int32_t* list_ids,
+                                 const float* queries, int64_t q, int32_t* out_ids,
+                                 float* out_dists, void* stream);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python

@@ -14,6 +14,7 @@ from .graphs import (KNNGraph, build_knn_graph, graph_metadata, has_metadata, kn
 from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, assign_arrays,
                          assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
                          pairwise_distances, take_pending_assignments, transform)
+from .ivf import IVFFlatIndex, TopKRouting, ivf_search_device, select_indices
 from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
                       index_distance, insert, knn_arrays, neighbor_ids, query, supports_mutation)
 
@@ -29,4 +30,5 @@ __all__ = [
     "KMeansAssignment", "KMeansTransform", "TransformResult", "assign_arrays", "assign_clusters", "fit",
     "get_bucket_assignment", "init_kmeans_plus_plus", "lloyd", "pairwise_distances",
     "take_pending_assignments", "transform",
+    "IVFFlatIndex", "TopKRouting", "ivf_search_device", "select_indices",
 ]

@@ -84,6 +84,18 @@ class KmeansParams(C.Structure):
     ]
 
 
+class IvfBuildParams(C.Structure):
+    _fields_ = [
+        ("nlist", C.c_int32),
+        ("centroid_metric", C.c_int32),
+        ("kmeans_max_iters", C.c_int32),
+        ("reserved", C.c_int32),
+        ("kmeans_tol", C.c_double),
+        ("kmeans_subsample", C.c_int64),
+        ("seed", C.c_uint64),
+    ]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -107,6 +119,13 @@ SIGNATURES = {
     "mann_kmeanspp": (_I32, [_P, _I64, _I32, _I32, _I64, _P, _P]),
     "mann_kmeans_lloyd": (_I32, [_P, _I64, _I32, _I32, _P, _I32, C.c_double, _I32, _P, _P]),
     "mann_kmeans_fit": (_I32, [C.POINTER(KmeansParams), _P, _I64, _I32, _P, _P, _P]),
+    "mann_ivf_build": (_I32, [C.POINTER(IvfBuildParams), _P, _I64, _I32, _P, _P, _P, _P]),
+    "mann_ivf_search": (_I32, [C.POINTER(KnnParams), _I32, _I32, _P, _I64, _I32, _P, _I32, _P, _P, _P,
+                               _I64, _P, _P]),
+    "mann_ivf_search_device": (_I32, [C.POINTER(KnnParams), _I32, _I32, _P, _I64, _I32, _P, _I32, _P,
+                                      _P, _P, _I64, _P, _P, _P]),
+    "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
+                                    _I64, _P, _P, _P]),
 }
 
 _lib = None

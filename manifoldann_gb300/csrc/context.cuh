@@ -52,6 +52,19 @@ enum ScratchSlot : int {
   SLOT_KM_X,          // host-pointer KMeans calls: points
   SLOT_KM_CENT,       // centroids
   SLOT_KM_ASSIGN,     // assignments
+  SLOT_IVF_DATA,      // IVF search: points gathered into list order
+  SLOT_IVF_CNT,       // IVF search: per-list query counts and cursors
+  SLOT_IVF_OFF,       // IVF search: per-list query and chunk offsets
+  SLOT_IVF_PAIRS,     // IVF search: (query, probe rank) pairs grouped by list
+  SLOT_IVF_PARTIAL,   // IVF search: per-probe top-k lists
+  SLOT_IVF_KEYS,      // IVF search: merged top-k lists
+  SLOT_IVF_PROBES,    // IVF search: routed lists
+  SLOT_IVF_ROUTE_D,   // IVF search: routing distances
+  SLOT_IVF_ASSIGN,    // IVF build: cluster of every point
+  SLOT_IVF_START,     // IVF build: list starts and sizes
+  SLOT_IVF_MEMBERS,   // IVF build: members grouped by list
+  SLOT_IVF_LOFF,      // host-pointer IVF calls: list offsets
+  SLOT_IVF_LIDS,      // host-pointer IVF calls: list ids
   SLOT_COUNT
 };
 

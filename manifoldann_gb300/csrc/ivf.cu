@@ -1,0 +1,423 @@
+// ivf.cu -- IVF-Flat on the GPU: build (KMeans + inverted lists) and search
+// (route to nprobe lists, scan them, top-k).
+//
+// Replaces src/indices/ivf_flat.jl: build_index (:30-93), _centroid_distances
+// + partialsortperm routing (:103-131, :150) and the list scan into a bounded
+// heap (:153-167); the routing hook is select_indices(TopKRouting)
+// (src/indices/multilevel/routing.jl:94-118), and mann_ivf_scan takes any
+// routing (the learned probe supplies its own).
+//
+// The scan runs "inverted" like the reference's batched multi-level query
+// (src/indices/multilevel/query.jl:363-396): queries are grouped by the list
+// they probe, the data is gathered into list order once per call, and one
+// CTA scans one list for up to 32 of its queries, every distance in the FP32
+// form's sequential arithmetic, keeping each query's top-k.  Order: (distance,
+// id); the reference's heap keeps an arbitrary member of an exact tie at the
+// k-th place, this keeps the lower id.
+#include <algorithm>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace mann {
+
+namespace {
+
+constexpr int SCAN_Q = 32;    // queries per CTA
+constexpr int SCAN_P = 64;    // points per tile
+constexpr int SCAN_D = 64;    // dimensions per stage
+constexpr int SCAN_THREADS = 256;
+
+__global__ void ivf_lists_kernel(const int64_t* __restrict__ start, const int64_t* __restrict__ members,
+                                 int k, int64_t n, int64_t* __restrict__ offsets,
+                                 int32_t* __restrict__ ids) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) ids[i] = (int32_t)members[i];
+  if (i <= k) offsets[i] = i < k ? start[i] : n;
+}
+
+// data rows in list order
+__global__ void gather_lists_kernel(const float* __restrict__ data, int d,
+                                    const int32_t* __restrict__ ids, int64_t n,
+                                    float* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  const float* src = data + (int64_t)ids[r] * d;
+  float* dst = out + r * d;
+  for (int c = lane; c < d; c += 32) dst[c] = src[c];
+}
+
+__global__ void probe_count_kernel(const int32_t* __restrict__ probes, int64_t np, int nlist,
+                                   unsigned* __restrict__ cnt) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int l = probes[i];
+  if (l >= 0 && l < nlist) atomicAdd(&cnt[l], 1u);
+}
+
+// exclusive prefix sums of per-list query counts and of 32-query chunks
+__global__ void probe_scan_kernel(const unsigned* __restrict__ cnt, int nlist,
+                                  int64_t* __restrict__ qoff, int64_t* __restrict__ choff) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t a = 0, b = 0;
+  for (int l = 0; l < nlist; ++l) {
+    qoff[l] = a;
+    choff[l] = b;
+    a += cnt[l];
+    b += (cnt[l] + SCAN_Q - 1) / SCAN_Q;
+  }
+  qoff[nlist] = a;
+  choff[nlist] = b;
+}
+
+__global__ void probe_scatter_kernel(const int32_t* __restrict__ probes, int64_t nq, int nprobe,
+                                     int nlist, const int64_t* __restrict__ qoff,
+                                     unsigned* __restrict__ cursor, int32_t* __restrict__ pair_q,
+                                     int32_t* __restrict__ pair_r) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nq * nprobe) return;
+  const int l = probes[i];
+  if (l < 0 || l >= nlist) return;
+  const int64_t pos = qoff[l] + atomicAdd(&cursor[l], 1u);
+  pair_q[pos] = (int32_t)(i / nprobe);
+  pair_r[pos] = (int32_t)(i % nprobe);
+}
+
+// One CTA: list l, its queries [e0, e1) (at most 32).  Thread t serves query
+// t/8 and points t%8 + 8u of every 64-point tile; each thread keeps its own
+// sorted top-k in shared memory, the 8 lists of a query are merged at the end.
+template <int METRIC>
+__global__ void __launch_bounds__(SCAN_THREADS)
+    ivf_scan_kernel(const float* __restrict__ xs, const int64_t* __restrict__ loff,
+                    const int32_t* __restrict__ lids, const float* __restrict__ qs, int d,
+                    const int64_t* __restrict__ qoff, const int32_t* __restrict__ pair_q,
+                    const int32_t* __restrict__ pair_r, const int64_t* __restrict__ choff, int nlist,
+                    int k, int nprobe, uint64_t* __restrict__ partial) {
+  extern __shared__ uint64_t ivf_smem[];
+  uint64_t* lists = ivf_smem;                                               // [k][256]
+  float* qsm = reinterpret_cast<float*>(lists + (size_t)k * SCAN_THREADS);  // [32][SCAN_D]
+  float* psm = qsm + SCAN_Q * SCAN_D;                                       // [SCAN_D][SCAN_P + 1]
+
+  const int64_t w = blockIdx.x;
+  if (w >= choff[nlist]) return;
+  int lo = 0, hi = nlist - 1;
+  while (lo < hi) {  // last list whose chunk offset <= w
+    const int mid = (lo + hi + 1) >> 1;
+    if (choff[mid] <= w) lo = mid;
+    else hi = mid - 1;
+  }
+  const int l = lo;
+  const int64_t e0 = qoff[l] + (w - choff[l]) * SCAN_Q;
+  const int nqe = (int)min((int64_t)SCAN_Q, qoff[l + 1] - e0);
+  const int64_t p_begin = loff[l], p_end = loff[l + 1];
+
+  const int t = threadIdx.x;
+  const int qi = t >> 3, g = t & 7;
+  uint64_t* my = lists + t;  // entry j at my[j * 256]
+  for (int j = 0; j < k; ++j) my[j * SCAN_THREADS] = KEY_NONE;
+  uint64_t thr = KEY_NONE;
+  const int64_t qrow = qi < nqe ? (int64_t)pair_q[e0 + qi] : -1;
+
+  for (int64_t p0 = p_begin; p0 < p_end; p0 += SCAN_P) {
+    const int np = (int)min((int64_t)SCAN_P, p_end - p0);
+    float acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = 0.0f;
+    for (int c0 = 0; c0 < d; c0 += SCAN_D) {
+      const int dc = min(SCAN_D, d - c0);
+      __syncthreads();
+      for (int e = t; e < SCAN_Q * SCAN_D; e += SCAN_THREADS) {
+        const int r = e / SCAN_D, c = e % SCAN_D;
+        float v = 0.0f;
+        if (r < nqe && c < dc) v = qs[(int64_t)pair_q[e0 + r] * d + c0 + c];
+        qsm[r * SCAN_D + c] = v;
+      }
+      for (int e = t; e < SCAN_P * SCAN_D; e += SCAN_THREADS) {
+        const int j = e / SCAN_D, c = e % SCAN_D;
+        float v = 0.0f;
+        if (j < np && c < dc) v = xs[(p0 + j) * d + c0 + c];
+        psm[c * (SCAN_P + 1) + j] = v;
+      }
+      __syncthreads();
+      for (int c = 0; c < dc; ++c) {
+        const float qv = qsm[qi * SCAN_D + c];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const float tt = __fsub_rn(qv, psm[c * (SCAN_P + 1) + g + 8 * u]);
+          acc[u] = __fmaf_rn(tt, tt, acc[u]);
+        }
+      }
+    }
+    if (qrow >= 0) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = g + 8 * u;
+        if (j >= np) continue;
+        const float v = METRIC == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc[u]) : acc[u];
+        const uint64_t key = make_key(v, (uint32_t)lids[p0 + j]);
+        if (key < thr) {
+          int p = k - 1;
+          while (p > 0) {
+            const uint64_t prev = my[(p - 1) * SCAN_THREADS];
+            if (prev < key) break;
+            my[p * SCAN_THREADS] = prev;
+            --p;
+          }
+          my[p * SCAN_THREADS] = key;
+          thr = my[(k - 1) * SCAN_THREADS];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (g == 0 && qrow >= 0) {
+    // merge the 8 sorted lists of this query
+    int head[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) head[u] = 0;
+    uint64_t* dst = partial + ((int64_t)qrow * nprobe + pair_r[e0 + qi]) * k;
+    for (int e = 0; e < k; ++e) {
+      uint64_t best = KEY_NONE;
+      int bu = 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const uint64_t v = head[u] < k ? lists[head[u] * SCAN_THREADS + t + u] : KEY_NONE;
+        if (v < best) {
+          best = v;
+          bu = u;
+        }
+      }
+      dst[e] = best;
+      if (best != KEY_NONE) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (u == bu) ++head[u];
+      }
+    }
+  }
+}
+
+}  // namespace
+
+// Scan of the given probes [nq][nprobe] (list ids, -1 = none) over list-ordered
+// points; results as ids/dists [nq][k] (-1 / +inf padding).
+mann_status ivf_scan_device(Context* ctx, cudaStream_t s, const float* data, int64_t n, int d,
+                            int metric, const int64_t* loff, const int32_t* lids, int nlist,
+                            const float* qs, int64_t nq, const int32_t* probes, int nprobe, int k,
+                            int32_t* out_ids, float* out_dists) {
+  if (k < 1 || k > 64) return fail(MANN_EINVAL_ARG, "IVF search supports 1 <= k <= 64");
+  if (nprobe < 1 || nprobe > 128) return fail(MANN_EINVAL_ARG, "IVF search supports 1 <= nprobe <= 128");
+  if (metric == MANN_METRIC_COSINE) return fail(MANN_EINVAL_ARG, "IVF search: Euclidean / SqEuclidean");
+  if (nq <= 0) return MANN_OK;
+  float* xs = nullptr;
+  unsigned* cnt = nullptr;
+  int64_t *qoff = nullptr, *choff = nullptr;
+  int32_t *pair_q = nullptr, *pair_r = nullptr;
+  uint64_t *partial = nullptr, *keys = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_DATA, (size_t)n * d, &xs));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_CNT, (size_t)2 * nlist + 4, &cnt));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_OFF, (size_t)2 * (nlist + 1), &qoff));
+  choff = qoff + (nlist + 1);
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_PAIRS, (size_t)2 * nq * nprobe, &pair_q));
+  pair_r = pair_q + nq * nprobe;
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_PARTIAL, (size_t)nq * nprobe * k, &partial));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_KEYS, (size_t)nq * k, &keys));
+  gather_lists_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(data, d, lids, n, xs);
+  MANN_CHECK_LAUNCH();
+  MANN_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (2 * nlist + 4), s));
+  MANN_CUDA_TRY(cudaMemsetAsync(partial, 0xFF, sizeof(uint64_t) * nq * nprobe * k, s));
+  probe_count_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(probes, nq * nprobe, nlist, cnt);
+  MANN_CHECK_LAUNCH();
+  probe_scan_kernel<<<1, 32, 0, s>>>(cnt, nlist, qoff, choff);
+  MANN_CHECK_LAUNCH();
+  probe_scatter_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(
+      probes, nq, nprobe, nlist, qoff, cnt + nlist, pair_q, pair_r);
+  MANN_CHECK_LAUNCH();
+  // chunks <= pairs/32 + lists; blocks past the real count return at once
+  const int64_t max_chunks = ceil_div(nq * nprobe, SCAN_Q) + nlist;
+  const size_t smem = sizeof(uint64_t) * k * SCAN_THREADS +
+                      sizeof(float) * (SCAN_Q * SCAN_D + SCAN_D * (SCAN_P + 1));
+  if (metric == MANN_METRIC_EUCLIDEAN) {
+    MANN_CUDA_TRY(cudaFuncSetAttribute(ivf_scan_kernel<MANN_METRIC_EUCLIDEAN>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ctx->time_begin(s);
+    ivf_scan_kernel<MANN_METRIC_EUCLIDEAN><<<(unsigned)max_chunks, SCAN_THREADS, smem, s>>>(
+        xs, loff, lids, qs, d, qoff, pair_q, pair_r, choff, nlist, k, nprobe, partial);
+  } else {
+    MANN_CUDA_TRY(cudaFuncSetAttribute(ivf_scan_kernel<MANN_METRIC_SQEUCLIDEAN>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ctx->time_begin(s);
+    ivf_scan_kernel<MANN_METRIC_SQEUCLIDEAN><<<(unsigned)max_chunks, SCAN_THREADS, smem, s>>>(
+        xs, loff, lids, qs, d, qoff, pair_q, pair_r, choff, nlist, k, nprobe, partial);
+  }
+  ctx->time_end(s);
+  MANN_CHECK_LAUNCH();
+  MANN_TRY(launch_merge_lists(partial, nq, nprobe, k, keys, s));
+  MANN_TRY(launch_finish(keys, nq, k, k, -1, nullptr, out_ids, out_dists, s));
+  return MANN_OK;
+}
+
+// top-nprobe centroids of every query (TopKRouting on exact centroid distances)
+mann_status ivf_route_device(Context* ctx, cudaStream_t s, const float* centroids, int nlist, int d,
+                             int centroid_metric, const float* qs, int64_t nq, int nprobe,
+                             int32_t* probes) {
+  mann_knn_params p{};
+  p.metric = centroid_metric;
+  p.k = nprobe;
+  p.precision = MANN_PREC_AUTO;
+  float* dd = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_ROUTE_D, (size_t)nq * nprobe, &dd));
+  return exact_search_device(ctx, s, &p, centroids, nlist, qs, nq, d, -1, std::min(nprobe, nlist),
+                             nprobe, probes, dd, nullptr);
+}
+
+mann_status ivf_build_device(Context* ctx, cudaStream_t s, const float* data, int64_t n, int d,
+                             int nlist, int centroid_metric, int max_iters, double tol,
+                             int64_t subsample, uint64_t seed, float* centroids, int64_t* offsets,
+                             int32_t* ids, int* iters) {
+  int32_t* assign = nullptr;
+  int64_t *start = nullptr, *members = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_ASSIGN, (size_t)n, &assign));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_START, (size_t)2 * nlist, &start));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_MEMBERS, (size_t)n, &members));
+  MANN_TRY(kmeans_fit_device(ctx, s, data, n, d, nlist, centroid_metric, 1, max_iters, tol, subsample,
+                             seed, centroids, assign, iters));
+  MANN_TRY(group_by_cluster_device(ctx, s, assign, n, nlist, start, start + nlist, members));
+  ivf_lists_kernel<<<(unsigned)ceil_div(std::max<int64_t>(n, nlist + 1), 256), 256, 0, s>>>(
+      start, members, nlist, n, offsets, ids);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
+}  // namespace mann
+
+using namespace mann;
+
+extern "C" {
+
+mann_status mann_ivf_build(const mann_ivf_build_params* p, const float* data, int64_t n, int32_t d,
+                           float* out_centroids, int64_t* out_offsets, int32_t* out_ids,
+                           int32_t* out_iters) {
+  clear_error();
+  if (!p) return fail(MANN_EINVAL_ARG, "params must not be NULL");
+  if (d <= 0) return fail(MANN_EINVAL_ARG, "Dataset must have at least one dimension");
+  if (n <= 0) return fail(MANN_EINVAL_ARG, "Dataset must contain at least one point");
+  if (p->nlist <= 0) return fail(MANN_EINVAL_ARG, "nlist must be positive");
+  if (p->nlist > n) return fail(MANN_EINVAL_ARG, "Cannot fit " + std::to_string(p->nlist) +
+                                                     " clusters with only " + std::to_string(n) + " points");
+  if (p->centroid_metric != MANN_METRIC_EUCLIDEAN && p->centroid_metric != MANN_METRIC_SQEUCLIDEAN)
+    return fail(MANN_EINVAL_ARG, "centroid metric: Euclidean or SqEuclidean");
+  if (!data || !out_centroids || !out_offsets || !out_ids) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = ctx->stream;
+  CallScope scope(ctx, s);
+  float *dx = nullptr, *dc = nullptr;
+  int64_t* doff = nullptr;
+  int32_t* dids = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_BASE, (size_t)n * d, &dx));
+  MANN_TRY(ctx->scratch_t(SLOT_KM_CENT, (size_t)p->nlist * d, &dc));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_LOFF, (size_t)p->nlist + 1, &doff));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_LIDS, (size_t)n, &dids));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dx, data, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+  int iters = 0;
+  MANN_TRY(ivf_build_device(ctx, s, dx, n, d, p->nlist, p->centroid_metric,
+                            p->kmeans_max_iters > 0 ? p->kmeans_max_iters : 25,
+                            p->kmeans_tol > 0 ? p->kmeans_tol : 1e-4, p->kmeans_subsample, p->seed,
+                            dc, doff, dids, &iters));
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_centroids, dc, sizeof(float) * p->nlist * d, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_offsets, doff, sizeof(int64_t) * (p->nlist + 1), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_ids, dids, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  if (out_iters) *out_iters = iters;
+  return MANN_OK;
+}
+
+static mann_status ivf_check(const mann_knn_params* p, int32_t nprobe, const float* data, int64_t n,
+                             int32_t d, int32_t nlist, const int64_t* offs, const int32_t* ids,
+                             const float* qs, int64_t q) {
+  if (!p) return fail(MANN_EINVAL_ARG, "params must not be NULL");
+  if (d <= 0) return fail(MANN_EINVAL_ARG, "Dataset must have at least one dimension");
+  if (n <= 0) return fail(MANN_EINVAL_ARG, "Dataset must contain at least one point");
+  if (nlist <= 0 || nprobe <= 0) return fail(MANN_EINVAL_ARG, "nlist and nprobe must be positive");
+  if (q < 0) return fail(MANN_EINVAL_ARG, "negative query count");
+  if (!data || !offs || !ids || (q > 0 && !qs)) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  return MANN_OK;
+}
+
+mann_status mann_ivf_search_device(const mann_knn_params* p, int32_t nprobe, int32_t centroid_metric,
+                                   const float* data, int64_t n, int32_t d, const float* centroids,
+                                   int32_t nlist, const int64_t* list_offsets,
+                                   const int32_t* list_ids, const float* queries, int64_t q,
+                                   int32_t* out_ids, float* out_dists, void* stream) {
+  clear_error();
+  MANN_TRY(ivf_check(p, nprobe, data, n, d, nlist, list_offsets, list_ids, queries, q));
+  if (p->k <= 0 || q == 0) return MANN_OK;
+  nprobe = std::min(nprobe, nlist);  // clamp(nprobe, 1, nlist) (ivf_flat.jl:146)
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CallScope scope(ctx, s);
+  int32_t* probes = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_PROBES, (size_t)q * nprobe, &probes));
+  MANN_TRY(ivf_route_device(ctx, s, centroids, nlist, d, centroid_metric, queries, q, nprobe, probes));
+  return ivf_scan_device(ctx, s, data, n, d, p->metric, list_offsets, list_ids, nlist, queries, q,
+                         probes, nprobe, p->k, out_ids, out_dists);
+}
+
+mann_status mann_ivf_scan_device(const mann_knn_params* p, const int32_t* probes, int32_t nprobe,
+                                 const float* data, int64_t n, int32_t d, int32_t nlist,
+                                 const int64_t* list_offsets, const int32_t* list_ids,
+                                 const float* queries, int64_t q, int32_t* out_ids,
+                                 float* out_dists, void* stream) {
+  clear_error();
+  MANN_TRY(ivf_check(p, nprobe, data, n, d, nlist, list_offsets, list_ids, queries, q));
+  if (!probes && q > 0) return fail(MANN_EINVAL_ARG, "NULL probes");
+  if (p->k <= 0 || q == 0) return MANN_OK;
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CallScope scope(ctx, s);
+  return ivf_scan_device(ctx, s, data, n, d, p->metric, list_offsets, list_ids, nlist, queries, q,
+                         probes, nprobe, p->k, out_ids, out_dists);
+}
+
+mann_status mann_ivf_search(const mann_knn_params* p, int32_t nprobe, int32_t centroid_metric,
+                            const float* data, int64_t n, int32_t d, const float* centroids,
+                            int32_t nlist, const int64_t* list_offsets, const int32_t* list_ids,
+                            const float* queries, int64_t q, int32_t* out_ids, float* out_dists) {
+  clear_error();
+  MANN_TRY(ivf_check(p, nprobe, data, n, d, nlist, list_offsets, list_ids, queries, q));
+  if (p->k <= 0 || q == 0) return MANN_OK;
+  nprobe = std::min(nprobe, nlist);
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = ctx->stream;
+  CallScope scope(ctx, s);
+  float *dx = nullptr, *dc = nullptr, *dq = nullptr, *dd = nullptr;
+  int64_t* doff = nullptr;
+  int32_t *dids = nullptr, *dout = nullptr, *probes = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_BASE, (size_t)n * d, &dx));
+  MANN_TRY(ctx->scratch_t(SLOT_KM_CENT, (size_t)nlist * d, &dc));
+  MANN_TRY(ctx->scratch_t(SLOT_QUERIES, (size_t)q * d, &dq));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_LOFF, (size_t)nlist + 1, &doff));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_LIDS, (size_t)n, &dids));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_IDS, (size_t)q * p->k, &dout));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_DISTS, (size_t)q * p->k, &dd));
+  MANN_TRY(ctx->scratch_t(SLOT_IVF_PROBES, (size_t)q * nprobe, &probes));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dx, data, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dc, centroids, sizeof(float) * nlist * d, cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dq, queries, sizeof(float) * q * d, cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(doff, list_offsets, sizeof(int64_t) * (nlist + 1), cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dids, list_ids, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+  MANN_TRY(ivf_route_device(ctx, s, dc, nlist, d, centroid_metric, dq, q, nprobe, probes));
+  MANN_TRY(ivf_scan_device(ctx, s, dx, n, d, p->metric, doff, dids, nlist, dq, q, probes, nprobe,
+                           p->k, dout, dd));
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_ids, dout, sizeof(int32_t) * q * p->k, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_dists, dd, sizeof(float) * q * p->k, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  return MANN_OK;
+}
+
+}  // extern "C"

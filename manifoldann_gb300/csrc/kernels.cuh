@@ -61,6 +61,17 @@ mann_status exact_search_device(Context* ctx, cudaStream_t s, const mann_knn_par
                                 int64_t graph_self, int kreq, int kout, int32_t* ids, float* dists,
                                 mann_knn_report* rep);
 
+// Merge nsplit sorted key lists of k per query (nsplit <= 128) into one.
+mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, int k, uint64_t* out,
+                               cudaStream_t s);
+
+// KMeans pieces (kmeans.cu) used by the IVF index.
+mann_status kmeans_fit_device(Context* ctx, cudaStream_t s, const float* X, int64_t n, int d, int k,
+                              int metric, int init, int max_iters, double tol, int64_t subsample,
+                              uint64_t seed, float* C, int32_t* assign, int* iters_out);
+mann_status group_by_cluster_device(Context* ctx, cudaStream_t s, const int32_t* assign, int64_t n,
+                                    int k, int64_t* start, int64_t* count, int64_t* members);
+
 // Largest k handled by the fused top-k kernels.
 constexpr int KMAX_FUSED = 256;
 

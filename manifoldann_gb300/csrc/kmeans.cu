@@ -464,6 +464,27 @@ mann_status gather_rows_device(cudaStream_t s, const float* X, int d, const int6
   return MANN_OK;
 }
 
+// Group points by cluster: cluster c's members (ascending point index) are
+// members[start[c] .. start[c] + count[c]).
+mann_status group_by_cluster_device(Context* ctx, cudaStream_t s, const int32_t* assign, int64_t n,
+                                    int k, int64_t* start, int64_t* count, int64_t* members) {
+  const int64_t nb = ceil_div(n, SORT_CHUNK);
+  unsigned* hist = nullptr;
+  int64_t* offs = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_KM_A, (size_t)k * nb, &hist));
+  MANN_TRY(ctx->scratch_t(SLOT_KM_B, (size_t)k * nb, &offs));
+  MANN_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(unsigned) * k * nb, s));
+  sort_hist_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(assign, n, nb, hist);
+  MANN_CHECK_LAUNCH();
+  scan_kernel<<<1, 1024, 0, s>>>(hist, (int64_t)k * nb, offs);
+  MANN_CHECK_LAUNCH();
+  cluster_ranges_kernel<<<(unsigned)ceil_div(k, 256), 256, 0, s>>>(offs, k, nb, n, start, count);
+  MANN_CHECK_LAUNCH();
+  sort_scatter_kernel<<<(unsigned)ceil_div(nb, 4), 128, 0, s>>>(assign, n, nb, offs, members);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
 // Lloyd from the centroids in C (device, updated in place).
 mann_status lloyd_device(Context* ctx, cudaStream_t s, const float* X, int64_t n, int d, int k,
                          float* C, int max_iters, double tol, int metric, int32_t* assign,

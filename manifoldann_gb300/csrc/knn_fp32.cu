@@ -428,6 +428,15 @@ mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const
 
 }  // namespace
 
+mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, int k, uint64_t* out,
+                               cudaStream_t s) {
+  if (nq <= 0) return MANN_OK;
+  if (nsplit > 128) return fail(MANN_EINVAL_ARG, "at most 128 lists per query can be merged");
+  merge_lists_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, nsplit, k, out);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
 mann_status launch_row_sqnorm(const float* x, int64_t n, int d, float* out, cudaStream_t s) {
   if (n <= 0) return MANN_OK;
   row_sqnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, d, out);

@@ -36,6 +36,7 @@ _SIGS = {
     "cpu_bruteforce_batch": (_I32, [_P, _I64, _P, _I64, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_kmeanspp": (_I32, [_P, _I64, _I32, _I32, _I64, _P, _P]),
     "orc_kmeans_lloyd": (_I32, [_P, _I64, _I32, _I32, _P, _I32, C.c_double, _I32, _P, _P, _I32]),
+    "orc_ivf_scan_f32": (_I32, [_P, _I32, _P, _P, _P, _I64, _P, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_max_threads": (_I32, []),
 }
 
@@ -162,6 +163,20 @@ def ivf_query_f32(data, centroids, centroid_norms, list_offsets, list_ids, queri
                                     list_offsets.ctypes.data, list_ids.ctypes.data, queries.ctypes.data,
                                     nq, k, nprobe, metric, centroid_metric, ids.ctypes.data,
                                     d.ctypes.data, threads))
+    return ids, d
+
+
+def ivf_scan_f32(data, list_offsets, list_ids, queries, probes, k, metric, threads=0):
+    data, queries = _f32(data), _f32(queries)
+    list_offsets = np.ascontiguousarray(list_offsets, dtype=np.int64)
+    list_ids = np.ascontiguousarray(list_ids, dtype=np.int32)
+    probes = np.ascontiguousarray(probes, dtype=np.int32)
+    nq = queries.shape[0]
+    ids = np.empty((nq, k), np.int32)
+    d = np.empty((nq, k), np.float32)
+    _check(load().orc_ivf_scan_f32(data.ctypes.data, data.shape[1], list_offsets.ctypes.data,
+                                   list_ids.ctypes.data, queries.ctypes.data, nq, probes.ctypes.data,
+                                   probes.shape[1], k, metric, ids.ctypes.data, d.ctypes.data, threads))
     return ids, d
 
 

@@ -568,6 +568,54 @@ int orc_ivf_query_f32(const float* data, int32_t d, const float* centroids,
   return 0;
 }
 
+int orc_ivf_scan_f32(const float* data, int32_t d, const int64_t* list_offsets,
+                     const int32_t* list_ids, const float* q, int64_t nq, const int32_t* probes,
+                     int32_t nprobe, int32_t k, int32_t metric, int32_t* ids, float* dists,
+                     int32_t nthreads) {
+  if (d <= 0) return 2;
+  if (k <= 0 || nq <= 0) return 0;
+  int nt = resolve_threads(nthreads);
+#pragma omp parallel num_threads(nt)
+  {
+    nb_t* heap = (nb_t*)malloc(sizeof(nb_t) * (size_t)k);
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t qi = 0; qi < nq; ++qi) {
+      const float* qv = q + qi * (int64_t)d;
+      const int32_t* pr = probes + qi * (int64_t)nprobe;
+      int64_t avail = 0;
+      for (int32_t p = 0; p < nprobe; ++p)
+        if (pr[p] >= 0) avail += list_offsets[pr[p] + 1] - list_offsets[pr[p]];
+      int32_t ke = (int32_t)(k < avail ? k : avail);
+      int32_t len = 0;
+      for (int32_t p = 0; p < nprobe && ke > 0; ++p) {
+        const int32_t c = pr[p];
+        if (c < 0) continue;
+        for (int64_t t = list_offsets[c]; t < list_offsets[c + 1]; ++t) {
+          int32_t id = list_ids[t];
+          float v = orc_dist_f32(data + (int64_t)id * d, qv, d, metric);
+          if (len < ke) {
+            heap[len].dist = v;
+            heap[len].id = id;
+            ++len;
+            heap_sift_up(heap, len);
+          } else if (v < heap[0].dist) {
+            heap[0].dist = v;
+            heap[0].id = id;
+            heap_sift_down(heap, len, 1);
+          }
+        }
+      }
+      qsort(heap, (size_t)len, sizeof(nb_t), nb_cmp);
+      for (int32_t i = 0; i < k; ++i) {
+        ids[qi * (int64_t)k + i] = i < len ? (int32_t)heap[i].id : -1;
+        dists[qi * (int64_t)k + i] = i < len ? heap[i].dist : INFINITY;
+      }
+    }
+    free(heap);
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------ CPU baseline */
 
 static inline float dist_simd16(const float* x, const float* y, int32_t d, int32_t metric) {

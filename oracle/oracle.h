@@ -100,6 +100,15 @@ int orc_ivf_query_f32(const float* data, int32_t d, const float* centroids,
                       int32_t nprobe, int32_t metric, int32_t centroid_metric, int32_t* ids,
                       float* dists, int32_t nthreads);
 
+/* The list scan of the IVF-Flat query (src/indices/ivf_flat.jl:153-167) for
+ * given probes [nq][nprobe] (0-based list ids, -1 = none): k_eff =
+ * min(k, points in the probed lists), BoundedMaxHeap admission, final (dist,
+ * id) sort.  Output [nq][k] padded with -1 / +inf. */
+int orc_ivf_scan_f32(const float* data, int32_t d, const int64_t* list_offsets,
+                     const int32_t* list_ids, const float* q, int64_t nq, const int32_t* probes,
+                     int32_t nprobe, int32_t k, int32_t metric, int32_t* ids, float* dists,
+                     int32_t nthreads);
+
 /* Reference-algorithm CPU baseline (timed, not a parity oracle): per query all
  * n distances into a vector, then a (dist, index) selection; threads over the
  * queries when there are at least 64 of them, else over the points
