@@ -192,6 +192,63 @@ mann_status mann_ivf_scan_device(const mann_knn_params* p, const int32_t* probes
                                  const float* queries, int64_t q, int32_t* out_ids,
                                  float* out_dists, void* stream);
 
+/* ----------------------------------------------------- learned coarse probe
+ * No counterpart in the reference: a routing strategy beside TopKRouting
+ * (select_indices, src/indices/multilevel/routing.jl:91-118) that ranks the
+ * IVF lists of a query with a BF16 MLP din -> hidden1 -> hidden2 -> nout
+ * (GELU after both hidden layers), trained on the GPU with softmax
+ * cross-entropy against the lists holding the query's exact neighbours.
+ * With use_prior the score of list c is MLP(q)_c - beta ||q - c||^2, beta =
+ * exp(theta) learned with the rest.
+ * Flat FP32 parameters (mann_probe_param_count floats): W1[hidden1][din],
+ * b1[hidden1], W2[hidden2][hidden1], b2[hidden2], W3[nout][hidden2], b3[nout],
+ * theta. */
+typedef struct {
+  int32_t din, hidden1, hidden2, nout;
+  int32_t batch;      /* training rows per step (<= 0: 1024) */
+  int32_t use_prior;  /* 1: add the distance prior (needs the centroids) */
+  float lr, beta1, beta2, eps, weight_decay; /* AdamW (<= 0: 1e-3, 0.9, 0.999, 1e-8; decay as given) */
+  float beta_init;    /* initial beta of the prior (<= 0: 1) */
+  uint64_t seed;      /* initialisation and shuffling */
+} mann_probe_params;
+
+typedef struct mann_probe mann_probe; /* device-resident model */
+
+int64_t mann_probe_param_count(const mann_probe_params* p);
+/* Seeded initialisation (uniform +-1/sqrt(fan_in); with the prior the output
+ * layer starts 20x smaller and its bias at zero). */
+mann_status mann_probe_init(const mann_probe_params* p, float* params);
+/* Model on the current device from flat params; centroids [nout][din] for the prior. */
+mann_status mann_probe_create(const mann_probe_params* p, const float* params, const float* centroids,
+                              mann_probe** out);
+mann_status mann_probe_destroy(mann_probe* m);
+mann_status mann_probe_get_params(mann_probe* m, float* params);
+/* AdamW training on host queries [nq][din], labels [nq][nlabel] (list ids,
+ * -1 = none); out_loss[epochs] = mean loss of each epoch (nullable). */
+mann_status mann_probe_train(mann_probe* m, const float* queries, int64_t nq, const int32_t* labels,
+                             int32_t nlabel, int32_t epochs, float* out_loss);
+/* Loss and gradient of one batch (nq <= 65536) without an update. */
+mann_status mann_probe_grad(mann_probe* m, const float* queries, int64_t nq, const int32_t* labels,
+                            int32_t nlabel, float* out_grad, float* out_loss);
+/* Scores [nq][nout] of host queries. */
+mann_status mann_probe_scores(mann_probe* m, const float* queries, int64_t nq, float* out_scores);
+/* Device queries [q][din] -> probes [q][nprobe] (best list first; ties to the
+ * lower id) and the softmax mass of the chosen lists (nullable). */
+mann_status mann_probe_route_device(mann_probe* m, const float* queries, int64_t q, int32_t nprobe,
+                                    int32_t* out_probes, float* out_coverage, void* stream);
+/* IVF search routed by the model (device pointers): mann_ivf_search_device
+ * with the probes chosen by the scores instead of the centroid distances. */
+mann_status mann_ivf_search_learned_device(mann_probe* m, const mann_knn_params* p, int32_t nprobe,
+                                           const float* data, int64_t n, int32_t d, int32_t nlist,
+                                           const int64_t* list_offsets, const int32_t* list_ids,
+                                           const float* queries, int64_t q, int32_t* out_ids,
+                                           float* out_dists, void* stream);
+/* Same with host buffers. */
+mann_status mann_ivf_search_learned(mann_probe* m, const mann_knn_params* p, int32_t nprobe, const float* data,
+                                    int64_t n, int32_t d, int32_t nlist, const int64_t* list_offsets,
+                                    const int32_t* list_ids, const float* queries, int64_t q,
+                                    int32_t* out_ids, float* out_dists);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python

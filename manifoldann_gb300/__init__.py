@@ -15,6 +15,7 @@ from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, ass
                          assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
                          pairwise_distances, take_pending_assignments, transform)
 from .ivf import IVFFlatIndex, TopKRouting, ivf_search_device, select_indices
+from .probe import LearnedProbeRouting, ProbeModel, ivf_search_learned, neighbour_list_labels
 from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
                       index_distance, insert, knn_arrays, neighbor_ids, query, supports_mutation)
 
@@ -31,4 +32,5 @@ __all__ = [
     "get_bucket_assignment", "init_kmeans_plus_plus", "lloyd", "pairwise_distances",
     "take_pending_assignments", "transform",
     "IVFFlatIndex", "TopKRouting", "ivf_search_device", "select_indices",
+    "LearnedProbeRouting", "ProbeModel", "ivf_search_learned", "neighbour_list_labels",
 ]

@@ -96,6 +96,24 @@ class IvfBuildParams(C.Structure):
     ]
 
 
+class ProbeParams(C.Structure):
+    _fields_ = [
+        ("din", C.c_int32),
+        ("hidden1", C.c_int32),
+        ("hidden2", C.c_int32),
+        ("nout", C.c_int32),
+        ("batch", C.c_int32),
+        ("use_prior", C.c_int32),
+        ("lr", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+        ("weight_decay", C.c_float),
+        ("beta_init", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -124,6 +142,19 @@ SIGNATURES = {
                                _I64, _P, _P]),
     "mann_ivf_search_device": (_I32, [C.POINTER(KnnParams), _I32, _I32, _P, _I64, _I32, _P, _I32, _P,
                                       _P, _P, _I64, _P, _P, _P]),
+    "mann_probe_param_count": (_I64, [C.POINTER(ProbeParams)]),
+    "mann_probe_init": (_I32, [C.POINTER(ProbeParams), _P]),
+    "mann_probe_create": (_I32, [C.POINTER(ProbeParams), _P, _P, C.POINTER(_P)]),
+    "mann_probe_destroy": (_I32, [_P]),
+    "mann_probe_get_params": (_I32, [_P, _P]),
+    "mann_probe_train": (_I32, [_P, _P, _I64, _P, _I32, _I32, _P]),
+    "mann_probe_grad": (_I32, [_P, _P, _I64, _P, _I32, _P, _P]),
+    "mann_probe_scores": (_I32, [_P, _P, _I64, _P]),
+    "mann_probe_route_device": (_I32, [_P, _P, _I64, _I32, _P, _P, _P]),
+    "mann_ivf_search_learned_device": (_I32, [_P, C.POINTER(KnnParams), _I32, _P, _I64, _I32, _I32, _P, _P,
+                                              _P, _I64, _P, _P, _P]),
+    "mann_ivf_search_learned": (_I32, [_P, C.POINTER(KnnParams), _I32, _P, _I64, _I32, _I32, _P, _P, _P,
+                                       _I64, _P, _P]),
     "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                     _I64, _P, _P, _P]),
 }

@@ -65,6 +65,11 @@ enum ScratchSlot : int {
   SLOT_IVF_MEMBERS,   // IVF build: members grouped by list
   SLOT_IVF_LOFF,      // host-pointer IVF calls: list offsets
   SLOT_IVF_LIDS,      // host-pointer IVF calls: list ids
+  SLOT_PROBE_X,       // learned probe: BF16 queries
+  SLOT_PROBE_H1,      // learned probe: first hidden layer
+  SLOT_PROBE_H2,      // learned probe: second hidden layer
+  SLOT_PROBE_LOGITS,  // learned probe: output scores
+  SLOT_PROBE_D,       // learned probe: squared distances to the centroids
   SLOT_COUNT
 };
 

@@ -166,11 +166,18 @@ def _order_keys(d: np.ndarray) -> np.ndarray:
     return np.where(np.isnan(d), np.uint32(0xFFFFFFFF), k)
 
 
-def select_indices(policy: TopKRouting, distances, indices):
+def select_indices(policy, distances, indices):
     """``select_indices(::TopKRouting, assignment, indices)`` (routing.jl:94-118):
     1-based indices of the min(k, available) smallest of the first
     ``available = min(len(indices), len(distances))`` distances, ascending by
-    (distance, index).  ``indices`` is the list of child indices or its length."""
+    (distance, index).  ``indices`` is the list of child indices or its length.
+    For a LearnedProbeRouting the second argument is the query vector."""
+    if not isinstance(policy, TopKRouting):
+        from .probe import LearnedProbeRouting, select_indices_learned
+
+        if isinstance(policy, LearnedProbeRouting):
+            return select_indices_learned(policy, distances, indices)
+        raise ArgumentError(f"no select_indices method for {type(policy).__name__}")
     n_children = indices if isinstance(indices, int) else len(indices)
     if n_children <= 0:
         return []
