@@ -37,7 +37,12 @@ sys.path.insert(0, str(ROOT))
 
 N_POINTS, N_QUERIES, DIM, K = 60000, 10000, 784, 10
 WORKLOAD = "quantized-mixture-784d: N=60000 points + Q=10000 held-out queries, SqEuclidean, k=10, plus the 60000-point self kNN graph"
-METRIC = "kNN queries/s (BF16+rerank exact kNN at recall@10=1.0)"
+METRIC = "kNN queries/s: BF16+rerank vs FP32 at recall@10=1.0; learned-probe QPS@0.95"
+IVF_N, IVF_Q, IVF_D, IVF_NLIST, IVF_TRAIN = 1_000_000, 10_000, 128, 4096, 200_000
+IVF_WORKLOAD = ("anisotropic-clusters-128d: N=1,000,000 points from 1,024 Gaussian clusters (sigma per dim "
+                "log-uniform in [0.05, 0.5]), Q=10,000 queries, SqEuclidean, k=10; IVF-Flat nlist=4,096 "
+                "(KMeans: k-means++ + 25 Lloyd iterations); probe MLP 128-512-512-4096 (GELU) trained on the "
+                "exact top-10 lists of 200,000 separate training queries")
 
 
 def parse():
@@ -49,7 +54,9 @@ def parse():
     ap.add_argument("--fp32-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--case", choices=["full", "profile"], default="full",
+    ap.add_argument("--ivf-epochs", type=int, default=30)
+    ap.add_argument("--no-ivf", action="store_true", help="skip the learned-probe IVF leg")
+    ap.add_argument("--case", choices=["full", "profile", "ivf"], default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
                          "launches per step), for ncu captures")
     return ap.parse_args()
@@ -211,6 +218,129 @@ def run_profile_case(args):
     return 0
 
 
+def run_ivf_leg(args, stream_ptr=0):
+    """Learned-probe IVF beside the exact scan on the 1M x 128 set: build,
+    train, sweep nprobe for the learned probe and for centroid routing, and
+    time each at the smallest nprobe that reaches recall@10 >= 0.95."""
+    import torch
+
+    import manifoldann_gb300 as M
+    from manifoldann_gb300 import _lib, synthetic
+    from manifoldann_gb300.probe import neighbour_list_labels
+
+    lib = _lib.load()
+    X = synthetic.anisotropic_clusters(IVF_N, IVF_D, seed=1)
+    TQ = synthetic.anisotropic_clusters(IVF_TRAIN, IVF_D, seed=2)
+    Q = synthetic.anisotropic_clusters(IVF_Q, IVF_D, seed=3)
+    t0 = time.perf_counter()
+    idx = M.build_index(M.IVFFlatIndex, X.T, nlist=IVF_NLIST, distance=M.SqEuclidean(), seed=1)
+    build_s = time.perf_counter() - t0
+    dev = torch.device("cuda")
+    Xd = torch.from_numpy(X).to(dev)
+    Qd = torch.from_numpy(Q).to(dev)
+    Cd = torch.from_numpy(np.ascontiguousarray(idx.centroids.T)).to(dev)
+    od = torch.from_numpy(idx.list_offsets).to(dev)
+    idd = torch.from_numpy(idx.list_ids).to(dev)
+    oi = torch.empty((IVF_Q, K), dtype=torch.int32, device=dev)
+    odist = torch.empty((IVF_Q, K), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    exact = {}
+    for name, prec in (("fp32", _lib.PREC_FP32), ("bf16", _lib.PREC_BF16)):
+        pp = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, prec)
+        ms = timed(lambda: _lib.check(lib.mann_knn_device(pp, Xd.data_ptr(), IVF_N, Qd.data_ptr(), IVF_Q, IVF_D,
+                                                          oi.data_ptr(), odist.data_ptr(), None, stream_ptr)),
+                   2 if prec == _lib.PREC_FP32 else 5)
+        exact[name] = {"ms": ms, "qps": IVF_Q / (ms / 1e3)}
+    truth = oi.cpu().numpy().copy()  # the BF16 form's certified exact top-10
+    t0 = time.perf_counter()
+    labels = neighbour_list_labels(idx, X.T, TQ.T, K)
+    label_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    model = M.ProbeModel(IVF_D, IVF_NLIST, (512, 512), use_prior=False, batch=1024, lr=1e-3,
+                         weight_decay=1e-4, seed=0)
+    loss = model.train(TQ, labels, args.ivf_epochs)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_FP32)
+
+    def learned(npb):
+        _lib.check(lib.mann_ivf_search_learned_device(model.handle, p, npb, Xd.data_ptr(), IVF_N, IVF_D, IVF_NLIST,
+                                                      od.data_ptr(), idd.data_ptr(), Qd.data_ptr(), IVF_Q,
+                                                      oi.data_ptr(), odist.data_ptr(), stream_ptr))
+
+    def centroid(npb):
+        _lib.check(lib.mann_ivf_search_device(p, npb, _lib.METRIC_SQEUCLIDEAN, Xd.data_ptr(), IVF_N, IVF_D,
+                                              Cd.data_ptr(), IVF_NLIST, od.data_ptr(), idd.data_ptr(),
+                                              Qd.data_ptr(), IVF_Q, oi.data_ptr(), odist.data_ptr(), stream_ptr))
+
+    def recall():
+        got = oi.cpu().numpy()
+        return float(sum(len(set(got[i]) & set(truth[i])) for i in range(IVF_Q)) / (10.0 * IVF_Q))
+
+    out = {}
+    for name, fn in (("learned", learned), ("centroid", centroid)):
+        sweep, chosen = [], None
+        for npb in (1, 2, 3, 4, 5, 6, 8, 12, 16, 24, 32):
+            fn(npb)
+            torch.cuda.synchronize()
+            r = recall()
+            sweep.append([npb, r])
+            if r >= 0.95:
+                chosen = (npb, r)
+                break
+        res = {"sweep": sweep}
+        if chosen:
+            ms = timed(lambda: fn(chosen[0]), max(args.steps, 5))
+            res.update({"nprobe": chosen[0], "recall_at_10": chosen[1], "ms": ms, "qps": IVF_Q / (ms / 1e3)})
+        out[name] = res
+    # e2e: host buffers through the C ABI (data, queries and lists copied every call)
+    e2e = None
+    if "qps" in out["learned"] and not args.no_e2e:
+        hq = np.ascontiguousarray(Q)
+        hi = np.empty((IVF_Q, K), np.int32)
+        hd = np.empty((IVF_Q, K), np.float32)
+        lib.mann_host_register(X.ctypes.data, X.nbytes)
+        lib.mann_host_register(hq.ctypes.data, hq.nbytes)
+        npb = out["learned"]["nprobe"]
+
+        def host():
+            _lib.check(lib.mann_ivf_search_learned(model.handle, p, npb, X.ctypes.data, IVF_N, IVF_D, IVF_NLIST,
+                                                   idx.list_offsets.ctypes.data, idx.list_ids.ctypes.data,
+                                                   hq.ctypes.data, IVF_Q, hi.ctypes.data, hd.ctypes.data))
+
+        host()
+        t0 = time.perf_counter()
+        reps = max(3, min(args.steps, 10))
+        for _ in range(reps):
+            host()
+        dt = (time.perf_counter() - t0) / reps
+        lib.mann_host_unregister(X.ctypes.data)
+        lib.mann_host_unregister(hq.ctypes.data)
+        e2e = {"value": IVF_Q / dt, "unit": "queries/s",
+               "h2d_bytes_per_step": int(X.nbytes + hq.nbytes + idx.list_offsets.nbytes + idx.list_ids.nbytes),
+               "d2h_bytes_per_step": int(IVF_Q * K * 8)}
+    best_exact = max(exact["fp32"]["qps"], exact["bf16"]["qps"])
+    res = {"workload": IVF_WORKLOAD, "build_s": build_s, "label_s": label_s, "train_s": train_s,
+           "train_epochs": args.ivf_epochs, "final_loss": float(loss[-1]), "exact": exact,
+           "learned": out["learned"], "centroid_routing": out["centroid"], "e2e_learned": e2e}
+    if "qps" in out["learned"]:
+        res["learned_over_exact"] = out["learned"]["qps"] / best_exact
+        res["learned_over_exact_fp32"] = out["learned"]["qps"] / exact["fp32"]["qps"]
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -335,6 +465,7 @@ def run_ours(args):
             "peak_source": f"{peak_src} bf16 dense (sustained)", "kernel": "k2_main (tcgen05 BF16 tiles + fused top-(k+m))",
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step_main)}
     cpu = cpu_baseline(base, q, args.cpu_seconds) if args.cpu_seconds > 0 else None
+    ivf = None if args.no_ivf else run_ivf_leg(args, sp)
     line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
@@ -346,7 +477,7 @@ def run_ours(args):
             "rows_fallback_per_step": fallback / args.steps,
             "candidates_per_query": cands / (args.steps * qps_step),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": launches}
+            "gpu_launches": launches, "ivf_learned_probe": ivf}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -359,6 +490,12 @@ def main():
         return run_reference(args)
     if args.case == "profile":
         return run_profile_case(args)
+    if args.case == "ivf":
+        import torch
+
+        print(json.dumps({"case": "ivf", "ivf_learned_probe": run_ivf_leg(
+            args, C.c_void_p(torch.cuda.current_stream().cuda_stream))}), flush=True)
+        return 0
     return run_ours(args)
 
 
