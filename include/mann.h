@@ -108,6 +108,23 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
                                   int32_t d, int32_t include_self, int32_t* out_ids,
                                   float* out_dists, mann_knn_report* report, void* stream);
 
+/* kNN graphs of nsets independent point sets stored back to back: set c is
+ * rows [set_offsets[c], set_offsets[c+1]) of data (set_offsets[0] = 0, host
+ * array of nsets+1).  Replaces a loop of build_knn_graph calls, one per set
+ * (src/graphs/knn_graph.jl:42-81), with one launch over all sets (FP32 form,
+ * Euclidean / SqEuclidean, k + (include_self ? 0 : 1) <= 32); row r of out
+ * holds the graph row of point r with ids local to its set.  The launches of
+ * a (buffers, sizes) signature are captured into a CUDA graph on first use
+ * and replayed; the tile height and split count come from a measuring
+ * autotuner (first call of a signature runs each candidate once). */
+mann_status mann_knn_graph_batched(const mann_knn_params* p, const float* data, const int64_t* set_offsets,
+                                   int32_t nsets, int32_t d, int32_t include_self, int32_t* out_ids,
+                                   float* out_dists, mann_knn_report* report);
+/* Same with device data and outputs (set_offsets stays a host array). */
+mann_status mann_knn_graph_batched_device(const mann_knn_params* p, const float* data, const int64_t* set_offsets,
+                                          int32_t nsets, int32_t d, int32_t include_self, int32_t* out_ids,
+                                          float* out_dists, mann_knn_report* report, void* stream);
+
 /* ------------------------------------------------------------ KMeans (KMeansTransform) */
 
 typedef struct {

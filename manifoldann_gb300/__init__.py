@@ -9,8 +9,8 @@ from ._lib import ArgumentError, DimensionMismatch, MannError
 from .distances import (CosineDist, Euclidean, SqEuclidean, cosine_distance, default_distance,
                         default_squared_distance, euclidean_distance)
 from .eval_utils import recall_at_k
-from .graphs import (KNNGraph, build_knn_graph, graph_metadata, has_metadata, knn_graph_arrays,
-                     node_metadata)
+from .graphs import (KNNGraph, build_knn_graph, build_knn_graphs, graph_metadata, has_metadata,
+                     knn_graph_arrays, knn_graph_batched_arrays, node_metadata)
 from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, assign_arrays,
                          assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
                          pairwise_distances, take_pending_assignments, transform)
@@ -24,8 +24,8 @@ __all__ = [
     "CosineDist", "Euclidean", "SqEuclidean", "cosine_distance", "default_distance",
     "default_squared_distance", "euclidean_distance",
     "recall_at_k",
-    "KNNGraph", "build_knn_graph", "graph_metadata", "has_metadata", "knn_graph_arrays",
-    "node_metadata",
+    "KNNGraph", "build_knn_graph", "build_knn_graphs", "graph_metadata", "has_metadata", "knn_graph_arrays",
+    "knn_graph_batched_arrays", "node_metadata",
     "AbstractANNIndex", "BruteForceIndex", "Neighbor", "build_index", "configured_k",
     "index_distance", "insert", "knn_arrays", "neighbor_ids", "query", "supports_mutation",
     "KMeansAssignment", "KMeansTransform", "TransformResult", "assign_arrays", "assign_clusters", "fit",

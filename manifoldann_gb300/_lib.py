@@ -155,6 +155,10 @@ SIGNATURES = {
                                               _P, _I64, _P, _P, _P]),
     "mann_ivf_search_learned": (_I32, [_P, C.POINTER(KnnParams), _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                        _I64, _P, _P]),
+    "mann_knn_graph_batched": (_I32, [C.POINTER(KnnParams), _P, _P, _I32, _I32, _I32, _P, _P,
+                                      C.POINTER(KnnReport)]),
+    "mann_knn_graph_batched_device": (_I32, [C.POINTER(KnnParams), _P, _P, _I32, _I32, _I32, _P, _P,
+                                             C.POINTER(KnnReport), _P]),
     "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                     _I64, _P, _P, _P]),
 }

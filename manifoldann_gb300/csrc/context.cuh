@@ -70,6 +70,8 @@ enum ScratchSlot : int {
   SLOT_PROBE_H2,      // learned probe: second hidden layer
   SLOT_PROBE_LOGITS,  // learned probe: output scores
   SLOT_PROBE_D,       // learned probe: squared distances to the centroids
+  SLOT_BATCH_ITEMS,   // batched graphs: work items
+  SLOT_BATCH_OFFS,    // batched graphs: set offsets
   SLOT_COUNT
 };
 

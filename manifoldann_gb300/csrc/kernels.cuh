@@ -62,6 +62,16 @@ mann_status exact_search_device(Context* ctx, cudaStream_t s, const mann_knn_par
                                 mann_knn_report* rep);
 
 // Merge nsplit sorted key lists of k per query (nsplit <= 128) into one.
+// Work item of the segmented FP32 tile kernel (batched point sets).
+struct SegItem {
+  int64_t q0, qend, nb0, nb1;
+  int32_t split, pad;
+};
+mann_status launch_k1_segmented(const float* data, const SegItem* items, int nitems, int d, int metric, int bq,
+                                int k, int nsplit, uint64_t* partial, cudaStream_t s);
+mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_knn_params* p, const float* data,
+                                     const int64_t* offs, int nsets, int d, int include_self, int32_t* ids,
+                                     float* dists, mann_knn_report* rep);
 mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, int k, uint64_t* out,
                                cudaStream_t s);
 

@@ -162,28 +162,25 @@ struct StageLoader {
   }
 };
 
+// One CTA's work: queries [q0, min(q0 + BQ, nq)) against points [nb0, nb1);
+// the sorted list of query row gq goes to dst + gq * dst_stride.
 template <int METRIC, int BQ, int KW, bool VEC>
-__global__ void __launch_bounds__(K1_THREADS, 1)
-    k1_tile_topk(const float* __restrict__ base, int64_t n, const float* __restrict__ qs,
-                 const int32_t* __restrict__ qrows, int64_t nq, int d,
-                 const float* __restrict__ qnorm, const float* __restrict__ bnorm, int k,
-                 int64_t split_len, int nsplit, uint64_t* __restrict__ partial) {
+__device__ __forceinline__ void k1_body(const float* __restrict__ base, int64_t nb0, int64_t nb1,
+                                        const float* __restrict__ qs, const int32_t* __restrict__ qrows,
+                                        int64_t q0, int64_t nq, int d, const float* __restrict__ qnorm,
+                                        const float* __restrict__ bnorm, int k, uint64_t* __restrict__ dst0,
+                                        int64_t dst_stride, float* smem) {
   constexpr int TQ = BQ / 16;
   constexpr int TN = 8;
   constexpr int RPW = BQ / 8;
   constexpr int QSTR = BQ + 4;
   constexpr int BSTR = K1_BN + 4;
-  extern __shared__ float4 k1_smem[];
-  float* Qs = reinterpret_cast<float*>(k1_smem);  // [2][DK][QSTR]
-  float* Bs = Qs + 2 * K1_DK * QSTR;               // [2][DK][BSTR]
-  float* Dt = Bs + 2 * K1_DK * BSTR;               // [BQ][BSTR]
+  float* Qs = smem;                   // [2][DK][QSTR]
+  float* Bs = Qs + 2 * K1_DK * QSTR;  // [2][DK][BSTR]
+  float* Dt = Bs + 2 * K1_DK * BSTR;  // [BQ][BSTR]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ty = tid >> 4, tx = tid & 15;
-  const int64_t q0 = (int64_t)blockIdx.x * BQ;
-  const int split = blockIdx.y;
-  const int64_t nb0 = (int64_t)split * split_len;
-  const int64_t nb1 = min(n, nb0 + split_len);
   const int nchunks = (d + K1_DK - 1) / K1_DK;
 
   uint64_t L[RPW][KW];
@@ -316,13 +313,43 @@ __global__ void __launch_bounds__(K1_THREADS, 1)
   for (int r = 0; r < RPW; ++r) {
     const int64_t gq = q0 + warp * RPW + r;
     if (gq >= nq) continue;
-    uint64_t* dst = partial + (gq * nsplit + split) * (int64_t)k;
+    uint64_t* dst = dst0 + gq * dst_stride;
 #pragma unroll
     for (int s = 0; s < KW; ++s) {
       const int e = s * 32 + lane;
       if (e < k) dst[e] = L[r][s];
     }
   }
+}
+
+template <int METRIC, int BQ, int KW, bool VEC>
+__global__ void __launch_bounds__(K1_THREADS, 1)
+    k1_tile_topk(const float* __restrict__ base, int64_t n, const float* __restrict__ qs,
+                 const int32_t* __restrict__ qrows, int64_t nq, int d,
+                 const float* __restrict__ qnorm, const float* __restrict__ bnorm, int k,
+                 int64_t split_len, int nsplit, uint64_t* __restrict__ partial) {
+  extern __shared__ float4 k1_smem[];
+  const int split = blockIdx.y;
+  const int64_t nb0 = (int64_t)split * split_len;
+  const int64_t nb1 = min(n, nb0 + split_len);
+  k1_body<METRIC, BQ, KW, VEC>(base, nb0, nb1, qs, qrows, (int64_t)blockIdx.x * BQ, nq, d, qnorm, bnorm, k,
+                               partial + (int64_t)split * k, (int64_t)nsplit * k,
+                               reinterpret_cast<float*>(k1_smem));
+}
+
+// Segmented form: one launch over the work items of many independent point
+// sets stored back to back; item i covers queries [q0, qend) of one set
+// against that set's points [nb0, nb1) (global rows, so the keys carry global
+// ids), writing split slot `split` of each query's lists.
+template <int METRIC, int BQ, bool VEC>
+__global__ void __launch_bounds__(K1_THREADS, 1)
+    k1_segmented(const float* __restrict__ data, const SegItem* __restrict__ items, int d, int k, int nsplit,
+                 uint64_t* __restrict__ partial) {
+  extern __shared__ float4 k1_smem[];
+  const SegItem it = items[blockIdx.x];
+  k1_body<METRIC, BQ, 1, VEC>(data, it.nb0, it.nb1, data, nullptr, it.q0, it.qend, d, nullptr, nullptr, k,
+                              partial + (int64_t)it.split * k, (int64_t)nsplit * k,
+                              reinterpret_cast<float*>(k1_smem));
 }
 
 // Merge nsplit sorted lists of k keys per query into one sorted list of k.
@@ -427,6 +454,40 @@ mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const
 }
 
 }  // namespace
+
+template <int METRIC, int BQ, bool VEC>
+static mann_status launch_seg_t(const float* data, const SegItem* items, int nitems, int d, int k, int nsplit,
+                                uint64_t* partial, cudaStream_t s) {
+  constexpr int QSTR = BQ + 4, BSTR = K1_BN + 4;
+  const size_t smem = sizeof(float) * (2 * K1_DK * QSTR + 2 * K1_DK * BSTR + BQ * BSTR);
+  auto kern = k1_segmented<METRIC, BQ, VEC>;
+  MANN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)nitems, K1_THREADS, smem, s>>>(data, items, d, k, nsplit, partial);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
+mann_status launch_k1_segmented(const float* data, const SegItem* items, int nitems, int d, int metric, int bq,
+                                int k, int nsplit, uint64_t* partial, cudaStream_t s) {
+  if (k < 1 || k > 32) return fail(MANN_EINVAL_ARG, "batched graphs support 1 <= k <= 32 (k+1 with self)");
+  if (nitems <= 0) return MANN_OK;
+  const bool vec = (d % 4) == 0;
+#define SEG_CASE(M, B)                                                                       \
+  return vec ? launch_seg_t<M, B, true>(data, items, nitems, d, k, nsplit, partial, s)       \
+             : launch_seg_t<M, B, false>(data, items, nitems, d, k, nsplit, partial, s)
+  if (metric == MANN_METRIC_EUCLIDEAN) {
+    if (bq == 64) SEG_CASE(MANN_METRIC_EUCLIDEAN, 64);
+    if (bq == 32) SEG_CASE(MANN_METRIC_EUCLIDEAN, 32);
+    SEG_CASE(MANN_METRIC_EUCLIDEAN, 128);
+  }
+  if (metric == MANN_METRIC_SQEUCLIDEAN) {
+    if (bq == 64) SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 64);
+    if (bq == 32) SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 32);
+    SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 128);
+  }
+#undef SEG_CASE
+  return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
+}
 
 mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, int k, uint64_t* out,
                                cudaStream_t s) {

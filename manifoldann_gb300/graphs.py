@@ -93,6 +93,47 @@ def knn_graph_arrays(index: BruteForceIndex, data, k: int, *, include_self: bool
     return ids, dists
 
 
+def knn_graph_batched_arrays(clouds, k: int, *, distance=None, include_self: bool = False,
+                             report: bool = False):
+    """Self-kNN graphs of many point sets (each d x n_i) in one library call:
+    (ids [sum n_i, k] 0-based ids local to each set, dists, offsets [nsets+1])."""
+    from .distances import default_distance
+
+    mats = [np.asarray(c) for c in clouds]
+    if not mats:
+        raise ArgumentError("at least one point set is needed")
+    d = mats[0].shape[0]
+    if any(m.ndim != 2 or m.shape[0] != d for m in mats):
+        raise ArgumentError("all point sets must be d x n_i matrices of one d")
+    offs = np.zeros(len(mats) + 1, np.int64)
+    offs[1:] = np.cumsum([m.shape[1] for m in mats])
+    pts = np.ascontiguousarray(np.concatenate([m.T for m in mats], axis=0), dtype=np.float32)
+    N = int(offs[-1])
+    ids = np.empty((N, k), np.int32)
+    dists = np.empty((N, k), np.float32)
+    p = _lib.params(metric_code(distance or default_distance), k, _lib.PREC_FP32)
+    rep = _lib.KnnReport()
+    _lib.check(_lib.load().mann_knn_graph_batched(p, pts.ctypes.data, offs.ctypes.data, len(mats), d,
+                                                  int(bool(include_self)), ids.ctypes.data, dists.ctypes.data,
+                                                  rep))
+    if report:
+        return ids, dists, offs, rep.as_dict()
+    return ids, dists, offs
+
+
+def build_knn_graphs(clouds, *, k: int, distance=None, include_self: bool = False) -> list:
+    """``build_knn_graph(build_index(BruteForceIndex, c; distance), c; k, include_self)``
+    for every point set c, as one batched call; a list of KNNGraph."""
+    ids, _, offs = knn_graph_batched_arrays(clouds, k, distance=distance, include_self=include_self)
+    out = []
+    for c in range(len(offs) - 1):
+        block = ids[offs[c]:offs[c + 1]]
+        adjacency = [[int(j) + 1 for j in row] for row in block]
+        out.append(KNNGraph(adjacency, k, include_self,
+                            _create_graph_metadata(k, True, None, int(offs[c + 1] - offs[c]))))
+    return out
+
+
 def build_knn_graph(index, data, *, k: Optional[int] = None, include_self: bool = False,
                     directed: bool = True, metadata=None, **query_kwargs) -> KNNGraph:
     """``build_knn_graph(index, data; k, include_self, directed, metadata)``
