@@ -56,7 +56,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--ivf-epochs", type=int, default=30)
     ap.add_argument("--no-ivf", action="store_true", help="skip the learned-probe IVF leg")
-    ap.add_argument("--case", choices=["full", "profile", "ivf"], default="full",
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven graphs leg")
+    ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "ivf-profile"], default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
                          "launches per step), for ncu captures")
     return ap.parse_args()
@@ -341,6 +342,93 @@ def run_ivf_leg(args, stream_ptr=0):
     return res
 
 
+BATCH_WORKLOAD = ("manifold-clouds-32d: 64 point clouds, sizes log-uniform in [2,000, 50,000] (Swiss roll, "
+                  "2-sphere, torus in R^3, zero-padded to 32-d, rotated, noise 0.01), SqEuclidean self-kNN k=15 "
+                  "per cloud, one launch per step replayed from a CUDA graph")
+
+
+def run_batched_leg(args, stream_ptr=0):
+    """Config of uneven batched graphs: every step builds all 64 clouds' graphs."""
+    import torch
+
+    from manifoldann_gb300 import _lib, synthetic
+
+    lib = _lib.load()
+    clouds = synthetic.manifold_clouds(64, 2000, 50000, 32, seed=0)
+    offs = np.zeros(65, np.int64)
+    offs[1:] = np.cumsum([len(c) for c in clouds])
+    N = int(offs[-1])
+    pairs = float(sum(float(len(c)) ** 2 for c in clouds))
+    X = torch.from_numpy(np.concatenate(clouds)).cuda()
+    ids = torch.empty((N, 15), dtype=torch.int32, device="cuda")
+    d = torch.empty((N, 15), dtype=torch.float32, device="cuda")
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, 15, _lib.PREC_FP32, 0, _lib.FLAG_TIME_KERNEL)
+    r = _lib.KnnReport()
+
+    def step():
+        _lib.check(lib.mann_knn_graph_batched_device(p, X.data_ptr(), offs.ctypes.data, 64, 32, 0, ids.data_ptr(),
+                                                     d.data_ptr(), r, stream_ptr))
+
+    for _ in range(max(args.warmup, 2)):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 20))
+    kernel_ms = 0.0
+    e0.record(stream)
+    for _ in range(reps):
+        step()
+        kernel_ms += r.kernel_ms
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    achieved = 2.0 * 32 * pairs / (ms / 1e3) / 1e12
+    return {"workload": BATCH_WORKLOAD, "points": N, "pairs": pairs, "ms_per_step": ms,
+            "graph_ms_per_step": kernel_ms / reps, "points_per_s": N / (ms / 1e3), "pairs_per_s": pairs / (ms / 1e3),
+            "autotuned": {"tile_rows": r.margin_used // 100, "splits": r.margin_used % 100},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak, "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2.07 GHz)",
+                         "work": "2*d flops per ordered pair"},
+            "launches_per_step": r.launches}
+
+
+def run_ivf_profile_case(args):
+    """Case for ncu: IVF searches only (learned routing with an untrained
+    network of the same shape -- same kernels and sizes -- then centroid
+    routing), each at nprobe=4 on the 1M x 128 set."""
+    import torch
+
+    import manifoldann_gb300 as M
+    from manifoldann_gb300 import _lib, synthetic
+
+    lib = _lib.load()
+    X = synthetic.anisotropic_clusters(IVF_N, IVF_D, seed=1)
+    Q = synthetic.anisotropic_clusters(IVF_Q, IVF_D, seed=3)
+    idx = M.build_index(M.IVFFlatIndex, X.T, nlist=IVF_NLIST, distance=M.SqEuclidean(), seed=1)
+    model = M.ProbeModel(IVF_D, IVF_NLIST, (512, 512), use_prior=False, seed=0)
+    dev = torch.device("cuda")
+    Xd, Qd = torch.from_numpy(X).to(dev), torch.from_numpy(Q).to(dev)
+    Cd = torch.from_numpy(np.ascontiguousarray(idx.centroids.T)).to(dev)
+    od, idd = torch.from_numpy(idx.list_offsets).to(dev), torch.from_numpy(idx.list_ids).to(dev)
+    oi = torch.empty((IVF_Q, K), dtype=torch.int32, device=dev)
+    odist = torch.empty((IVF_Q, K), dtype=torch.float32, device=dev)
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_FP32)
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for _ in range(args.warmup + args.steps):
+        _lib.check(lib.mann_ivf_search_learned_device(model.handle, p, 4, Xd.data_ptr(), IVF_N, IVF_D, IVF_NLIST,
+                                                      od.data_ptr(), idd.data_ptr(), Qd.data_ptr(), IVF_Q,
+                                                      oi.data_ptr(), odist.data_ptr(), sp))
+    for _ in range(args.warmup + args.steps):
+        _lib.check(lib.mann_ivf_search_device(p, 4, _lib.METRIC_SQEUCLIDEAN, Xd.data_ptr(), IVF_N, IVF_D,
+                                              Cd.data_ptr(), IVF_NLIST, od.data_ptr(), idd.data_ptr(),
+                                              Qd.data_ptr(), IVF_Q, oi.data_ptr(), odist.data_ptr(), sp))
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "ivf-profile", "searches": 2 * (args.warmup + args.steps)}), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -466,6 +554,7 @@ def run_ours(args):
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step_main)}
     cpu = cpu_baseline(base, q, args.cpu_seconds) if args.cpu_seconds > 0 else None
     ivf = None if args.no_ivf else run_ivf_leg(args, sp)
+    batched = None if args.no_batched else run_batched_leg(args, sp)
     line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
@@ -477,7 +566,7 @@ def run_ours(args):
             "rows_fallback_per_step": fallback / args.steps,
             "candidates_per_query": cands / (args.steps * qps_step),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": launches, "ivf_learned_probe": ivf}
+            "gpu_launches": launches, "ivf_learned_probe": ivf, "batched_graphs": batched}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -490,6 +579,14 @@ def main():
         return run_reference(args)
     if args.case == "profile":
         return run_profile_case(args)
+    if args.case == "ivf-profile":
+        return run_ivf_profile_case(args)
+    if args.case == "batched":
+        import torch
+
+        print(json.dumps({"case": "batched", "batched_graphs": run_batched_leg(
+            args, C.c_void_p(torch.cuda.current_stream().cuda_stream))}), flush=True)
+        return 0
     if args.case == "ivf":
         import torch
 
