@@ -52,7 +52,6 @@ enum ScratchSlot : int {
   SLOT_KM_X,          // host-pointer KMeans calls: points
   SLOT_KM_CENT,       // centroids
   SLOT_KM_ASSIGN,     // assignments
-  SLOT_IVF_DATA,      // IVF search: points gathered into list order
   SLOT_IVF_CNT,       // IVF search: per-list query counts and cursors
   SLOT_IVF_OFF,       // IVF search: per-list query and chunk offsets
   SLOT_IVF_PAIRS,     // IVF search: (query, probe rank) pairs grouped by list

@@ -18,15 +18,15 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "warp_list.cuh"
 
 namespace mann {
 
 namespace {
 
-constexpr int SCAN_Q = 32;    // queries per CTA
-constexpr int SCAN_P = 64;    // points per tile
-constexpr int SCAN_D = 64;    // dimensions per stage
-constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_Q = 32;    // queries per CTA (at most)
+constexpr int SCAN_T = 256;   // threads = points per pass
+constexpr int SCAN_DC = 32;   // dimensions per stage
 
 __global__ void ivf_lists_kernel(const int64_t* __restrict__ start, const int64_t* __restrict__ members,
                                  int k, int64_t n, int64_t* __restrict__ offsets,
@@ -34,18 +34,6 @@ __global__ void ivf_lists_kernel(const int64_t* __restrict__ start, const int64_
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) ids[i] = (int32_t)members[i];
   if (i <= k) offsets[i] = i < k ? start[i] : n;
-}
-
-// data rows in list order
-__global__ void gather_lists_kernel(const float* __restrict__ data, int d,
-                                    const int32_t* __restrict__ ids, int64_t n,
-                                    float* __restrict__ out) {
-  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (r >= n) return;
-  const float* src = data + (int64_t)ids[r] * d;
-  float* dst = out + r * d;
-  for (int c = lane; c < d; c += 32) dst[c] = src[c];
 }
 
 __global__ void probe_count_kernel(const int32_t* __restrict__ probes, int64_t np, int nlist,
@@ -56,19 +44,57 @@ __global__ void probe_count_kernel(const int32_t* __restrict__ probes, int64_t n
   if (l >= 0 && l < nlist) atomicAdd(&cnt[l], 1u);
 }
 
-// exclusive prefix sums of per-list query counts and of 32-query chunks
-__global__ void probe_scan_kernel(const unsigned* __restrict__ cnt, int nlist,
-                                  int64_t* __restrict__ qoff, int64_t* __restrict__ choff) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Exclusive prefix sums of the per-list query counts and of their 32-query
+// chunks; one block of 1024 threads, each owning a contiguous run of lists.
+__global__ void __launch_bounds__(1024) probe_scan_kernel(const unsigned* __restrict__ cnt, int nlist,
+                                                          int64_t* __restrict__ qoff,
+                                                          int64_t* __restrict__ choff) {
+  __shared__ int64_t wa[32], wb[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int per = (nlist + 1023) / 1024;
+  const int l0 = min(nlist, t * per), l1 = min(nlist, l0 + per);
   int64_t a = 0, b = 0;
-  for (int l = 0; l < nlist; ++l) {
-    qoff[l] = a;
-    choff[l] = b;
+  for (int l = l0; l < l1; ++l) {
     a += cnt[l];
     b += (cnt[l] + SCAN_Q - 1) / SCAN_Q;
   }
-  qoff[nlist] = a;
-  choff[nlist] = b;
+  int64_t ia = a, ib = b;  // inclusive scans within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t xa = __shfl_up_sync(0xffffffffu, ia, o), xb = __shfl_up_sync(0xffffffffu, ib, o);
+    if (lane >= o) {
+      ia += xa;
+      ib += xb;
+    }
+  }
+  if (lane == 31) {
+    wa[w] = ia;
+    wb[w] = ib;
+  }
+  __syncthreads();
+  if (w == 0) {
+    int64_t va = wa[lane], vb = wb[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t xa = __shfl_up_sync(0xffffffffu, va, o), xb = __shfl_up_sync(0xffffffffu, vb, o);
+      if (lane >= o) {
+        va += xa;
+        vb += xb;
+      }
+    }
+    wa[lane] = va;
+    wb[lane] = vb;
+  }
+  __syncthreads();
+  int64_t ea = ia - a + (w ? wa[w - 1] : 0), eb = ib - b + (w ? wb[w - 1] : 0);
+  for (int l = l0; l < l1; ++l) {
+    qoff[l] = ea;
+    choff[l] = eb;
+    ea += cnt[l];
+    eb += (cnt[l] + SCAN_Q - 1) / SCAN_Q;
+  }
+  if (t == 1023) {
+    qoff[nlist] = ea;
+    choff[nlist] = eb;
+  }
 }
 
 __global__ void probe_scatter_kernel(const int32_t* __restrict__ probes, int64_t nq, int nprobe,
@@ -84,20 +110,22 @@ __global__ void probe_scatter_kernel(const int32_t* __restrict__ probes, int64_t
   pair_r[pos] = (int32_t)(i % nprobe);
 }
 
-// One CTA: list l, its queries [e0, e1) (at most 32).  Thread t serves query
-// t/8 and points t%8 + 8u of every 64-point tile; each thread keeps its own
-// sorted top-k in shared memory, the 8 lists of a query are merged at the end.
-template <int METRIC>
-__global__ void __launch_bounds__(SCAN_THREADS)
-    ivf_scan_kernel(const float* __restrict__ xs, const int64_t* __restrict__ loff,
+// One CTA: list l and up to 32 of its queries.  Each thread takes one point
+// of the list per pass (read in place through the list's ids) and computes
+// its distance to every query of the CTA -- the point's coordinates in
+// registers, the queries' in shared memory, each distance the sequential
+// difference-form sum over dimensions 0..d-1 of the FP32 form.  Warp w keeps
+// the sorted top-k of queries w, w+8, w+16, w+24 as warp-distributed lists.
+template <int METRIC, int KW, bool VEC>
+__global__ void __launch_bounds__(SCAN_T, 2)
+    ivf_scan_kernel(const float* __restrict__ data, const int64_t* __restrict__ loff,
                     const int32_t* __restrict__ lids, const float* __restrict__ qs, int d,
                     const int64_t* __restrict__ qoff, const int32_t* __restrict__ pair_q,
                     const int32_t* __restrict__ pair_r, const int64_t* __restrict__ choff, int nlist,
                     int k, int nprobe, uint64_t* __restrict__ partial) {
-  extern __shared__ uint64_t ivf_smem[];
-  uint64_t* lists = ivf_smem;                                               // [k][256]
-  float* qsm = reinterpret_cast<float*>(lists + (size_t)k * SCAN_THREADS);  // [32][SCAN_D]
-  float* psm = qsm + SCAN_Q * SCAN_D;                                       // [SCAN_D][SCAN_P + 1]
+  __shared__ __align__(16) float qsm[SCAN_Q][SCAN_DC];
+  __shared__ float dsm[SCAN_Q][SCAN_T + 1];
+  __shared__ int32_t s_q[SCAN_Q];
 
   const int64_t w = blockIdx.x;
   if (w >= choff[nlist]) return;
@@ -111,111 +139,151 @@ __global__ void __launch_bounds__(SCAN_THREADS)
   const int64_t e0 = qoff[l] + (w - choff[l]) * SCAN_Q;
   const int nqe = (int)min((int64_t)SCAN_Q, qoff[l + 1] - e0);
   const int64_t p_begin = loff[l], p_end = loff[l + 1];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t < nqe) s_q[t] = pair_q[e0 + t];
+  __syncthreads();
 
-  const int t = threadIdx.x;
-  const int qi = t >> 3, g = t & 7;
-  uint64_t* my = lists + t;  // entry j at my[j * 256]
-  for (int j = 0; j < k; ++j) my[j * SCAN_THREADS] = KEY_NONE;
-  uint64_t thr = KEY_NONE;
-  const int64_t qrow = qi < nqe ? (int64_t)pair_q[e0 + qi] : -1;
+  uint64_t L[4][KW];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int s = 0; s < KW; ++s) L[m][s] = KEY_NONE;
 
-  for (int64_t p0 = p_begin; p0 < p_end; p0 += SCAN_P) {
-    const int np = (int)min((int64_t)SCAN_P, p_end - p0);
-    float acc[8];
+  for (int64_t p0 = p_begin; p0 < p_end; p0 += SCAN_T) {
+    const int64_t pi = p0 + t;
+    const bool valid = pi < p_end;
+    const float* prow = data + (valid ? (int64_t)lids[pi] : 0) * d;
+    float acc[SCAN_Q];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) acc[u] = 0.0f;
-    for (int c0 = 0; c0 < d; c0 += SCAN_D) {
-      const int dc = min(SCAN_D, d - c0);
+    for (int j = 0; j < SCAN_Q; ++j) acc[j] = 0.0f;
+    for (int c0 = 0; c0 < d; c0 += SCAN_DC) {
+      const int dc = min(SCAN_DC, d - c0);
       __syncthreads();
-      for (int e = t; e < SCAN_Q * SCAN_D; e += SCAN_THREADS) {
-        const int r = e / SCAN_D, c = e % SCAN_D;
-        float v = 0.0f;
-        if (r < nqe && c < dc) v = qs[(int64_t)pair_q[e0 + r] * d + c0 + c];
-        qsm[r * SCAN_D + c] = v;
+      for (int e = t; e < SCAN_Q * SCAN_DC; e += SCAN_T) {
+        const int r = e / SCAN_DC, c = e % SCAN_DC;
+        qsm[r][c] = (r < nqe && c < dc) ? __ldg(&qs[(int64_t)s_q[r] * d + c0 + c]) : 0.0f;
       }
-      for (int e = t; e < SCAN_P * SCAN_D; e += SCAN_THREADS) {
-        const int j = e / SCAN_D, c = e % SCAN_D;
-        float v = 0.0f;
-        if (j < np && c < dc) v = xs[(p0 + j) * d + c0 + c];
-        psm[c * (SCAN_P + 1) + j] = v;
-      }
-      __syncthreads();
-      for (int c = 0; c < dc; ++c) {
-        const float qv = qsm[qi * SCAN_D + c];
+      float pv[SCAN_DC];
+      if (VEC && dc == SCAN_DC) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const float tt = __fsub_rn(qv, psm[c * (SCAN_P + 1) + g + 8 * u]);
-          acc[u] = __fmaf_rn(tt, tt, acc[u]);
+        for (int c = 0; c < SCAN_DC; c += 4) {
+          const float4 v = valid ? __ldg(reinterpret_cast<const float4*>(prow + c0 + c)) : make_float4(0, 0, 0, 0);
+          pv[c] = v.x;
+          pv[c + 1] = v.y;
+          pv[c + 2] = v.z;
+          pv[c + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < SCAN_DC; ++c) pv[c] = (valid && c < dc) ? __ldg(prow + c0 + c) : 0.0f;
+      }
+      __syncthreads();
+      // dimensions past d are zero in both operands: (0 - 0)^2 adds nothing
+#pragma unroll
+      for (int j = 0; j < SCAN_Q; ++j) {
+        if (j < nqe) {
+          float a = acc[j];
+#pragma unroll
+          for (int c = 0; c < SCAN_DC; c += 4) {
+            const float4 q4 = *reinterpret_cast<const float4*>(&qsm[j][c]);
+            float u = __fsub_rn(q4.x, pv[c]);
+            a = __fmaf_rn(u, u, a);
+            u = __fsub_rn(q4.y, pv[c + 1]);
+            a = __fmaf_rn(u, u, a);
+            u = __fsub_rn(q4.z, pv[c + 2]);
+            a = __fmaf_rn(u, u, a);
+            u = __fsub_rn(q4.w, pv[c + 3]);
+            a = __fmaf_rn(u, u, a);
+          }
+          acc[j] = a;
         }
       }
     }
-    if (qrow >= 0) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int j = g + 8 * u;
-        if (j >= np) continue;
-        const float v = METRIC == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc[u]) : acc[u];
-        const uint64_t key = make_key(v, (uint32_t)lids[p0 + j]);
-        if (key < thr) {
-          int p = k - 1;
-          while (p > 0) {
-            const uint64_t prev = my[(p - 1) * SCAN_THREADS];
-            if (prev < key) break;
-            my[p * SCAN_THREADS] = prev;
-            --p;
+    for (int j = 0; j < SCAN_Q; ++j)
+      if (j < nqe) dsm[j][t] = METRIC == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc[j]) : acc[j];
+    __syncthreads();
+    const int np = (int)min((int64_t)SCAN_T, p_end - p0);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int j = warp + 8 * m;
+      if (j >= nqe) continue;  // warp-uniform
+      uint64_t thr = wl::list_get<KW>(L[m], k - 1);
+      for (int c8 = 0; c8 < SCAN_T; c8 += 32) {
+        const int col = c8 + lane;
+        const uint64_t key = col < np ? make_key(dsm[j][col], (uint32_t)lids[p0 + col]) : KEY_NONE;
+        unsigned pend = __ballot_sync(wl::FULL, key < thr);
+        while (pend) {
+          const int src = __ffs(pend) - 1;
+          pend &= pend - 1;
+          const uint64_t cnd = __shfl_sync(wl::FULL, key, src);
+          if (cnd < thr) {
+            wl::list_insert<KW>(L[m], cnd, lane);
+            thr = wl::list_get<KW>(L[m], k - 1);
           }
-          my[p * SCAN_THREADS] = key;
-          thr = my[(k - 1) * SCAN_THREADS];
         }
       }
     }
   }
-  __syncthreads();
-  if (g == 0 && qrow >= 0) {
-    // merge the 8 sorted lists of this query
-    int head[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) head[u] = 0;
-    uint64_t* dst = partial + ((int64_t)qrow * nprobe + pair_r[e0 + qi]) * k;
-    for (int e = 0; e < k; ++e) {
-      uint64_t best = KEY_NONE;
-      int bu = 0;
+  for (int m = 0; m < 4; ++m) {
+    const int j = warp + 8 * m;
+    if (j >= nqe) continue;
+    uint64_t* dst = partial + ((int64_t)s_q[j] * nprobe + pair_r[e0 + j]) * k;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const uint64_t v = head[u] < k ? lists[head[u] * SCAN_THREADS + t + u] : KEY_NONE;
-        if (v < best) {
-          best = v;
-          bu = u;
-        }
-      }
-      dst[e] = best;
-      if (best != KEY_NONE) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if (u == bu) ++head[u];
-      }
+    for (int s = 0; s < KW; ++s) {
+      const int e = s * 32 + lane;
+      if (e < k) dst[e] = L[m][s];
     }
   }
 }
 
+
+template <int METRIC, int KW, bool VEC>
+mann_status launch_scan_t(cudaStream_t s, int64_t grid, const float* data, const int64_t* loff,
+                          const int32_t* lids, const float* qs, int d, const int64_t* qoff,
+                          const int32_t* pair_q, const int32_t* pair_r, const int64_t* choff, int nlist, int k,
+                          int nprobe, uint64_t* partial) {
+  ivf_scan_kernel<METRIC, KW, VEC><<<(unsigned)grid, SCAN_T, 0, s>>>(data, loff, lids, qs, d, qoff, pair_q, pair_r,
+                                                                     choff, nlist, k, nprobe, partial);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
+template <int METRIC>
+mann_status launch_scan_m(cudaStream_t s, int64_t grid, bool vec, const float* data, const int64_t* loff,
+                          const int32_t* lids, const float* qs, int d, const int64_t* qoff,
+                          const int32_t* pair_q, const int32_t* pair_r, const int64_t* choff, int nlist, int k,
+                          int nprobe, uint64_t* partial) {
+  if (k <= 32)
+    return vec ? launch_scan_t<METRIC, 1, true>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+                                                nlist, k, nprobe, partial)
+               : launch_scan_t<METRIC, 1, false>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+                                                 nlist, k, nprobe, partial);
+  return vec ? launch_scan_t<METRIC, 2, true>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+                                              nlist, k, nprobe, partial)
+             : launch_scan_t<METRIC, 2, false>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+                                               nlist, k, nprobe, partial);
+}
+
 }  // namespace
 
-// Scan of the given probes [nq][nprobe] (list ids, -1 = none) over list-ordered
-// points; results as ids/dists [nq][k] (-1 / +inf padding).
+// Scan of the given probes [nq][nprobe] (list ids, -1 = none): the points of
+// the probed lists are read in place through list_ids; results as ids/dists
+// [nq][k] (-1 / +inf padding).
 mann_status ivf_scan_device(Context* ctx, cudaStream_t s, const float* data, int64_t n, int d,
                             int metric, const int64_t* loff, const int32_t* lids, int nlist,
                             const float* qs, int64_t nq, const int32_t* probes, int nprobe, int k,
                             int32_t* out_ids, float* out_dists) {
+  (void)n;
   if (k < 1 || k > 64) return fail(MANN_EINVAL_ARG, "IVF search supports 1 <= k <= 64");
   if (nprobe < 1 || nprobe > 128) return fail(MANN_EINVAL_ARG, "IVF search supports 1 <= nprobe <= 128");
   if (metric == MANN_METRIC_COSINE) return fail(MANN_EINVAL_ARG, "IVF search: Euclidean / SqEuclidean");
   if (nq <= 0) return MANN_OK;
-  float* xs = nullptr;
   unsigned* cnt = nullptr;
   int64_t *qoff = nullptr, *choff = nullptr;
   int32_t *pair_q = nullptr, *pair_r = nullptr;
   uint64_t *partial = nullptr, *keys = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_IVF_DATA, (size_t)n * d, &xs));
   MANN_TRY(ctx->scratch_t(SLOT_IVF_CNT, (size_t)2 * nlist + 4, &cnt));
   MANN_TRY(ctx->scratch_t(SLOT_IVF_OFF, (size_t)2 * (nlist + 1), &qoff));
   choff = qoff + (nlist + 1);
@@ -223,36 +291,26 @@ mann_status ivf_scan_device(Context* ctx, cudaStream_t s, const float* data, int
   pair_r = pair_q + nq * nprobe;
   MANN_TRY(ctx->scratch_t(SLOT_IVF_PARTIAL, (size_t)nq * nprobe * k, &partial));
   MANN_TRY(ctx->scratch_t(SLOT_IVF_KEYS, (size_t)nq * k, &keys));
-  gather_lists_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(data, d, lids, n, xs);
-  MANN_CHECK_LAUNCH();
   MANN_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(unsigned) * (2 * nlist + 4), s));
   MANN_CUDA_TRY(cudaMemsetAsync(partial, 0xFF, sizeof(uint64_t) * nq * nprobe * k, s));
   probe_count_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(probes, nq * nprobe, nlist, cnt);
   MANN_CHECK_LAUNCH();
-  probe_scan_kernel<<<1, 32, 0, s>>>(cnt, nlist, qoff, choff);
+  probe_scan_kernel<<<1, 1024, 0, s>>>(cnt, nlist, qoff, choff);
   MANN_CHECK_LAUNCH();
   probe_scatter_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(
       probes, nq, nprobe, nlist, qoff, cnt + nlist, pair_q, pair_r);
   MANN_CHECK_LAUNCH();
   // chunks <= pairs/32 + lists; blocks past the real count return at once
   const int64_t max_chunks = ceil_div(nq * nprobe, SCAN_Q) + nlist;
-  const size_t smem = sizeof(uint64_t) * k * SCAN_THREADS +
-                      sizeof(float) * (SCAN_Q * SCAN_D + SCAN_D * (SCAN_P + 1));
-  if (metric == MANN_METRIC_EUCLIDEAN) {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(ivf_scan_kernel<MANN_METRIC_EUCLIDEAN>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ctx->time_begin(s);
-    ivf_scan_kernel<MANN_METRIC_EUCLIDEAN><<<(unsigned)max_chunks, SCAN_THREADS, smem, s>>>(
-        xs, loff, lids, qs, d, qoff, pair_q, pair_r, choff, nlist, k, nprobe, partial);
-  } else {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(ivf_scan_kernel<MANN_METRIC_SQEUCLIDEAN>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    ctx->time_begin(s);
-    ivf_scan_kernel<MANN_METRIC_SQEUCLIDEAN><<<(unsigned)max_chunks, SCAN_THREADS, smem, s>>>(
-        xs, loff, lids, qs, d, qoff, pair_q, pair_r, choff, nlist, k, nprobe, partial);
-  }
+  const bool vec = (d % 4) == 0 && (reinterpret_cast<uintptr_t>(data) & 15) == 0;
+  ctx->time_begin(s);
+  if (metric == MANN_METRIC_EUCLIDEAN)
+    MANN_TRY(launch_scan_m<MANN_METRIC_EUCLIDEAN>(s, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q, pair_r,
+                                                  choff, nlist, k, nprobe, partial));
+  else
+    MANN_TRY(launch_scan_m<MANN_METRIC_SQEUCLIDEAN>(s, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q,
+                                                    pair_r, choff, nlist, k, nprobe, partial));
   ctx->time_end(s);
-  MANN_CHECK_LAUNCH();
   MANN_TRY(launch_merge_lists(partial, nq, nprobe, k, keys, s));
   MANN_TRY(launch_finish(keys, nq, k, k, -1, nullptr, out_ids, out_dists, s));
   return MANN_OK;

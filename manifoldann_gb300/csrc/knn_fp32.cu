@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "kernels.cuh"
+#include "warp_list.cuh"
 
 namespace mann {
 
@@ -22,6 +23,8 @@ constexpr int K1_THREADS = 256;
 constexpr int K1_BN = 128;  // points per tile
 constexpr int K1_DK = 16;   // dimensions per shared-memory stage
 constexpr unsigned FULL = 0xFFFFFFFFu;
+using wl::list_get;
+using wl::list_insert;
 
 __global__ void row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
                                   float* __restrict__ out) {
@@ -31,38 +34,6 @@ __global__ void row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
   float s = 0.0f;
   for (int j = 0; j < d; ++j) s = __fmaf_rn(r[j], r[j], s);
   out[i] = s;
-}
-
-// ---- warp-distributed sorted list: entry e lives in slot e/32 of lane e%32
-template <int KW>
-__device__ __forceinline__ void list_insert(uint64_t (&L)[KW], uint64_t c, int lane) {
-  int pos = 0;
-#pragma unroll
-  for (int s = 0; s < KW; ++s) pos += __popc(__ballot_sync(FULL, L[s] < c));
-  uint64_t up[KW], last[KW];
-#pragma unroll
-  for (int s = 0; s < KW; ++s) {
-    up[s] = __shfl_up_sync(FULL, L[s], 1);
-    last[s] = __shfl_sync(FULL, L[s], 31);
-  }
-#pragma unroll
-  for (int s = 0; s < KW; ++s) {
-    const int e = s * 32 + lane;
-    uint64_t shifted = up[s];
-    if (lane == 0) shifted = (s == 0) ? KEY_NONE : last[s > 0 ? s - 1 : 0];
-    if (e > pos) L[s] = shifted;
-    else if (e == pos) L[s] = c;
-  }
-}
-
-template <int KW>
-__device__ __forceinline__ uint64_t list_get(const uint64_t (&L)[KW], int e) {
-  const int slot = e >> 5, ln = e & 31;
-  uint64_t v = L[0];
-#pragma unroll
-  for (int s = 1; s < KW; ++s)
-    if (slot == s) v = L[s];
-  return __shfl_sync(FULL, v, ln);
 }
 
 // Thread-tile row/column maps.  TQ rows per thread: 8 -> {ty*4+i, 64+ty*4+i},

@@ -641,6 +641,71 @@ __global__ void __launch_bounds__(ROUTE_THREADS)
   }
 }
 
+// Warp per query for small nprobe: every lane keeps the NP best keys of its
+// columns (key = score order << 32 | list id) and an online softmax sum; the
+// warp then pops the nprobe smallest heads.
+template <int NP>
+__global__ void route_topk_warp_kernel(const float* __restrict__ logits, int noutp, const float* __restrict__ D,
+                                       const float* __restrict__ theta, int nout, int64_t nq, int nprobe,
+                                       int32_t* __restrict__ probes, float* __restrict__ coverage) {
+  const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (q >= nq) return;
+  const float beta = D ? expf(*theta) : 0.0f;
+  uint64_t lst[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) lst[i] = KEY_NONE;
+  float mx = -INFINITY, sm = 0.0f;
+  const float* lrow = logits + q * noutp;
+  const float* drow = D ? D + q * nout : nullptr;
+  for (int c = lane; c < nout; c += 32) {
+    float sc = lrow[c];
+    if (D) sc -= beta * drow[c];
+    if (sc > mx) {
+      sm = (mx == -INFINITY ? 0.0f : sm * expf(mx - sc)) + 1.0f;
+      mx = sc;
+    } else if (sc > -INFINITY) {
+      sm += expf(sc - mx);
+    }
+    const uint64_t key = ((uint64_t)score_key(sc) << 32) | (uint32_t)c;
+    if (key < lst[NP - 1]) {
+      lst[NP - 1] = key;
+#pragma unroll
+      for (int i = NP - 1; i > 0; --i)
+        if (lst[i] < lst[i - 1]) {
+          const uint64_t x = lst[i];
+          lst[i] = lst[i - 1];
+          lst[i - 1] = x;
+        }
+    }
+  }
+  float gmx = mx;
+  for (int o = 16; o; o >>= 1) gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
+  float gs = (mx == -INFINITY) ? 0.0f : sm * expf(mx - gmx);
+  for (int o = 16; o; o >>= 1) gs += __shfl_xor_sync(0xffffffffu, gs, o);
+  float cov = 0.0f;
+  for (int r = 0; r < nprobe; ++r) {
+    uint64_t m = lst[0];
+    for (int o = 16; o; o >>= 1) {
+      const uint64_t x = __shfl_xor_sync(0xffffffffu, m, o);
+      m = x < m ? x : m;
+    }
+    if (lst[0] == m) {  // keys are unique: exactly one lane pops
+#pragma unroll
+      for (int i = 0; i < NP - 1; ++i) lst[i] = lst[i + 1];
+      lst[NP - 1] = KEY_NONE;
+    }
+    if (lane == 0) {
+      const int id = (int)(uint32_t)(m & 0xFFFFFFFFu);
+      probes[q * nprobe + r] = id;
+      float sc = lrow[id];
+      if (D) sc -= beta * drow[id];
+      cov += expf(sc - gmx);
+    }
+  }
+  if (coverage && lane == 0) coverage[q] = cov / gs;
+}
+
 // ------------------------------------------------------------ host model
 struct Splitmix {
   uint64_t s;
@@ -934,12 +999,20 @@ mann_status probe_route_device(Context* ctx, ProbeModel* m, cudaStream_t s, cons
       MANN_TRY(ctx->scratch_t(SLOT_PROBE_D, (size_t)nb * P.nout, &D));
       MANN_TRY(prior_dist(ctx, m, s, qs + r0 * P.din, nb, D));
     }
-    const size_t smem = sizeof(uint32_t) * P.nout;
-    if (smem > 48 * 1024)
-      MANN_CUDA_TRY(cudaFuncSetAttribute(route_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    route_topk_kernel<<<(unsigned)nb, ROUTE_THREADS, smem, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb,
-                                                                nprobe, probes + r0 * nprobe,
-                                                                coverage ? coverage + r0 : nullptr);
+    int32_t* pr = probes + r0 * nprobe;
+    float* cv = coverage ? coverage + r0 : nullptr;
+    const unsigned wgrid = (unsigned)ceil_div(nb, 8);
+    if (nprobe <= 8) {
+      route_topk_warp_kernel<8><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe, pr, cv);
+    } else if (nprobe <= 16) {
+      route_topk_warp_kernel<16><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe, pr, cv);
+    } else {
+      const size_t smem = sizeof(uint32_t) * P.nout;
+      if (smem > 48 * 1024)
+        MANN_CUDA_TRY(cudaFuncSetAttribute(route_topk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      route_topk_kernel<<<(unsigned)nb, ROUTE_THREADS, smem, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb,
+                                                                  nprobe, pr, cv);
+    }
     MANN_CHECK_LAUNCH();
   }
   return MANN_OK;

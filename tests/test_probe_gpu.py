@@ -83,18 +83,18 @@ def test_route_topk_order_and_ties(gpu_lib):
     X = rng.standard_normal((777, 64)).astype(np.float32)
     m = _model(dims, False, params=params)
     S = m.scores(X)
-    nprobe = 37
     qd = torch.from_numpy(X).cuda()
-    pr = torch.empty((777, nprobe), dtype=torch.int32, device="cuda")
-    cov = torch.empty(777, dtype=torch.float32, device="cuda")
-    m.route_device(qd, nprobe, pr, cov)
-    torch.cuda.synchronize()
-    pr = pr.cpu().numpy()
-    want = np.stack([np.lexsort((np.arange(1000), -S[i]))[:nprobe] for i in range(777)])
-    assert np.array_equal(pr, want)
+    order = np.stack([np.lexsort((np.arange(1000), -S[i])) for i in range(777)])
     e = np.exp(S - S.max(1, keepdims=True))
-    cov_o = np.take_along_axis(e, want, 1).sum(1) / e.sum(1)
-    assert np.allclose(cov.cpu().numpy(), cov_o, rtol=1e-4, atol=1e-6)
+    for nprobe in (1, 3, 8, 13, 16, 37, 128):  # warp kernels up to 16, radix select above
+        pr = torch.empty((777, nprobe), dtype=torch.int32, device="cuda")
+        cov = torch.empty(777, dtype=torch.float32, device="cuda")
+        m.route_device(qd, nprobe, pr, cov)
+        torch.cuda.synchronize()
+        want = order[:, :nprobe]
+        assert np.array_equal(pr.cpu().numpy(), want), nprobe
+        cov_o = np.take_along_axis(e, want, 1).sum(1) / e.sum(1)
+        assert np.allclose(cov.cpu().numpy(), cov_o, rtol=1e-4, atol=1e-6), nprobe
     # all-equal scores: ties go to the lower list id
     z = np.zeros_like(params)
     mz = _model(dims, False, params=z)
