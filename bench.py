@@ -57,7 +57,9 @@ def parse():
     ap.add_argument("--ivf-epochs", type=int, default=30)
     ap.add_argument("--no-ivf", action="store_true", help="skip the learned-probe IVF leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven graphs leg")
-    ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "ivf-profile"], default="full",
+    ap.add_argument("--no-angular", action="store_true", help="skip the angular (cosine) leg")
+    ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "ivf-profile", "angular"],
+                    default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
                          "launches per step), for ncu captures")
     return ap.parse_args()
@@ -429,6 +431,57 @@ def run_ivf_profile_case(args):
     return 0
 
 
+ANG_WORKLOAD = ("angular-clusters-256d: N=290,000 points and Q=10,000 queries, Gaussian (sigma=0.3) around "
+                "100 random unit centres then L2-normalised, CosineDist, k=20")
+
+
+def run_angular_leg(args, stream_ptr=0):
+    """Angular set: the cosine BF16 form (unit-normalised tensor-core pass,
+    FP32-form cosine rerank) beside the FP32 form on the same queries."""
+    import torch
+
+    from manifoldann_gb300 import _lib, synthetic
+
+    lib = _lib.load()
+    n, nq, d, k = 290000, 10000, 256, 20
+    base = torch.from_numpy(synthetic.angular_clusters(n, d, seed=1)).cuda()
+    q = torch.from_numpy(synthetic.angular_clusters(nq, d, seed=2)).cuda()
+    ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+    dd = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {"workload": ANG_WORKLOAD}
+    res = {}
+    for name, prec, reps in (("bf16", _lib.PREC_BF16, max(3, min(args.steps, 10))), ("fp32", _lib.PREC_FP32, 2)):
+        p = _lib.params(_lib.METRIC_COSINE, k, prec)
+        r = _lib.KnnReport()
+
+        def call():
+            _lib.check(lib.mann_knn_device(p, base.data_ptr(), n, q.data_ptr(), nq, d, ids.data_ptr(),
+                                           dd.data_ptr(), r, stream_ptr))
+
+        for _ in range(2):
+            call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[name] = (ids.cpu().numpy().copy(), dd.cpu().numpy().copy())
+        out[name] = {"ms": ms, "qps": nq / (ms / 1e3), "rows_fallback": r.rows_fallback,
+                     "candidates_per_query": r.candidates / nq if prec == _lib.PREC_BF16 else None}
+    out["bf16_over_fp32"] = out["bf16"]["qps"] / out["fp32"]["qps"]
+    out["bf16_equals_fp32_form"] = bool(np.array_equal(res["bf16"][0], res["fp32"][0]) and
+                                        np.array_equal(res["bf16"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
+    peak_tf, _, _ = measured_peaks()
+    flops = 2.0 * d * n * nq
+    out["roofline_bf16"] = {"bound": "tensor", "achieved": flops / (out["bf16"]["ms"] / 1e3) / 1e12,
+                            "peak": peak_tf, "unit": "TFLOP/s", "note": "whole call (normalise, passes, rerank)"}
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -555,6 +608,7 @@ def run_ours(args):
     cpu = cpu_baseline(base, q, args.cpu_seconds) if args.cpu_seconds > 0 else None
     ivf = None if args.no_ivf else run_ivf_leg(args, sp)
     batched = None if args.no_batched else run_batched_leg(args, sp)
+    angular = None if args.no_angular else run_angular_leg(args, sp)
     line = {"metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
@@ -566,7 +620,8 @@ def run_ours(args):
             "rows_fallback_per_step": fallback / args.steps,
             "candidates_per_query": cands / (args.steps * qps_step),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": launches, "ivf_learned_probe": ivf, "batched_graphs": batched}
+            "gpu_launches": launches, "ivf_learned_probe": ivf, "batched_graphs": batched,
+            "angular_cosine": angular}
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -581,6 +636,12 @@ def main():
         return run_profile_case(args)
     if args.case == "ivf-profile":
         return run_ivf_profile_case(args)
+    if args.case == "angular":
+        import torch
+
+        print(json.dumps({"case": "angular", "angular_cosine": run_angular_leg(
+            args, C.c_void_p(torch.cuda.current_stream().cuda_stream))}), flush=True)
+        return 0
     if args.case == "batched":
         import torch
 

@@ -68,9 +68,16 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
   if (kreq > KMAX_FUSED)
     return fail(MANN_EINVAL_ARG, "k = " + std::to_string(kreq) + " exceeds the fused top-k limit " +
                                      std::to_string(KMAX_FUSED));
+  bool use_bf16 = false;
+  if (p->precision == MANN_PREC_BF16) {
+    if (kreq > 24) return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= 24 (k+1 for graphs)");
+    use_bf16 = true;
+  } else if (p->precision == MANN_PREC_AUTO) {
+    use_bf16 = kreq <= 24 && d >= 128 && n >= 4096;
+  }
   const float* qn = nullptr;
   const float* bn = nullptr;
-  if (p->metric == MANN_METRIC_COSINE) {
+  if (p->metric == MANN_METRIC_COSINE && !use_bf16) {
     float *db = nullptr, *dq = nullptr;
     MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &db));
     MANN_TRY(launch_row_sqnorm(base, n, d, db, s));
@@ -82,15 +89,6 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
       MANN_TRY(launch_row_sqnorm(qs, nq, d, dq, s));
       qn = dq;
     }
-  }
-  const bool l2 = p->metric != MANN_METRIC_COSINE;
-  bool use_bf16 = false;
-  if (p->precision == MANN_PREC_BF16) {
-    if (!l2) return fail(MANN_EINVAL_ARG, "the BF16 form supports SqEuclidean and Euclidean");
-    if (kreq > 24) return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= 24 (k+1 for graphs)");
-    use_bf16 = true;
-  } else if (p->precision == MANN_PREC_AUTO) {
-    use_bf16 = l2 && kreq <= 24 && d >= 128 && n >= 4096;
   }
   uint64_t* keys = nullptr;
   if (use_bf16) {

@@ -66,12 +66,14 @@ struct RowInfo {
   float nrm;    // ||x~||^2 (FP64 sum rounded to nearest)
   float xn_up;  // ||x~|| rounded up
   float r_up;   // bound on ||(x - mu) - x~|| (includes the FP32 rounding of x - mu)
-  float pad;
+  float lo_up;  // split form: ||x_lo|| rounded up (0 otherwise)
 };
 
 struct BaseMax {
   unsigned xn_bits;  // max over points of xn_up (positive float bits, integer max)
   unsigned r_bits;   // max over points of r_up
+  unsigned lo_bits;  // max over points of lo_up
+  unsigned pad;
 };
 
 // ---------------------------------------------------------------- prep kernels
@@ -79,6 +81,21 @@ struct BaseMax {
 // Column means over an evenly spaced sample of rows.  Any centre keeps the
 // distances unchanged; a good one shrinks the BF16 values and their rounding.
 // Block (32 columns x 32 row groups): FP32 partial sums per thread, FP64 across groups.
+// Unit-normalised copy of every row (cosine): |x|^2 as the FP32 form's
+// sequential sum (kept for the rerank), x^ = x / sqrt(|x|^2); a zero row stays zero.
+__global__ void normalize_rows_kernel(const float* __restrict__ x, int64_t n, int d, float* __restrict__ xh,
+                                      float* __restrict__ sqn) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = x + i * (int64_t)d;
+  float s = 0.0f;
+  for (int c = 0; c < d; ++c) s = __fmaf_rn(r[c], r[c], s);
+  sqn[i] = s;
+  const float nr = __fsqrt_rn(s);
+  float* o = xh + i * (int64_t)d;
+  for (int c = 0; c < d; ++c) o[c] = nr > 0.0f ? __fdiv_rn(r[c], nr) : 0.0f;
+}
+
 __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
                                      int64_t rows, float* __restrict__ mu) {
   __shared__ double part[32][33];
@@ -140,13 +157,14 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
 // pick the candidate with the smallest residual (moving off the plain mean
 // only for a clear win), replace mu by its centre and publish its scale
 __global__ void choose_scale_kernel(const double* __restrict__ score, float* __restrict__ mu, int d,
-                                    float* __restrict__ scale_out) {
+                                    float* __restrict__ scale_out, int* __restrict__ inexact) {
   __shared__ int best;
   if (threadIdx.x == 0) {
     int b = 0;
     for (int i = 1; i < NUM_SCALES; ++i)
       if (score[i] < 0.25 * score[b]) b = i;
     best = b;
+    *inexact = score[b] > 0.0 ? 1 : 0;
     float sc, mc;
     scale_candidate(b, 0.0f, &sc, &mc);
     *scale_out = sc;
@@ -160,37 +178,54 @@ __global__ void choose_scale_kernel(const double* __restrict__ score, float* __r
 }
 
 // One warp per row: BF16 copy of scale*(x - mu) padded to dp, and the row's bound terms.
+// Split form (split = 1): x~ = hi + lo with hi = bf16(cv), lo = bf16(cv - hi),
+// written as three dp-wide segments -- [hi | hi | lo] for query rows (role 0),
+// [hi | lo | hi] for point rows (role 1) -- so one MMA over 3dp columns gives
+// hi.hi + hi.lo + lo.hi = q~.p~ - lo_q.lo_p.
 __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
                                     const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
-                                    float* __restrict__ norms, BaseMax* __restrict__ bmax) {
+                                    float* __restrict__ norms, BaseMax* __restrict__ bmax, int split,
+                                    int role) {
   const int lane = threadIdx.x & 31;
   const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (row >= n) return;
   const float* xr = x + row * d;
-  __nv_bfloat16* br = xb + row * dp;
+  __nv_bfloat16* br = xb + row * (int64_t)(split ? 3 * dp : dp);
   // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
   // certificate adds to its bound (norm_rel_err)
-  float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f;
+  float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f, f_l = 0.0f;
   for (int c = lane; c < dp; c += 32) {
     float cv = 0.0f;
     if (c < d) cv = __fmul_rn(scale, __fsub_rn(xr[c], mu[c]));
     const __nv_bfloat16 b = __float2bfloat16_rn(cv);
-    br[c] = b;
-    const float bv = __bfloat162float(b);
+    float bv = __bfloat162float(b);
+    if (split) {
+      // cv - hi is exact in FP32; hi + lo spans at most 17 bits, also exact
+      const __nv_bfloat16 lb = __float2bfloat16_rn(cv - bv);
+      const float lv = __bfloat162float(lb);
+      br[c] = b;
+      br[dp + c] = role ? lb : b;
+      br[2 * dp + c] = role ? b : lb;
+      bv = bv + lv;
+      f_l = __fmaf_rn(lv, lv, f_l);
+    } else {
+      br[c] = b;
+    }
     const float rv = cv - bv;  // exact: the rounding residual of a float fits in a float
     f_b = __fmaf_rn(bv, bv, f_b);
     f_r = __fmaf_rn(rv, rv, f_r);
     f_c = __fmaf_rn(cv, cv, f_c);
   }
-  double s_b = f_b, s_r = f_r, s_c = f_c;
+  double s_b = f_b, s_r = f_r, s_c = f_c, s_l = f_l;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     s_b += __shfl_xor_sync(FULL, s_b, o);
     s_r += __shfl_xor_sync(FULL, s_r, o);
     s_c += __shfl_xor_sync(FULL, s_c, o);
+    s_l += __shfl_xor_sync(FULL, s_l, o);
   }
   if (lane == 0) {
     const double rel = (double)((dp + 31) / 32 + 2) * 5.9604644775390625e-08;
@@ -200,12 +235,13 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     // ||s(x-mu)_exact - x~|| <= ||cv - x~|| + 2u ||cv|| (1+u), cv = fl(s fl(x-mu))
     ri.r_up = round_up_f((sqrt(s_r * (1.0 + rel)) +
                           2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c * (1.0 + rel))) * (1.0 + 1e-9));
-    ri.pad = 0.0f;
+    ri.lo_up = split ? round_up_f(sqrt(s_l * (1.0 + rel)) * (1.0 + 1e-12)) : 0.0f;
     info[row] = ri;
     if (norms) norms[row] = ri.nrm;
     if (bmax) {
       atomicMax(&bmax->xn_bits, __float_as_uint(ri.xn_up));
       atomicMax(&bmax->r_bits, __float_as_uint(ri.r_up));
+      atomicMax(&bmax->lo_bits, __float_as_uint(ri.lo_up));
     }
   }
 }
@@ -608,6 +644,12 @@ struct RerankArgs {
   int* fb_rows;           // rows that need the FP32 scan
   int* fb_count;
   unsigned long long* cand_total;
+  // cosine: the tensor-core pass ran on unit-normalised rows; the candidates
+  // are reranked with the FP32 form's cosine on the original rows
+  const float* cos_qn;  // [nq] squared norms of the original queries (FP32 form order)
+  const float* cos_bn;  // [n]  squared norms of the original points
+  double eps_c;         // |FP32 cosine - ||q^ - p^||^2 / 2| bound
+  int kdim;             // columns of the tensor-core dot (dp, or 3 dp in the split form)
 };
 
 // sequential difference-form sum over dimensions 0..d-1 (the FP32 form's order)
@@ -638,6 +680,17 @@ __device__ __forceinline__ float fp32_dist_row(const float* __restrict__ x,
   return metric == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(s) : s;
 }
 
+// the FP32 form's cosine: sequential dot, then 1 - dot / (sqrt(|q|^2) sqrt(|p|^2)), clamped at 0
+__device__ __forceinline__ float fp32_cos_row(const float* __restrict__ x, const float* __restrict__ y, int d,
+                                              float xn, float yn) {
+  float s = 0.0f;
+  for (int c = 0; c < d; ++c) s = __fmaf_rn(__ldg(x + c), __ldg(y + c), s);
+  const float den = __fmul_rn(__fsqrt_rn(xn), __fsqrt_rn(yn));
+  float v = __fsub_rn(1.0f, __fdiv_rn(s, den));
+  if (v < 0.0f) v = 0.0f;
+  return v;
+}
+
 __global__ void k2_rerank(RerankArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -651,24 +704,33 @@ __global__ void k2_rerank(RerankArgs a) {
   const double br = (double)__uint_as_float(a.bmax->r_bits);
   const double u = 5.9604644775390625e-08;
   // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
-  const double gam = (double)((a.d + 15) / 16 + 2) * 2.384185791015625e-07;
+  const double gam = (double)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07;
   // + the relative error of the FP32-accumulated row norms (two of them)
   const int dpad = (a.d + 7) & ~7;
   const double nerr = (double)((dpad + 31) / 32 + 2) * u;
   const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
-  const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn);
+  // split form: the MMA adds |hi| |lo| cross terms to the magnitudes it sums
+  // (<= (1 + 2^-7) |x~| per side) and leaves out 2 lo_q.lo_p of the estimate
+  const double blo = (double)__uint_as_float(a.bmax->lo_bits);
+  const double inflate = blo > 0.0 ? 1.0161 : 1.0;
+  const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn) * inflate +
+                   2.0 * (double)qi.lo_up * blo / c1;
   const double Rs = (double)qi.r_up + br;
   const double qn = (double)qi.nrm;  // list keys hold est' = est - ||q~||^2
   const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key) + qn, 0.0);
-  const double sU = sqrt(ek + c1 * A) + Rs;
+  const double sc = (double)*a.scale;
+  const bool cosine = a.metric == MANN_METRIC_COSINE;
+  double sU = sqrt(ek + c1 * A) + Rs;
+  // cosine: every point of the FP32-form top-k has ||q^ - p^||^2 <= U / s^2 + 4 eps_c
+  if (cosine) sU = sqrt(sU * sU + 4.0 * a.eps_c * sc * sc);
   const double U = sU * sU;
   const double slack = 3.0 * (double)(a.d + 2) * u * U + 1e-6 * U + 1e-30;
   const double T = ((sU + Rs) * (sU + Rs) + c1 * A + slack) * (1.0 + 1e-9);
   // lower bound on the exact distance of any point outside the list's est <= T set
   const double e_floor = fmax(T - c1 * A, 0.0);
   const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
-  const double sc = (double)*a.scale;
-  double d_floor = s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
+  double d_floor = cosine ? 0.5 * s_floor * s_floor / (sc * sc) - a.eps_c
+                          : s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
   // Every point outside the merged list has est' >= its depth-th entry, or >=
   // the seed when the list is not full; with neither, the list holds every point.
   const float sd = a.seed ? a.seed[q] : __int_as_float(0x7F800000);
@@ -676,7 +738,9 @@ __global__ void k2_rerank(RerankArgs a) {
   const double beyond = last_key != KEY_NONE ? (double)key_dist(last_key) : (double)sd;
   // without the row's k-th estimate (fewer than k points admitted below the
   // seed) the threshold is unknown: the row is not certified
-  const bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
+  bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
+  // a zero-norm (or non-finite) query has no unit direction: the FP32 form answers it
+  if (cosine && !(a.cos_qn[q] > 0.0f && a.cos_qn[q] < 3.0e38f)) certified = false;
   {
     // depth this row's certificate needs: one past its last est <= T entry
     const uint64_t kl = lst[lane];
@@ -703,12 +767,29 @@ __global__ void k2_rerank(RerankArgs a) {
       const uint64_t k = lst[e];
       if (k != KEY_NONE && (double)key_dist(k) + qn <= T) {
         const int id = key_id(k);
-        const float dist = fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
+        const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
+                                  : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
         key[s] = make_key(dist, (uint32_t)id);
       }
     }
   }
   ncand = __popc(__ballot_sync(FULL, key[0] != KEY_NONE)) + __popc(__ballot_sync(FULL, key[1] != KEY_NONE));
+  if (cosine && !all_in) {
+    // a zero-norm point has a NaN cosine and no bound from the unit-norm
+    // pass: a row that needs such points (fewer than k finite candidates)
+    // goes to the FP32 form
+    const bool f0 = key[0] != KEY_NONE && key_dist(key[0]) == key_dist(key[0]);
+    const bool f1 = key[1] != KEY_NONE && key_dist(key[1]) == key_dist(key[1]);
+    const int nfin = __popc(__ballot_sync(FULL, f0)) + __popc(__ballot_sync(FULL, f1));
+    if (nfin < a.kreq) {
+      if (lane == 0) {
+        const int slot = atomicAdd(a.fb_count, 1);
+        a.fb_rows[slot] = (int)q;
+        a.cand_count[q] = -1;
+      }
+      return;
+    }
+  }
   // rank sort by (distance, id)
   int rank[2] = {0, 0};
   for (int src = 0; src < 32; ++src) {
@@ -726,7 +807,7 @@ __global__ void k2_rerank(RerankArgs a) {
   for (int e = ncand + lane; e < a.L; e += 32) out[e] = KEY_NONE;
   if (lane == 0) {
     a.cand_count[q] = ncand;
-    float fl = (float)d_floor;
+    float fl = cosine ? __double2float_rd(d_floor) : (float)d_floor;
     if (a.metric == MANN_METRIC_EUCLIDEAN) fl = (float)sqrt(fmax(d_floor, 0.0)) * (1.0f - 1e-6f);
     a.floor_val[q] = fl;
     atomicAdd(a.cand_total, (unsigned long long)ncand);
@@ -1059,7 +1140,6 @@ struct Bf16Operand {
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
                           bool fp64, uint64_t** out_keys, mann_knn_report* rep) {
-  if (metric == MANN_METRIC_COSINE) return fail(MANN_EINVAL_ARG, "BF16 form: L2 metrics only");
   if (nq <= 0) return MANN_OK;
   const int L = LIST;
   // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
@@ -1079,6 +1159,31 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
                                      " (k+1 for graphs)");
   const int dp = (d + 7) & ~7;
   const bool self = (qs == base);
+  const bool cosine = metric == MANN_METRIC_COSINE;
+
+  // ---- cosine: the tensor-core passes run on unit-normalised rows
+  // (1 - cos = ||q^ - p^||^2 / 2); the rerank uses the original rows
+  const float* mbase = base;
+  const float* mqs = qs;
+  float *cos_bn = nullptr, *cos_qn = nullptr;
+  if (cosine) {
+    float *xb = nullptr, *xq = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_COS_B, (size_t)n * d, &xb));
+    MANN_TRY(ctx->scratch_t(SLOT_COS_NB, (size_t)n, &cos_bn));
+    normalize_rows_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(base, n, d, xb, cos_bn);
+    MANN_CHECK_LAUNCH();
+    mbase = xb;
+    if (self) {
+      mqs = xb;
+      cos_qn = cos_bn;
+    } else {
+      MANN_TRY(ctx->scratch_t(SLOT_COS_Q, (size_t)nq * d, &xq));
+      MANN_TRY(ctx->scratch_t(SLOT_COS_NQ, (size_t)nq, &cos_qn));
+      normalize_rows_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(qs, nq, d, xq, cos_qn);
+      MANN_CHECK_LAUNCH();
+      mqs = xq;
+    }
+  }
 
   // ---- prep
   double* cpart = nullptr;
@@ -1089,7 +1194,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   {
     const int64_t rows = std::min<int64_t>(n, 4096);
     const int64_t stride = n / rows;
-    centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(base, n, d, stride, rows, mu);
+    centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(mbase, n, d, stride, rows, mu);
     MANN_CHECK_LAUNCH();
   }
   // pick the centre / scale with the smallest BF16 residual on a row sample
@@ -1098,26 +1203,39 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   const int64_t sample_rows = std::min<int64_t>(n, 1024);
   const int64_t stride = std::max<int64_t>(1, n / sample_rows);
   dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
-  scale_probe_kernel<<<pg, 256, 0, s>>>(base, n, d, mu, stride, score);
+  scale_probe_kernel<<<pg, 256, 0, s>>>(mbase, n, d, mu, stride, score);
   MANN_CHECK_LAUNCH();
   float* scale = reinterpret_cast<float*>(bmax + 1);
-  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale);
+  int* inexact = reinterpret_cast<int*>(scale + 1);
+  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale, inexact);
   MANN_CHECK_LAUNCH();
   MANN_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(BaseMax), s));
+  // Data that BF16 cannot hold exactly (after the best centre and scale) runs
+  // in the split form: x~ = hi + lo, three BF16 products per term, bounds ~2^8
+  // tighter, so the certificate holds for close neighbours too.
+  int h_inexact = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  const int split = h_inexact ? 1 : 0;
+  const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
+  if (margin <= 0) {
+    auto it = ctx->tune.find(tkey ^ ((uint64_t)split << 62));
+    depth = it != ctx->tune.end() ? (int)it->second : L;
+  }
   Bf16Operand B, Q;
-  MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp, &B.xb));
+  MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dpe, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
   MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
-  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, dp, mu, scale, B.xb, B.info,
-                                                              B.norms, bmax);
+  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, mu, scale, B.xb, B.info,
+                                                              B.norms, bmax, split, 1);
   MANN_CHECK_LAUNCH();
-  if (self) {
+  if (self && !split) {
     Q = B;
   } else {
-    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dp, &Q.xb));
+    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dpe, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
-    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, dp, mu, scale, Q.xb, Q.info,
-                                                                  nullptr, nullptr);
+    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, mu, scale, Q.xb, Q.info,
+                                                                  nullptr, nullptr, split, 0);
     MANN_CHECK_LAUNCH();
   }
 
@@ -1130,7 +1248,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
 
   CUtensorMap mapA;
-  MANN_TRY(make_map(&mapA, Q.xb, nq, dp, BM));
+  MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM));
 
   // ---- seed pass: the 5th smallest est' of each query over an evenly spaced
   // sample of SEED_SAMPLE points becomes its admission seed in the main pass
@@ -1140,9 +1258,9 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (n >= 16 * SEED_SAMPLE) {
     const int64_t bstride = n / SEED_SAMPLE;
     CUtensorMap mapS;
-    MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dp, BN, bstride));
+    MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dpe, BN, bstride));
     uint64_t* slists = nullptr;
-    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dp, 5,
+    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dpe, 5,
                            nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
     seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, 4, seed);
@@ -1151,9 +1269,9 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
   // ---- main pass over every point
   CUtensorMap mapB;
-  MANN_TRY(make_map(&mapB, B.xb, n, dp, BN));
+  MANN_TRY(make_map(&mapB, B.xb, n, dpe, BN));
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, B.norms, 1, n, nq, d, dp, depth, seed, err,
+  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, B.norms, 1, n, nq, d, dpe, depth, seed, err,
                          SLOT_PARTIAL, SLOT_KEYS, true, &lists));
 
   // ---- certify + rerank
@@ -1187,6 +1305,14 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.fb_rows = fb_rows;
   ra.fb_count = fb_count;
   ra.cand_total = counters + 2;
+  ra.kdim = dpe;
+  ra.cos_qn = cos_qn;
+  ra.cos_bn = cos_bn;
+  {
+    const double u = 5.9604644775390625e-08;
+    const double gd = (double)d * u / (1.0 - (double)d * u);
+    ra.eps_c = 1.25 * (4.0 * gd + 16.0 * u);
+  }
   k2_rerank<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(ra);
   MANN_CHECK_LAUNCH();
 
@@ -1217,7 +1343,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
         }
       }
     }
-    ctx->tune[tkey] = (uint64_t)want;
+    ctx->tune[tkey ^ ((uint64_t)split << 62)] = (uint64_t)want;
   }
   if (h_err != 0)
     return fail(MANN_ETIMEOUT, "tensor-core kernel: a bounded wait ran out (role " + std::to_string(h_err) + ")");
@@ -1225,8 +1351,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     const int kk = (int)std::min<int64_t>(std::min<int64_t>(n, KMAX_FUSED), std::min(L, kreq + 32));
     uint64_t* fkeys = nullptr;
     const float* no_norm = nullptr;
-    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_fb, d, metric, kk, fb_rows, no_norm, no_norm,
-                           &fkeys, SLOT_FALLBACK_KEYS, SLOT_MISC2));
+    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_fb, d, metric, kk, fb_rows, cosine ? cos_qn : no_norm,
+                           cosine ? cos_bn : no_norm, &fkeys, SLOT_FALLBACK_KEYS, SLOT_MISC2));
     k2_scatter_fallback<<<h_fb, 64, 0, s>>>(fkeys, fb_rows, fb_count, kk, L, cand, cand_count, floor_val);
     MANN_CHECK_LAUNCH();
   }

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from conftest import load_golden
-from test_knn_gpu import M_EUC, M_SQ, gpu_graph, gpu_knn, same_bits
+from test_knn_gpu import M_COS, M_EUC, M_SQ, gpu_graph, gpu_knn, same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -153,3 +153,53 @@ def test_bf16_seeded_pass(gpu_lib, orc):
     for _ in range(3):
         ids, d, rep = gpu_knn(base, q, 10, M_SQ, precision="bf16", report=True)
         assert np.array_equal(ids, ids_o) and same_bits(d, d_o)
+
+
+# ---- cosine: the tensor-core pass on unit-normalised rows, FP32-form cosine rerank
+
+def _angular(n, d, seed):
+    from manifoldann_gb300 import synthetic
+
+    return synthetic.angular_clusters(n, d, seed=seed)
+
+
+@pytest.mark.parametrize("n,nq,d,k", [(20000, 600, 256, 20), (6000, 300, 128, 10), (9000, 200, 200, 24)])
+def test_bf16_cosine_equals_oracle(gpu_lib, orc, n, nq, d, k):
+    base = _angular(n, d, 1)
+    q = _angular(nq, d, 2)
+    ids, dd, rep = gpu_knn(base, q, k, M_COS, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, k, M_COS)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dd, d_o)
+    assert rep["precision_used"] == 1
+    assert rep["rows_fallback"] <= nq // 50, rep
+
+
+def test_bf16_cosine_graph_and_unnormalised_rows(gpu_lib, orc):
+    rng = np.random.default_rng(5)
+    data = _angular(8000, 128, 3) * rng.uniform(0.1, 10.0, size=(8000, 1)).astype(np.float32)
+    g, gd = gpu_graph(data, 15, M_COS, precision="bf16")
+    g_o, gd_o = orc.knn_graph_f32(data, 15, M_COS)
+    assert np.array_equal(g, g_o) and same_bits(gd, gd_o)
+
+
+def test_bf16_cosine_zero_rows_fall_back(gpu_lib, orc):
+    base = _angular(6000, 128, 4)
+    base[[5, 777, 4000]] = 0.0
+    q = _angular(100, 128, 6)
+    q[[3, 50]] = 0.0
+    ids, dd, rep = gpu_knn(base, q, 10, M_COS, precision="bf16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 10, M_COS)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dd, d_o)
+    assert rep["rows_fallback"] >= 2
+
+
+def test_bf16_cosine_full_size_equals_fp32_kernel(gpu_lib):
+    # N=290,000 angular points (d=256), 10,000 queries, k=20: both GPU forms agree bit for bit
+    base = _angular(290000, 256, 1)
+    q = _angular(10000, 256, 2)
+    i32, d32 = gpu_knn(base, q, 20, M_COS, precision="fp32")
+    ib, db, rep = gpu_knn(base, q, 20, M_COS, precision="bf16", report=True)
+    assert np.array_equal(i32, ib) and same_bits(d32, db)
+    assert rep["rows_fallback"] <= 100, rep
