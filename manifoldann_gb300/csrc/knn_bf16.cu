@@ -157,14 +157,16 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
 // pick the candidate with the smallest residual (moving off the plain mean
 // only for a clear win), replace mu by its centre and publish its scale
 __global__ void choose_scale_kernel(const double* __restrict__ score, float* __restrict__ mu, int d,
-                                    float* __restrict__ scale_out, int* __restrict__ inexact) {
+                                    float* __restrict__ scale_out, int* __restrict__ inexact, int64_t nrows) {
   __shared__ int best;
   if (threadIdx.x == 0) {
     int b = 0;
     for (int i = 1; i < NUM_SCALES; ++i)
       if (score[i] < 0.25 * score[b]) b = i;
     best = b;
-    *inexact = score[b] > 0.0 ? 1 : 0;
+    // the mean squared relative residual of the sampled rows: ~2^-18 for data
+    // off any grid, ~1e-14 for grid data that FP32 centring merely blurs
+    *inexact = score[b] > 1e-10 * (double)(nrows > 0 ? nrows : 1) ? 1 : 0;
     float sc, mc;
     scale_candidate(b, 0.0f, &sc, &mc);
     *scale_out = sc;
@@ -1207,7 +1209,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   MANN_CHECK_LAUNCH();
   float* scale = reinterpret_cast<float*>(bmax + 1);
   int* inexact = reinterpret_cast<int*>(scale + 1);
-  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale, inexact);
+  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale, inexact, ceil_div(n, stride));
   MANN_CHECK_LAUNCH();
   MANN_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(BaseMax), s));
   // Data that BF16 cannot hold exactly (after the best centre and scale) runs

@@ -323,6 +323,151 @@ __global__ void __launch_bounds__(K1_THREADS, 1)
                               reinterpret_cast<float*>(k1_smem));
 }
 
+// Exact FP32 scan for a handful of query rows (nq <= 32, e.g. the rows the
+// BF16 form could not certify): one point per thread, blocks striding over
+// 256-point chunks, every distance the FP32 form's sequential sum in
+// dimension order (queries staged 32 dimensions at a time in shared memory,
+// the point's slice in registers); warp w keeps the lists of rows w, w+8,
+// w+16, w+24; one list per (row, block), merged afterwards.
+constexpr int FEW_Q = 32;
+constexpr int FEW_T = 256;
+constexpr int FEW_DC = 32;
+
+template <int METRIC, int KW, bool VEC>
+__global__ void __launch_bounds__(FEW_T, 2)
+    few_rows_kernel(const float* __restrict__ base, int64_t n, const float* __restrict__ qs,
+                    const int32_t* __restrict__ qrows, int nq, int d, const float* __restrict__ qnorm,
+                    const float* __restrict__ bnorm, int k, uint64_t* __restrict__ partial) {
+  __shared__ __align__(16) float qsm[FEW_Q][FEW_DC];
+  __shared__ float dsm[FEW_Q][FEW_T + 1];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint64_t L[4][KW];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int s = 0; s < KW; ++s) L[m][s] = KEY_NONE;
+  for (int64_t p0 = (int64_t)blockIdx.x * FEW_T; p0 < n; p0 += (int64_t)gridDim.x * FEW_T) {
+    const int64_t pi = p0 + t;
+    const bool valid = pi < n;
+    const float* prow = base + (valid ? pi : 0) * d;
+    float acc[FEW_Q];
+#pragma unroll
+    for (int j = 0; j < FEW_Q; ++j) acc[j] = 0.0f;
+    for (int c0 = 0; c0 < d; c0 += FEW_DC) {
+      const int dc = min(FEW_DC, d - c0);
+      __syncthreads();
+      for (int e = t; e < FEW_Q * FEW_DC; e += FEW_T) {
+        const int r = e / FEW_DC, c = e % FEW_DC;
+        float v = 0.0f;
+        if (r < nq && c < dc) v = __ldg(&qs[(int64_t)(qrows ? qrows[r] : r) * d + c0 + c]);
+        qsm[r][c] = v;
+      }
+      float pv[FEW_DC];
+      if (VEC && dc == FEW_DC) {
+#pragma unroll
+        for (int c = 0; c < FEW_DC; c += 4) {
+          const float4 v = valid ? __ldg(reinterpret_cast<const float4*>(prow + c0 + c)) : make_float4(0, 0, 0, 0);
+          pv[c] = v.x;
+          pv[c + 1] = v.y;
+          pv[c + 2] = v.z;
+          pv[c + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < FEW_DC; ++c) pv[c] = (valid && c < dc) ? __ldg(prow + c0 + c) : 0.0f;
+      }
+      __syncthreads();
+      // dimensions past d are zero on both sides and add nothing
+#pragma unroll
+      for (int j = 0; j < FEW_Q; ++j) {
+        if (j < nq) {
+          float a = acc[j];
+#pragma unroll
+          for (int c = 0; c < FEW_DC; c += 4) {
+            const float4 q4 = *reinterpret_cast<const float4*>(&qsm[j][c]);
+            if constexpr (METRIC == MANN_METRIC_COSINE) {
+              a = __fmaf_rn(q4.x, pv[c], a);
+              a = __fmaf_rn(q4.y, pv[c + 1], a);
+              a = __fmaf_rn(q4.z, pv[c + 2], a);
+              a = __fmaf_rn(q4.w, pv[c + 3], a);
+            } else {
+              float u = __fsub_rn(q4.x, pv[c]);
+              a = __fmaf_rn(u, u, a);
+              u = __fsub_rn(q4.y, pv[c + 1]);
+              a = __fmaf_rn(u, u, a);
+              u = __fsub_rn(q4.z, pv[c + 2]);
+              a = __fmaf_rn(u, u, a);
+              u = __fsub_rn(q4.w, pv[c + 3]);
+              a = __fmaf_rn(u, u, a);
+            }
+          }
+          acc[j] = a;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < FEW_Q; ++j) {
+      if (j < nq) {
+        float v = acc[j];
+        if constexpr (METRIC == MANN_METRIC_EUCLIDEAN) {
+          v = __fsqrt_rn(v);
+        } else if constexpr (METRIC == MANN_METRIC_COSINE) {
+          const float qnv = qnorm[qrows ? qrows[j] : j];
+          const float bnv = valid ? bnorm[pi] : 1.0f;
+          const float den = __fmul_rn(__fsqrt_rn(qnv), __fsqrt_rn(bnv));
+          v = __fsub_rn(1.0f, __fdiv_rn(v, den));
+          if (v < 0.0f) v = 0.0f;
+        }
+        dsm[j][t] = v;
+      }
+    }
+    __syncthreads();
+    const int np = (int)min((int64_t)FEW_T, n - p0);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int j = warp + 8 * m;
+      if (j >= nq) continue;  // warp-uniform
+      uint64_t thr = list_get<KW>(L[m], k - 1);
+      for (int c8 = 0; c8 < FEW_T; c8 += 32) {
+        const int col = c8 + lane;
+        const uint64_t key = col < np ? make_key(dsm[j][col], (uint32_t)(p0 + col)) : KEY_NONE;
+        unsigned pend = __ballot_sync(FULL, key < thr);
+        while (pend) {
+          const int src = __ffs(pend) - 1;
+          pend &= pend - 1;
+          const uint64_t cnd = __shfl_sync(FULL, key, src);
+          if (cnd < thr) {
+            list_insert<KW>(L[m], cnd, lane);
+            thr = list_get<KW>(L[m], k - 1);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const int j = warp + 8 * m;
+    if (j >= nq) continue;
+    uint64_t* dst = partial + ((int64_t)j * gridDim.x + blockIdx.x) * k;
+#pragma unroll
+    for (int s = 0; s < KW; ++s) {
+      const int e = s * 32 + lane;
+      if (e < k) dst[e] = L[m][s];
+    }
+  }
+}
+
+template <int METRIC, bool VEC>
+mann_status launch_few_m(int grid, const float* base, int64_t n, const float* qs, const int32_t* rows, int nq,
+                         int d, const float* qn, const float* bn, int kk, uint64_t* partial, cudaStream_t s) {
+  if (kk <= 32)
+    few_rows_kernel<METRIC, 1, VEC><<<grid, FEW_T, 0, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
+  else
+    few_rows_kernel<METRIC, 2, VEC><<<grid, FEW_T, 0, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
 // Merge nsplit sorted lists of k keys per query into one sorted list of k.
 // One warp per query; lane s walks list s (and s+32, ...).
 __global__ void merge_lists_kernel(const uint64_t* __restrict__ partial, int64_t nq, int nsplit,
@@ -494,6 +639,39 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (nq <= 0) return MANN_OK;
   if (metric == MANN_METRIC_COSINE && (qn == nullptr || bn == nullptr))
     return fail(MANN_EINVAL_ARG, "cosine search needs row norms");
+  if (nq <= FEW_Q && kk <= 64) {
+    // a handful of rows: one point per thread across the whole GPU
+    const int grid = (int)std::min<int64_t>(128, ceil_div(n, FEW_T));
+    uint64_t* partial = nullptr;
+    MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * grid * kk, &partial));
+    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
+    ctx->time_begin(s);
+    switch (metric) {
+      case MANN_METRIC_EUCLIDEAN:
+        MANN_TRY((vec4 ? launch_few_m<MANN_METRIC_EUCLIDEAN, true>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)
+                       : launch_few_m<MANN_METRIC_EUCLIDEAN, false>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)));
+        break;
+      case MANN_METRIC_SQEUCLIDEAN:
+        MANN_TRY((vec4 ? launch_few_m<MANN_METRIC_SQEUCLIDEAN, true>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)
+                       : launch_few_m<MANN_METRIC_SQEUCLIDEAN, false>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)));
+        break;
+      default:
+        MANN_TRY((vec4 ? launch_few_m<MANN_METRIC_COSINE, true>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)
+                       : launch_few_m<MANN_METRIC_COSINE, false>(grid, base, n, qs, rows, (int)nq, d, qn, bn, kk, partial, s)));
+        break;
+    }
+    ctx->time_end(s);
+    if (grid == 1) {
+      *out_keys = partial;
+      return MANN_OK;
+    }
+    uint64_t* keys = nullptr;
+    MANN_TRY(ctx->scratch_t(slot_keys, (size_t)nq * kk, &keys));
+    merge_lists_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, grid, kk, keys);
+    MANN_CHECK_LAUNCH();
+    *out_keys = keys;
+    return MANN_OK;
+  }
   const int bq = nq <= 32 ? 32 : (kk <= 64 ? 128 : (kk <= 128 ? 64 : 32));
   const int64_t qblocks = ceil_div(nq, bq);
   const int64_t tiles = ceil_div(n, K1_BN);
