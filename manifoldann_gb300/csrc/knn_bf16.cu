@@ -192,16 +192,31 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   const int lane = threadIdx.x & 31;
   const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (row >= n) return;
-  const float* xr = x + row * d;
-  __nv_bfloat16* br = xb + row * (int64_t)(split ? 3 * dp : dp);
+  __shared__ unsigned blk_max[3];
+  if (threadIdx.x < 3) blk_max[threadIdx.x] = 0u;
+  __syncthreads();
+  const bool valid = row < n;
+  const float* xr = x + (valid ? row : 0) * d;
+  __nv_bfloat16* br = xb + (valid ? row : 0) * (int64_t)(split ? 3 * dp : dp);
   // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
   // certificate adds to its bound (norm_rel_err)
   float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f, f_l = 0.0f;
-  for (int c = lane; c < dp; c += 32) {
+  constexpr int PF = 8;  // loads in flight per lane (the kernel is latency-bound otherwise)
+  for (int c0 = lane; valid && c0 < dp; c0 += 32 * PF) {
+    float xv[PF], mv[PF];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      const int c = c0 + 32 * u;
+      xv[u] = c < d ? __ldg(xr + c) : 0.0f;
+      mv[u] = c < d ? __ldg(mu + c) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+    const int c = c0 + 32 * u;
+    if (c >= dp) break;
     float cv = 0.0f;
-    if (c < d) cv = __fmul_rn(scale, __fsub_rn(xr[c], mu[c]));
+    if (c < d) cv = __fmul_rn(scale, __fsub_rn(xv[u], mv[u]));
     const __nv_bfloat16 b = __float2bfloat16_rn(cv);
     float bv = __bfloat162float(b);
     if (split) {
@@ -220,17 +235,20 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     f_b = __fmaf_rn(bv, bv, f_b);
     f_r = __fmaf_rn(rv, rv, f_r);
     f_c = __fmaf_rn(cv, cv, f_c);
+    }
   }
-  double s_b = f_b, s_r = f_r, s_c = f_c, s_l = f_l;
+  // cross-lane sums in FP32 (a 5-level tree of nonnegative terms adds at most
+  // 5u of relative error; FP64 arithmetic is slow on this part)
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    s_b += __shfl_xor_sync(FULL, s_b, o);
-    s_r += __shfl_xor_sync(FULL, s_r, o);
-    s_c += __shfl_xor_sync(FULL, s_c, o);
-    s_l += __shfl_xor_sync(FULL, s_l, o);
+    f_b += __shfl_xor_sync(FULL, f_b, o);
+    f_r += __shfl_xor_sync(FULL, f_r, o);
+    f_c += __shfl_xor_sync(FULL, f_c, o);
+    f_l += __shfl_xor_sync(FULL, f_l, o);
   }
-  if (lane == 0) {
-    const double rel = (double)((dp + 31) / 32 + 2) * 5.9604644775390625e-08;
+  const double s_b = f_b, s_r = f_r, s_c = f_c, s_l = f_l;
+  if (lane == 0 && valid) {
+    const double rel = (double)((dp + 31) / 32 + 2 + 5) * 5.9604644775390625e-08;
     RowInfo ri;
     ri.nrm = __double2float_rn(s_b);
     ri.xn_up = round_up_f(sqrt(s_b * (1.0 + rel)) * (1.0 + 1e-12));
@@ -240,10 +258,18 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     ri.lo_up = split ? round_up_f(sqrt(s_l * (1.0 + rel)) * (1.0 + 1e-12)) : 0.0f;
     info[row] = ri;
     if (norms) norms[row] = ri.nrm;
-    if (bmax) {
-      atomicMax(&bmax->xn_bits, __float_as_uint(ri.xn_up));
-      atomicMax(&bmax->r_bits, __float_as_uint(ri.r_up));
-      atomicMax(&bmax->lo_bits, __float_as_uint(ri.lo_up));
+    if (bmax) {  // one global atomic per block and field, not per row
+      atomicMax(&blk_max[0], __float_as_uint(ri.xn_up));
+      atomicMax(&blk_max[1], __float_as_uint(ri.r_up));
+      atomicMax(&blk_max[2], __float_as_uint(ri.lo_up));
+    }
+  }
+  if (bmax) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      atomicMax(&bmax->xn_bits, blk_max[0]);
+      atomicMax(&bmax->r_bits, blk_max[1]);
+      atomicMax(&bmax->lo_bits, blk_max[2]);
     }
   }
 }
@@ -612,11 +638,23 @@ __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int s
   const int c1 = cta_of(qb * tiles + tiles - 1, work, grid);
   const int nseg = (c1 - c0 + 1) * nsets;
   uint64_t Lr = lane < depth ? partial[(q * smax + 0) * L + lane] : KEY_NONE;
+  uint64_t pre[4];  // the next lists, one coalesced load each, issued together
+#pragma unroll
+  for (int u = 0; u < 4; ++u) pre[u] = 1 + u < nseg ? partial[(q * smax + 1 + u) * L + lane] : KEY_NONE;
   for (int g = 1; g < nseg; ++g) {
-    const uint64_t* src = partial + (q * smax + g) * L;
+    // entries then come by shuffle
+    uint64_t mine;
+    if (g <= 4) {
+      mine = pre[0];
+#pragma unroll
+      for (int u = 1; u < 4; ++u)
+        if (g == 1 + u) mine = pre[u];
+    } else {
+      mine = partial[(q * smax + g) * L + lane];
+    }
     uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
     for (int e = 0; e < depth; ++e) {
-      const uint64_t c = src[e];  // sorted: stop at the first that cannot enter
+      const uint64_t c = __shfl_sync(FULL, (unsigned long long)mine, e);  // sorted: stop at the first that cannot enter
       if (!(c < tk)) break;
       uint64_t one[1] = {Lr};
       wl_insert<1>(one, c, lane);
@@ -662,6 +700,8 @@ __device__ __forceinline__ float fp32_dist_row(const float* __restrict__ x,
   if ((d & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0) {
     const float4* x4 = reinterpret_cast<const float4*>(x);
     const float4* y4 = reinterpret_cast<const float4*>(y);
+    // two float4 per step: each lane reads whole 32-byte sectors of its row
+#pragma unroll 2
     for (; c < (d >> 2); ++c) {
       const float4 a = __ldg(x4 + c), b = __ldg(y4 + c);
       float t = __fsub_rn(a.x, b.x);
@@ -709,7 +749,7 @@ __global__ void k2_rerank(RerankArgs a) {
   const double gam = (double)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07;
   // + the relative error of the FP32-accumulated row norms (two of them)
   const int dpad = (a.d + 7) & ~7;
-  const double nerr = (double)((dpad + 31) / 32 + 2) * u;
+  const double nerr = (double)((dpad + 31) / 32 + 2 + 5) * u;
   const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
   // split form: the MMA adds |hi| |lo| cross terms to the magnitudes it sums
   // (<= (1 + 2^-7) |x~| per side) and leaves out 2 lo_q.lo_p of the estimate
