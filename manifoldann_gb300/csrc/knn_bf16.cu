@@ -137,21 +137,21 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
   const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * stride;
   const int cand = blockIdx.y;
   if (row >= n) return;
-  double rr = 0.0, cc = 0.0;
+  float rr = 0.0f, cc = 0.0f;  // a heuristic score: FP32 is plenty
   for (int c = lane; c < d; c += 32) {
     float sc, mc;
     scale_candidate(cand, mu[c], &sc, &mc);
     const float cv = __fmul_rn(sc, __fsub_rn(x[row * d + c], mc));
     const float bv = __bfloat162float(__float2bfloat16_rn(cv));
-    rr += (double)(cv - bv) * (double)(cv - bv);
-    cc += (double)cv * (double)cv;
+    rr = __fmaf_rn(cv - bv, cv - bv, rr);
+    cc = __fmaf_rn(cv, cv, cc);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     rr += __shfl_xor_sync(FULL, rr, o);
     cc += __shfl_xor_sync(FULL, cc, o);
   }
-  if (lane == 0) atomicAdd(&score[cand], cc > 0.0 ? rr / cc : 0.0);
+  if (lane == 0) atomicAdd(&score[cand], cc > 0.0f ? (double)rr / (double)cc : 0.0);
 }
 
 // pick the candidate with the smallest residual (moving off the plain mean
@@ -740,49 +740,59 @@ __global__ void k2_rerank(RerankArgs a) {
   const uint64_t* lst = a.lists + q * a.L;
   const uint64_t ek_key = lst[a.kreq - 1];
   const uint64_t last_key = lst[a.depth - 1];
-  // threshold (identical on every lane)
-  const RowInfo qi = a.qinfo[q];
-  const double bxn = (double)__uint_as_float(a.bmax->xn_bits);
-  const double br = (double)__uint_as_float(a.bmax->r_bits);
-  const double u = 5.9604644775390625e-08;
-  // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
-  const double gam = (double)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07;
-  // + the relative error of the FP32-accumulated row norms (two of them)
-  const int dpad = (a.d + 7) & ~7;
-  const double nerr = (double)((dpad + 31) / 32 + 2 + 5) * u;
-  const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
-  // split form: the MMA adds |hi| |lo| cross terms to the magnitudes it sums
-  // (<= (1 + 2^-7) |x~| per side) and leaves out 2 lo_q.lo_p of the estimate
-  const double blo = (double)__uint_as_float(a.bmax->lo_bits);
-  const double inflate = blo > 0.0 ? 1.0161 : 1.0;
-  const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn) * inflate +
-                   2.0 * (double)qi.lo_up * blo / c1;
-  const double Rs = (double)qi.r_up + br;
-  const double qn = (double)qi.nrm;  // list keys hold est' = est - ||q~||^2
-  const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key) + qn, 0.0);
-  const double sc = (double)*a.scale;
+  // threshold: computed by lane 0 (FP64 is slow on this part), then broadcast
   const bool cosine = a.metric == MANN_METRIC_COSINE;
-  double sU = sqrt(ek + c1 * A) + Rs;
-  // cosine: every point of the FP32-form top-k has ||q^ - p^||^2 <= U / s^2 + 4 eps_c
-  if (cosine) sU = sqrt(sU * sU + 4.0 * a.eps_c * sc * sc);
-  const double U = sU * sU;
-  const double slack = 3.0 * (double)(a.d + 2) * u * U + 1e-6 * U + 1e-30;
-  const double T = ((sU + Rs) * (sU + Rs) + c1 * A + slack) * (1.0 + 1e-9);
-  // lower bound on the exact distance of any point outside the list's est <= T set
-  const double e_floor = fmax(T - c1 * A, 0.0);
-  const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
-  double d_floor = cosine ? 0.5 * s_floor * s_floor / (sc * sc) - a.eps_c
-                          : s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
-  // Every point outside the merged list has est' >= its depth-th entry, or >=
-  // the seed when the list is not full; with neither, the list holds every point.
-  const float sd = a.seed ? a.seed[q] : __int_as_float(0x7F800000);
-  const bool all_in = (last_key == KEY_NONE) && !(sd < 3.0e38f);
-  const double beyond = last_key != KEY_NONE ? (double)key_dist(last_key) : (double)sd;
-  // without the row's k-th estimate (fewer than k points admitted below the
-  // seed) the threshold is unknown: the row is not certified
-  bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
-  // a zero-norm (or non-finite) query has no unit direction: the FP32 form answers it
-  if (cosine && !(a.cos_qn[q] > 0.0f && a.cos_qn[q] < 3.0e38f)) certified = false;
+  const double qn = (double)a.qinfo[q].nrm;  // list keys hold est' = est - ||q~||^2
+  double T = 0.0, d_floor = 0.0;
+  int cert_i = 0, all_in_i = 0;
+  if (lane == 0) {
+    const RowInfo qi = a.qinfo[q];
+    const double bxn = (double)__uint_as_float(a.bmax->xn_bits);
+    const double br = (double)__uint_as_float(a.bmax->r_bits);
+    const double u = 5.9604644775390625e-08;
+    // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
+    const double gam = (double)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07;
+    // + the relative error of the FP32-accumulated row norms (two of them)
+    const int dpad = (a.d + 7) & ~7;
+    const double nerr = (double)((dpad + 31) / 32 + 2 + 5) * u;
+    const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
+    // split form: the MMA adds |hi| |lo| cross terms to the magnitudes it sums
+    // (<= (1 + 2^-7) |x~| per side) and leaves out 2 lo_q.lo_p of the estimate
+    const double blo = (double)__uint_as_float(a.bmax->lo_bits);
+    const double inflate = blo > 0.0 ? 1.0161 : 1.0;
+    const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn) * inflate +
+                     2.0 * (double)qi.lo_up * blo / c1;
+    const double Rs = (double)qi.r_up + br;
+    const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key) + qn, 0.0);
+    const double sc = (double)*a.scale;
+    double sU = sqrt(ek + c1 * A) + Rs;
+    // cosine: every point of the FP32-form top-k has ||q^ - p^||^2 <= U / s^2 + 4 eps_c
+    if (cosine) sU = sqrt(sU * sU + 4.0 * a.eps_c * sc * sc);
+    const double U = sU * sU;
+    const double slack = 3.0 * (double)(a.d + 2) * u * U + 1e-6 * U + 1e-30;
+    T = ((sU + Rs) * (sU + Rs) + c1 * A + slack) * (1.0 + 1e-9);
+    // lower bound on the exact distance of any point outside the list's est <= T set
+    const double e_floor = fmax(T - c1 * A, 0.0);
+    const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
+    d_floor = cosine ? 0.5 * s_floor * s_floor / (sc * sc) - a.eps_c
+                     : s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
+    // Every point outside the merged list has est' >= its depth-th entry, or >=
+    // the seed when the list is not full; with neither, the list holds every point.
+    const float sd = a.seed ? a.seed[q] : __int_as_float(0x7F800000);
+    const bool all_in = (last_key == KEY_NONE) && !(sd < 3.0e38f);
+    const double beyond = last_key != KEY_NONE ? (double)key_dist(last_key) : (double)sd;
+    // without the row's k-th estimate (fewer than k points admitted below the
+    // seed) the threshold is unknown: the row is not certified
+    bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
+    // a zero-norm (or non-finite) query has no unit direction: the FP32 form answers it
+    if (cosine && !(a.cos_qn[q] > 0.0f && a.cos_qn[q] < 3.0e38f)) certified = false;
+    cert_i = certified ? 1 : 0;
+    all_in_i = all_in ? 1 : 0;
+  }
+  T = __shfl_sync(FULL, T, 0);
+  d_floor = __shfl_sync(FULL, d_floor, 0);
+  const bool certified = __shfl_sync(FULL, cert_i, 0) != 0;
+  const bool all_in = __shfl_sync(FULL, all_in_i, 0) != 0;
   {
     // depth this row's certificate needs: one past its last est <= T entry
     const uint64_t kl = lst[lane];
