@@ -46,7 +46,7 @@ __global__ void probe_count_kernel(const int32_t* __restrict__ probes, int64_t n
 
 // Exclusive prefix sums of the per-list query counts and of their 32-query
 // chunks; one block of 1024 threads, each owning a contiguous run of lists.
-__global__ void __launch_bounds__(1024) probe_scan_kernel(const unsigned* __restrict__ cnt, int nlist,
+__global__ void __launch_bounds__(1024) probe_scan_kernel(const unsigned* __restrict__ cnt, int nlist, int qc,
                                                           int64_t* __restrict__ qoff,
                                                           int64_t* __restrict__ choff) {
   __shared__ int64_t wa[32], wb[32];
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(1024) probe_scan_kernel(const unsigned* __rest
   int64_t a = 0, b = 0;
   for (int l = l0; l < l1; ++l) {
     a += cnt[l];
-    b += (cnt[l] + SCAN_Q - 1) / SCAN_Q;
+    b += (cnt[l] + qc - 1) / qc;
   }
   int64_t ia = a, ib = b;  // inclusive scans within the warp
   for (int o = 1; o < 32; o <<= 1) {
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(1024) probe_scan_kernel(const unsigned* __rest
     qoff[l] = ea;
     choff[l] = eb;
     ea += cnt[l];
-    eb += (cnt[l] + SCAN_Q - 1) / SCAN_Q;
+    eb += (cnt[l] + qc - 1) / qc;
   }
   if (t == 1023) {
     qoff[nlist] = ea;
@@ -110,22 +110,22 @@ __global__ void probe_scatter_kernel(const int32_t* __restrict__ probes, int64_t
   pair_r[pos] = (int32_t)(i % nprobe);
 }
 
-// One CTA: list l and up to 32 of its queries.  Each thread takes one point
+// One CTA: list l and up to QC (16 or 32) of its queries.  Each thread takes one point
 // of the list per pass (read in place through the list's ids) and computes
 // its distance to every query of the CTA -- the point's coordinates in
 // registers, the queries' in shared memory, each distance the sequential
 // difference-form sum over dimensions 0..d-1 of the FP32 form.  Warp w keeps
-// the sorted top-k of queries w, w+8, w+16, w+24 as warp-distributed lists.
-template <int METRIC, int KW, bool VEC>
-__global__ void __launch_bounds__(SCAN_T, 2)
+// the sorted top-k of queries w, w+8, ... as warp-distributed lists.
+template <int METRIC, int KW, bool VEC, int QC>
+__global__ void __launch_bounds__(SCAN_T, QC == 16 ? 3 : 2)
     ivf_scan_kernel(const float* __restrict__ data, const int64_t* __restrict__ loff,
                     const int32_t* __restrict__ lids, const float* __restrict__ qs, int d,
                     const int64_t* __restrict__ qoff, const int32_t* __restrict__ pair_q,
                     const int32_t* __restrict__ pair_r, const int64_t* __restrict__ choff, int nlist,
                     int k, int nprobe, uint64_t* __restrict__ partial) {
-  __shared__ __align__(16) float qsm[SCAN_Q][SCAN_DC];
-  __shared__ float dsm[SCAN_Q][SCAN_T + 1];
-  __shared__ int32_t s_q[SCAN_Q];
+  __shared__ __align__(16) float qsm[QC][SCAN_DC];
+  __shared__ float dsm[QC][SCAN_T + 1];
+  __shared__ int32_t s_q[QC];
 
   const int64_t w = blockIdx.x;
   if (w >= choff[nlist]) return;
@@ -136,16 +136,17 @@ __global__ void __launch_bounds__(SCAN_T, 2)
     else hi = mid - 1;
   }
   const int l = lo;
-  const int64_t e0 = qoff[l] + (w - choff[l]) * SCAN_Q;
-  const int nqe = (int)min((int64_t)SCAN_Q, qoff[l + 1] - e0);
+  const int64_t e0 = qoff[l] + (w - choff[l]) * QC;
+  const int nqe = (int)min((int64_t)QC, qoff[l + 1] - e0);
   const int64_t p_begin = loff[l], p_end = loff[l + 1];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (t < nqe) s_q[t] = pair_q[e0 + t];
   __syncthreads();
 
-  uint64_t L[4][KW];
+  constexpr int MW = QC / 8;  // queries per warp
+  uint64_t L[MW][KW];
 #pragma unroll
-  for (int m = 0; m < 4; ++m)
+  for (int m = 0; m < MW; ++m)
 #pragma unroll
     for (int s = 0; s < KW; ++s) L[m][s] = KEY_NONE;
 
@@ -153,13 +154,13 @@ __global__ void __launch_bounds__(SCAN_T, 2)
     const int64_t pi = p0 + t;
     const bool valid = pi < p_end;
     const float* prow = data + (valid ? (int64_t)lids[pi] : 0) * d;
-    float acc[SCAN_Q];
+    float acc[QC];
 #pragma unroll
-    for (int j = 0; j < SCAN_Q; ++j) acc[j] = 0.0f;
+    for (int j = 0; j < QC; ++j) acc[j] = 0.0f;
     for (int c0 = 0; c0 < d; c0 += SCAN_DC) {
       const int dc = min(SCAN_DC, d - c0);
       __syncthreads();
-      for (int e = t; e < SCAN_Q * SCAN_DC; e += SCAN_T) {
+      for (int e = t; e < QC * SCAN_DC; e += SCAN_T) {
         const int r = e / SCAN_DC, c = e % SCAN_DC;
         qsm[r][c] = (r < nqe && c < dc) ? __ldg(&qs[(int64_t)s_q[r] * d + c0 + c]) : 0.0f;
       }
@@ -180,7 +181,7 @@ __global__ void __launch_bounds__(SCAN_T, 2)
       __syncthreads();
       // dimensions past d are zero in both operands: (0 - 0)^2 adds nothing
 #pragma unroll
-      for (int j = 0; j < SCAN_Q; ++j) {
+      for (int j = 0; j < QC; ++j) {
         if (j < nqe) {
           float a = acc[j];
 #pragma unroll
@@ -200,12 +201,12 @@ __global__ void __launch_bounds__(SCAN_T, 2)
       }
     }
 #pragma unroll
-    for (int j = 0; j < SCAN_Q; ++j)
+    for (int j = 0; j < QC; ++j)
       if (j < nqe) dsm[j][t] = METRIC == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc[j]) : acc[j];
     __syncthreads();
     const int np = (int)min((int64_t)SCAN_T, p_end - p0);
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
+    for (int m = 0; m < MW; ++m) {
       const int j = warp + 8 * m;
       if (j >= nqe) continue;  // warp-uniform
       uint64_t thr = wl::list_get<KW>(L[m], k - 1);
@@ -226,7 +227,7 @@ __global__ void __launch_bounds__(SCAN_T, 2)
     }
   }
 #pragma unroll
-  for (int m = 0; m < 4; ++m) {
+  for (int m = 0; m < MW; ++m) {
     const int j = warp + 8 * m;
     if (j >= nqe) continue;
     uint64_t* dst = partial + ((int64_t)s_q[j] * nprobe + pair_r[e0 + j]) * k;
@@ -240,29 +241,33 @@ __global__ void __launch_bounds__(SCAN_T, 2)
 
 
 template <int METRIC, int KW, bool VEC>
-mann_status launch_scan_t(cudaStream_t s, int64_t grid, const float* data, const int64_t* loff,
+mann_status launch_scan_t(cudaStream_t s, int qc, int64_t grid, const float* data, const int64_t* loff,
                           const int32_t* lids, const float* qs, int d, const int64_t* qoff,
                           const int32_t* pair_q, const int32_t* pair_r, const int64_t* choff, int nlist, int k,
                           int nprobe, uint64_t* partial) {
-  ivf_scan_kernel<METRIC, KW, VEC><<<(unsigned)grid, SCAN_T, 0, s>>>(data, loff, lids, qs, d, qoff, pair_q, pair_r,
-                                                                     choff, nlist, k, nprobe, partial);
+  if (qc == 16)
+    ivf_scan_kernel<METRIC, KW, VEC, 16><<<(unsigned)grid, SCAN_T, 0, s>>>(data, loff, lids, qs, d, qoff, pair_q,
+                                                                           pair_r, choff, nlist, k, nprobe, partial);
+  else
+    ivf_scan_kernel<METRIC, KW, VEC, 32><<<(unsigned)grid, SCAN_T, 0, s>>>(data, loff, lids, qs, d, qoff, pair_q,
+                                                                           pair_r, choff, nlist, k, nprobe, partial);
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
 template <int METRIC>
-mann_status launch_scan_m(cudaStream_t s, int64_t grid, bool vec, const float* data, const int64_t* loff,
+mann_status launch_scan_m(cudaStream_t s, int qc, int64_t grid, bool vec, const float* data, const int64_t* loff,
                           const int32_t* lids, const float* qs, int d, const int64_t* qoff,
                           const int32_t* pair_q, const int32_t* pair_r, const int64_t* choff, int nlist, int k,
                           int nprobe, uint64_t* partial) {
   if (k <= 32)
-    return vec ? launch_scan_t<METRIC, 1, true>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+    return vec ? launch_scan_t<METRIC, 1, true>(s, qc, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
                                                 nlist, k, nprobe, partial)
-               : launch_scan_t<METRIC, 1, false>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+               : launch_scan_t<METRIC, 1, false>(s, qc, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
                                                  nlist, k, nprobe, partial);
-  return vec ? launch_scan_t<METRIC, 2, true>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+  return vec ? launch_scan_t<METRIC, 2, true>(s, qc, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
                                               nlist, k, nprobe, partial)
-             : launch_scan_t<METRIC, 2, false>(s, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
+             : launch_scan_t<METRIC, 2, false>(s, qc, grid, data, loff, lids, qs, d, qoff, pair_q, pair_r, choff,
                                                nlist, k, nprobe, partial);
 }
 
@@ -295,20 +300,22 @@ mann_status ivf_scan_device(Context* ctx, cudaStream_t s, const float* data, int
   MANN_CUDA_TRY(cudaMemsetAsync(partial, 0xFF, sizeof(uint64_t) * nq * nprobe * k, s));
   probe_count_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(probes, nq * nprobe, nlist, cnt);
   MANN_CHECK_LAUNCH();
-  probe_scan_kernel<<<1, 1024, 0, s>>>(cnt, nlist, qoff, choff);
+  // 16-query chunks when lists see few queries (more, lighter CTAs), else 32
+  const int qc = nq * nprobe <= (int64_t)12 * nlist ? 16 : SCAN_Q;
+  probe_scan_kernel<<<1, 1024, 0, s>>>(cnt, nlist, qc, qoff, choff);
   MANN_CHECK_LAUNCH();
   probe_scatter_kernel<<<(unsigned)ceil_div(nq * nprobe, 256), 256, 0, s>>>(
       probes, nq, nprobe, nlist, qoff, cnt + nlist, pair_q, pair_r);
   MANN_CHECK_LAUNCH();
   // chunks <= pairs/32 + lists; blocks past the real count return at once
-  const int64_t max_chunks = ceil_div(nq * nprobe, SCAN_Q) + nlist;
+  const int64_t max_chunks = ceil_div(nq * nprobe, qc) + nlist;
   const bool vec = (d % 4) == 0 && (reinterpret_cast<uintptr_t>(data) & 15) == 0;
   ctx->time_begin(s);
   if (metric == MANN_METRIC_EUCLIDEAN)
-    MANN_TRY(launch_scan_m<MANN_METRIC_EUCLIDEAN>(s, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q, pair_r,
+    MANN_TRY(launch_scan_m<MANN_METRIC_EUCLIDEAN>(s, qc, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q, pair_r,
                                                   choff, nlist, k, nprobe, partial));
   else
-    MANN_TRY(launch_scan_m<MANN_METRIC_SQEUCLIDEAN>(s, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q,
+    MANN_TRY(launch_scan_m<MANN_METRIC_SQEUCLIDEAN>(s, qc, max_chunks, vec, data, loff, lids, qs, d, qoff, pair_q,
                                                     pair_r, choff, nlist, k, nprobe, partial));
   ctx->time_end(s);
   MANN_TRY(launch_merge_lists(partial, nq, nprobe, k, keys, s));
