@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "kernels.cuh"
+#include "f32x2.cuh"
 #include "warp_list.cuh"
 
 namespace mann {
@@ -165,11 +166,12 @@ __device__ __forceinline__ void k1_body(const float* __restrict__ base, int64_t 
 
   for (int64_t t0 = nb0; t0 < nb1; t0 += K1_BN) {
     const int64_t tend = min(nb1, t0 + K1_BN);
-    float acc[TQ][TN];
+    // accumulators of columns 2j, 2j+1 packed in one f32x2 pair
+    uint64_t acc2[TQ][TN / 2];
 #pragma unroll
     for (int i = 0; i < TQ; ++i)
 #pragma unroll
-      for (int j = 0; j < TN; ++j) acc[i][j] = 0.0f;
+      for (int j = 0; j < TN / 2; ++j) acc2[i][j] = 0ull;
 
     qload.load(qs, qrows, q0, nq, d, 0, tid);
     bload.load(base, nullptr, t0, tend, d, 0, tid);
@@ -191,17 +193,22 @@ __device__ __forceinline__ void k1_body(const float* __restrict__ base, int64_t 
         float qv[TQ], bv[TN];
         load_q_frag<TQ>(qsb + kk * QSTR, ty, qv);
         load_b_frag(bsb + kk * BSTR, tx, bv);
+        uint64_t b2[TN / 2];
 #pragma unroll
-        for (int i = 0; i < TQ; ++i)
+        for (int j = 0; j < TN / 2; ++j) b2[j] = f2::pack(bv[2 * j], bv[2 * j + 1]);
 #pragma unroll
-          for (int j = 0; j < TN; ++j) {
+        for (int i = 0; i < TQ; ++i) {
+          const uint64_t q2 = f2::pack(qv[i], qv[i]);
+#pragma unroll
+          for (int j = 0; j < TN / 2; ++j) {
             if constexpr (METRIC == MANN_METRIC_COSINE) {
-              acc[i][j] = __fmaf_rn(qv[i], bv[j], acc[i][j]);
+              acc2[i][j] = f2::fma(q2, b2[j], acc2[i][j]);
             } else {
-              const float t = __fsub_rn(qv[i], bv[j]);
-              acc[i][j] = __fmaf_rn(t, t, acc[i][j]);
+              const uint64_t t = f2::sub(q2, b2[j]);
+              acc2[i][j] = f2::fma(t, t, acc2[i][j]);
             }
           }
+        }
       }
       if (more) {
         qload.store(Qs + (buf ^ 1) * K1_DK * QSTR, QSTR, tid);
@@ -210,6 +217,11 @@ __device__ __forceinline__ void k1_body(const float* __restrict__ base, int64_t 
       __syncthreads();
     }
 
+    float acc[TQ][TN];
+#pragma unroll
+    for (int i = 0; i < TQ; ++i)
+#pragma unroll
+      for (int j = 0; j < TN / 2; ++j) f2::unpack(acc2[i][j], acc[i][2 * j], acc[i][2 * j + 1]);
     // finish the metric and stage the tile
 #pragma unroll
     for (int i = 0; i < TQ; ++i) {
