@@ -266,6 +266,32 @@ mann_status mann_ivf_search_learned(mann_probe* m, const mann_knn_params* p, int
                                     const int32_t* list_ids, const float* queries, int64_t q,
                                     int32_t* out_ids, float* out_dists);
 
+/* ------------------------------------------------------ local PCA (batched)
+ * fit_geometry(::PCAMethod, data, center, neighbor_indices)
+ * (src/geometry/pca.jl:101-241) for m centres at once -- the per-node fits of
+ * LocalGeometryEstimator in build_weighted_graph
+ * (src/graphs/weighted_knn_graph.jl:247-264).  Centre i is data row
+ * centres[i], or query_points[i] (row-major [m][d]) when centres is NULL;
+ * neighbors[m][k] (k <= 32) are data row ids, -1 = none.  Outputs:
+ * out_dim[m], out_eigvals[m][maxd] (descending; zero past the dimension),
+ * out_basis[m][maxd][d] (principal directions as rows, i.e. the bytes of
+ * Julia's d x dim basis).  FP32, one-sided Jacobi; the eigenvalues are the
+ * squared singular values of the centred neighbours, as the reference's. */
+typedef struct {
+  int32_t intrinsic_dim;      /* > 0: fixed dimension; 0: by variance ratio */
+  int32_t reserved;
+  double min_variance_ratio;  /* (0, 1], default 0.95 */
+} mann_pca_params;
+
+mann_status mann_local_pca(const mann_pca_params* p, const float* data, int64_t n, int32_t d,
+                           const int32_t* centres, const float* query_points, int64_t m,
+                           const int32_t* neighbors, int32_t k, int32_t maxd, int32_t* out_dim,
+                           float* out_eigvals, float* out_basis);
+mann_status mann_local_pca_device(const mann_pca_params* p, const float* data, int64_t n, int32_t d,
+                                  const int32_t* centres, const float* query_points, int64_t m,
+                                  const int32_t* neighbors, int32_t k, int32_t maxd, int32_t* out_dim,
+                                  float* out_eigvals, float* out_basis, void* stream);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python

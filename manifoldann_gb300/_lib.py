@@ -114,6 +114,10 @@ class ProbeParams(C.Structure):
     ]
 
 
+class PcaParams(C.Structure):
+    _fields_ = [("intrinsic_dim", C.c_int32), ("reserved", C.c_int32), ("min_variance_ratio", C.c_double)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -159,6 +163,9 @@ SIGNATURES = {
                                       C.POINTER(KnnReport)]),
     "mann_knn_graph_batched_device": (_I32, [C.POINTER(KnnParams), _P, _P, _I32, _I32, _I32, _P, _P,
                                              C.POINTER(KnnReport), _P]),
+    "mann_local_pca": (_I32, [C.POINTER(PcaParams), _P, _I64, _I32, _P, _P, _I64, _P, _I32, _I32, _P, _P, _P]),
+    "mann_local_pca_device": (_I32, [C.POINTER(PcaParams), _P, _I64, _I32, _P, _P, _I64, _P, _I32, _I32, _P, _P,
+                                     _P, _P]),
     "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                     _I64, _P, _P, _P]),
 }

@@ -75,6 +75,8 @@ enum ScratchSlot : int {
   SLOT_COS_Q,         // BF16 cosine: unit-normalised queries
   SLOT_COS_NB,        // BF16 cosine: squared norms of the points
   SLOT_COS_NQ,        // BF16 cosine: squared norms of the queries
+  SLOT_PCA_IDX,       // host-pointer local PCA: neighbour and centre ids, dimensions
+  SLOT_PCA_BASIS,     // host-pointer local PCA: bases
   SLOT_COUNT
 };
 
