@@ -406,6 +406,20 @@ def run_batched_leg(args, stream_ptr=0):
     e1.record(stream)
     torch.cuda.synchronize()
     pca_ms = e0.elapsed_time(e1) / 3
+    wts = torch.empty((N, 15), dtype=torch.float32, device="cuda")
+
+    def weights():
+        _lib.check(lib.mann_edge_weights_device(4, X.data_ptr(), N, 32, glob.data_ptr(), 15, dims.data_ptr(),
+                                                basis.data_ptr(), 15, wts.data_ptr(), None, stream_ptr))
+
+    weights()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(3):
+        weights()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wt_ms = e0.elapsed_time(e1) / 3
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     achieved = 2.0 * 32 * pairs / (ms / 1e3) / 1e12
     return {"workload": BATCH_WORKLOAD, "points": N, "pairs": pairs, "ms_per_step": ms,
@@ -415,7 +429,8 @@ def run_batched_leg(args, stream_ptr=0):
                          "frac": achieved / fp32_peak, "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2.07 GHz)",
                          "work": "2*d flops per ordered pair"},
             "launches_per_step": r.launches,
-            "local_pca": {"ms": pca_ms, "nodes_per_s": N / (pca_ms / 1e3), "neighbours": 15, "intrinsic_dim": 2}}
+            "local_pca": {"ms": pca_ms, "nodes_per_s": N / (pca_ms / 1e3), "neighbours": 15, "intrinsic_dim": 2},
+            "edge_weights": {"rule": "CurvatureFreeSymmetric", "ms": wt_ms, "edges_per_s": N * 15 / (wt_ms / 1e3)}}
 
 
 def run_ivf_profile_case(args):

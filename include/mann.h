@@ -292,6 +292,27 @@ mann_status mann_local_pca_device(const mann_pca_params* p, const float* data, i
                                   const int32_t* neighbors, int32_t k, int32_t maxd, int32_t* out_dim,
                                   float* out_eigvals, float* out_basis, void* stream);
 
+/* ---------------------------------------------------------- edge weights
+ * compute_edge_weight for every edge of a kNN graph
+ * (src/graphs/edge_weight.jl:163-262, src/graphs/weighted_knn_graph.jl:194-236):
+ * nbrs[n][k] (0-based, -1 = none -> NaN weight), per-vertex tangent estimates
+ * as written by mann_local_pca (dims[n], basis[n][maxd][d]); out_weights[n][k];
+ * *out_negative = edges where the curvature-free estimator fell back to the
+ * Euclidean chord (EstimatorDiagnostics.n_negative_fallbacks). */
+#define MANN_EDGE_EUCLIDEAN_CHORD 0  /* ||x_j - x_i|| */
+#define MANN_EDGE_TANGENT_SOURCE 1   /* d_T^(i) */
+#define MANN_EDGE_TANGENT_MEAN 2     /* (d_T^(i) + d_T^(j)) / 2 */
+#define MANN_EDGE_TANGENT_MAX 3      /* max(d_T^(i), d_T^(j)) */
+#define MANN_EDGE_CURVATURE_FREE 4   /* (8 d_E - d_T^(i) - d_T^(j)) / 6, d_E when negative */
+
+mann_status mann_edge_weights(int32_t rule, const float* data, int64_t n, int32_t d, const int32_t* nbrs,
+                              int32_t k, const int32_t* dims, const float* basis, int32_t maxd,
+                              float* out_weights, int64_t* out_negative);
+mann_status mann_edge_weights_device(int32_t rule, const float* data, int64_t n, int32_t d,
+                                     const int32_t* nbrs, int32_t k, const int32_t* dims,
+                                     const float* basis, int32_t maxd, float* out_weights,
+                                     int64_t* out_negative, void* stream);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python

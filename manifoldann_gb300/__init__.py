@@ -14,8 +14,10 @@ from .graphs import (KNNGraph, build_knn_graph, build_knn_graphs, graph_metadata
 from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, assign_arrays,
                          assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
                          pairwise_distances, take_pending_assignments, transform)
-from .geometry import (PCAGeometry, PCAMethod, fit_geometries, fit_geometry, intrinsic_dimension,
-                       local_distance, project, reconstruct)
+from .geometry import (CurvatureFreeSymmetric, EuclideanChord, PCAGeometry, PCAMethod,
+                       TangentProjectedSourceOnly, TangentProjectedSymmetricMax,
+                       TangentProjectedSymmetricMean, compute_edge_weights, fit_geometries, fit_geometry,
+                       intrinsic_dimension, local_distance, project, reconstruct)
 from .ivf import IVFFlatIndex, TopKRouting, ivf_search_device, select_indices
 from .probe import LearnedProbeRouting, ProbeModel, ivf_search_learned, neighbour_list_labels
 from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
@@ -36,5 +38,6 @@ __all__ = [
     "IVFFlatIndex", "TopKRouting", "ivf_search_device", "select_indices",
     "LearnedProbeRouting", "ProbeModel", "ivf_search_learned", "neighbour_list_labels",
     "PCAGeometry", "PCAMethod", "fit_geometries", "fit_geometry", "intrinsic_dimension", "local_distance",
-    "project", "reconstruct",
+    "project", "reconstruct", "CurvatureFreeSymmetric", "EuclideanChord", "TangentProjectedSourceOnly",
+    "TangentProjectedSymmetricMax", "TangentProjectedSymmetricMean", "compute_edge_weights",
 ]

@@ -77,6 +77,7 @@ enum ScratchSlot : int {
   SLOT_COS_NQ,        // BF16 cosine: squared norms of the queries
   SLOT_PCA_IDX,       // host-pointer local PCA: neighbour and centre ids, dimensions
   SLOT_PCA_BASIS,     // host-pointer local PCA: bases
+  SLOT_EDGE_COUNT,    // edge weights: negative-fallback counter
   SLOT_COUNT
 };
 

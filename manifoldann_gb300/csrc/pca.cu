@@ -287,3 +287,156 @@ mann_status mann_local_pca(const mann_pca_params* p, const float* data, int64_t 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- edge weights
+// compute_edge_weight over every edge of a kNN graph
+// (src/graphs/edge_weight.jl:163-262 via _compute_edge_weights_and_diagnostics,
+// src/graphs/weighted_knn_graph.jl:194-236): warp per node, lane per edge.
+// d_E = ||x_j - x_i||; d_T^(c) = ||B_c^T (x_j - x_i)|| with B_c node c's
+// principal directions (rows of basis[c], dims[c] of them).
+namespace mann {
+namespace {
+
+__device__ __forceinline__ float tangent_chord(const float* __restrict__ B, int dim, int d,
+                                               const float* __restrict__ x, const float* __restrict__ y) {
+  // the displacement's coordinates: with the geometry centred on an endpoint
+  // this is project(y) - project(x) of the reference
+  float s = 0.0f;
+  for (int r = 0; r < dim; ++r) {
+    const float* b = B + (int64_t)r * d;
+    float t = 0.0f;
+    for (int c = 0; c < d; ++c) t = __fmaf_rn(b[c], __fsub_rn(y[c], x[c]), t);
+    s = __fmaf_rn(t, t, s);
+  }
+  return sqrtf(s);
+}
+
+__global__ void edge_weights_kernel(int rule, const float* __restrict__ data, int64_t n, int d,
+                                    const int32_t* __restrict__ nbrs, int k, const int32_t* __restrict__ dims,
+                                    const float* __restrict__ basis, int maxd, float* __restrict__ out,
+                                    unsigned long long* __restrict__ n_neg) {
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  for (int e = lane; e < k; e += 32) {
+    const int32_t j = nbrs[i * k + e];
+    float wv = __int_as_float(0x7fc00000);
+    if (j >= 0 && j < n) {
+      const float* x = data + i * d;
+      const float* y = data + (int64_t)j * d;
+      float s = 0.0f;
+      for (int c = 0; c < d; ++c) {
+        const float t = __fsub_rn(y[c], x[c]);
+        s = __fmaf_rn(t, t, s);
+      }
+      const float dE = sqrtf(s);
+      if (rule == MANN_EDGE_EUCLIDEAN_CHORD) {
+        wv = dE;
+      } else {
+        const float dx = tangent_chord(basis + i * (int64_t)maxd * d, dims[i], d, x, y);
+        if (rule == MANN_EDGE_TANGENT_SOURCE) {
+          wv = dx;
+        } else {
+          const float dy = tangent_chord(basis + (int64_t)j * maxd * d, dims[j], d, x, y);
+          if (rule == MANN_EDGE_TANGENT_MEAN) {
+            wv = 0.5f * (dx + dy);
+          } else if (rule == MANN_EDGE_TANGENT_MAX) {
+            wv = fmaxf(dx, dy);
+          } else {  // curvature-free symmetric, Euclidean chord when negative
+            const float raw = (8.0f * dE - dx - dy) / 6.0f;
+            if (raw < 0.0f) {
+              wv = dE;
+              atomicAdd(n_neg, 1ull);
+            } else {
+              wv = raw;
+            }
+          }
+        }
+      }
+    }
+    out[i * k + e] = wv;
+  }
+}
+
+}  // namespace
+}  // namespace mann
+
+extern "C" {
+
+static mann_status edge_check(int32_t rule, const float* data, int64_t n, int32_t d, const int32_t* nbrs, int32_t k,
+                              const int32_t* dims, const float* basis, int32_t maxd, const float* out) {
+  if (rule < MANN_EDGE_EUCLIDEAN_CHORD || rule > MANN_EDGE_CURVATURE_FREE)
+    return fail(MANN_EINVAL_ARG, "unknown edge weight rule");
+  if (d <= 0 || n <= 0 || k < 0) return fail(MANN_EINVAL_ARG, "empty graph");
+  if (!data || !nbrs || !out) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  if (rule != MANN_EDGE_EUCLIDEAN_CHORD && (!dims || !basis || maxd <= 0))
+    return fail(MANN_EINVAL_ARG, "tangent-projected weights require per-vertex tangent estimates");
+  return MANN_OK;
+}
+
+mann_status mann_edge_weights_device(int32_t rule, const float* data, int64_t n, int32_t d, const int32_t* nbrs,
+                                     int32_t k, const int32_t* dims, const float* basis, int32_t maxd,
+                                     float* out_weights, int64_t* out_negative, void* stream) {
+  clear_error();
+  MANN_TRY(edge_check(rule, data, n, d, nbrs, k, dims, basis, maxd, out_weights));
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  CallScope scope(ctx, s);
+  unsigned long long* cnt = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_EDGE_COUNT, 1, &cnt));
+  MANN_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+  if (k > 0) {
+    edge_weights_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(rule, data, n, d, nbrs, k, dims, basis, maxd,
+                                                                out_weights, cnt);
+    MANN_CHECK_LAUNCH();
+  }
+  if (out_negative) {
+    unsigned long long h = 0;
+    MANN_CUDA_TRY(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
+    MANN_CUDA_TRY(cudaStreamSynchronize(s));
+    *out_negative = (int64_t)h;
+  }
+  return MANN_OK;
+}
+
+mann_status mann_edge_weights(int32_t rule, const float* data, int64_t n, int32_t d, const int32_t* nbrs, int32_t k,
+                              const int32_t* dims, const float* basis, int32_t maxd, float* out_weights,
+                              int64_t* out_negative) {
+  clear_error();
+  MANN_TRY(edge_check(rule, data, n, d, nbrs, k, dims, basis, maxd, out_weights));
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = ctx->stream;
+  CallScope scope(ctx, s);
+  const bool tangent = rule != MANN_EDGE_EUCLIDEAN_CHORD;
+  float *dx = nullptr, *dw = nullptr, *db = nullptr;
+  int32_t* dn = nullptr;
+  unsigned long long* cnt = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_BASE, (size_t)n * d, &dx));
+  MANN_TRY(ctx->scratch_t(SLOT_PCA_IDX, (size_t)n * (k + 1), &dn));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_DISTS, (size_t)n * k + 1, &dw));
+  MANN_TRY(ctx->scratch_t(SLOT_EDGE_COUNT, 1, &cnt));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dx, data, sizeof(float) * n * d, cudaMemcpyHostToDevice, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dn, nbrs, sizeof(int32_t) * n * k, cudaMemcpyHostToDevice, s));
+  int32_t* ddim = dn + n * k;
+  if (tangent) {
+    MANN_TRY(ctx->scratch_t(SLOT_PCA_BASIS, (size_t)n * maxd * d, &db));
+    MANN_CUDA_TRY(cudaMemcpyAsync(ddim, dims, sizeof(int32_t) * n, cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(db, basis, sizeof(float) * n * maxd * d, cudaMemcpyHostToDevice, s));
+  }
+  MANN_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), s));
+  if (k > 0) {
+    edge_weights_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(rule, dx, n, d, dn, k, tangent ? ddim : nullptr,
+                                                                db, maxd, dw, cnt);
+    MANN_CHECK_LAUNCH();
+  }
+  unsigned long long h = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(out_weights, dw, sizeof(float) * n * k, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  if (out_negative) *out_negative = (int64_t)h;
+  return MANN_OK;
+}
+
+}  // extern "C"

@@ -109,3 +109,60 @@ def fit_geometry(method: PCAMethod, data, center, neighbor_indices) -> PCAGeomet
         dims, eig, basis = fit_geometries(method, a, nb, query_points=c.reshape(-1, 1))
     dd = int(dims[0])
     return PCAGeometry(c, basis[0, :dd].T.copy(), eig[0, :dd].copy())
+
+
+# ---------------------------------------------------------------- edge weights
+class AbstractEdgeWeight:
+    code = -1
+
+
+class EuclideanChord(AbstractEdgeWeight):
+    """``EuclideanChord()`` (src/graphs/edge_weight.jl:80): ||x_j - x_i||."""
+    code = 0
+
+
+class TangentProjectedSourceOnly(AbstractEdgeWeight):
+    """``TangentProjectedSourceOnly()`` (edge_weight.jl:94)."""
+    code = 1
+
+
+class TangentProjectedSymmetricMean(AbstractEdgeWeight):
+    """``TangentProjectedSymmetricMean()`` (edge_weight.jl:106)."""
+    code = 2
+
+
+class TangentProjectedSymmetricMax(AbstractEdgeWeight):
+    """``TangentProjectedSymmetricMax()`` (edge_weight.jl:119)."""
+    code = 3
+
+
+class CurvatureFreeSymmetric(AbstractEdgeWeight):
+    """``CurvatureFreeSymmetric()`` (edge_weight.jl:147): (8 d_E - d_T^(x) - d_T^(y)) / 6,
+    the chord where that is negative (counted)."""
+    code = 4
+
+
+def compute_edge_weights(rule: AbstractEdgeWeight, data, neighbors, dims=None, bases=None):
+    """Weights of every edge of a graph: neighbors [n][k] 1-based (0 = none ->
+    NaN), tangent estimates (dims [n], bases [n][maxd][d] from fit_geometries)
+    for the tangent rules.  Returns (weights [n][k] float32, negative fallbacks)."""
+    import ctypes as C
+
+    X = points_view(np.asarray(data))
+    n, d = X.shape
+    nb = np.asarray(neighbors)
+    if nb.shape[0] != n:
+        raise DimensionMismatch("one neighbour row per point")
+    k = nb.shape[1]
+    nb0 = np.ascontiguousarray(np.where(nb > 0, nb - 1, -1), dtype=np.int32)
+    out = np.empty((n, k), np.float32)
+    neg = C.c_int64(0)
+    if rule.code != 0 and (dims is None or bases is None):
+        raise ArgumentError(f"{type(rule).__name__} requires per-vertex tangent estimates; got `geometries=nothing`")
+    dd = np.ascontiguousarray(dims, np.int32) if dims is not None else None
+    bb = np.ascontiguousarray(bases, np.float32) if bases is not None else None
+    maxd = int(bb.shape[1]) if bb is not None else 0
+    _lib.check(_lib.load().mann_edge_weights(
+        rule.code, X.ctypes.data, n, d, nb0.ctypes.data, k, dd.ctypes.data if dd is not None else None,
+        bb.ctypes.data if bb is not None else None, maxd, out.ctypes.data, C.byref(neg)))
+    return out, int(neg.value)

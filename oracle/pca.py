@@ -52,3 +52,40 @@ def fit_pca(center, neighbors, intrinsic_dim=None, min_variance_ratio=0.95):
         hit = np.nonzero(cum >= min_variance_ratio)[0]
         dim = int(hit[0]) + 1 if hit.size else max_d
     return dim, vals[:dim], vecs[:, :dim]
+
+
+def edge_weights(rule, X, nbrs, bases, dims):
+    """FP64 compute_edge_weight for every edge (src/graphs/edge_weight.jl:163-262):
+    rule 0 chord, 1 source tangent, 2 mean, 3 max, 4 curvature-free (chord when
+    negative).  bases[i] is d x dim_i.  Returns (weights [n][k], negatives)."""
+    X = np.asarray(X, np.float64)
+    n, k = nbrs.shape
+    out = np.full((n, k), np.nan)
+    neg = 0
+    for i in range(n):
+        for e in range(k):
+            j = nbrs[i, e]
+            if j < 0:
+                continue
+            diff = X[j] - X[i]
+            dE = np.linalg.norm(diff)
+            if rule == 0:
+                out[i, e] = dE
+                continue
+            dx = np.linalg.norm(bases[i][:, :dims[i]].T @ diff)
+            if rule == 1:
+                out[i, e] = dx
+                continue
+            dy = np.linalg.norm(bases[j][:, :dims[j]].T @ diff)
+            if rule == 2:
+                out[i, e] = 0.5 * (dx + dy)
+            elif rule == 3:
+                out[i, e] = max(dx, dy)
+            else:
+                raw = (8 * dE - dx - dy) / 6
+                if raw < 0:
+                    out[i, e] = dE
+                    neg += 1
+                else:
+                    out[i, e] = raw
+    return out, neg

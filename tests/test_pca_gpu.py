@@ -103,3 +103,32 @@ def test_local_pca_full_graph(gpu_lib):
     for i in rng.choice(N, 300, replace=False):
         _, vals_o, B_o = pca.fit_pca(X[i], X[glob[i]], intrinsic_dim=2)
         assert np.allclose(eig[i, :2], vals_o, rtol=1e-3, atol=1e-7)
+
+
+@pytest.mark.parametrize("rule", [0, 1, 2, 3, 4])
+def test_edge_weights_match_oracle(gpu_lib, rule):
+    import manifoldann_gb300 as M
+    from oracle import pca
+
+    from manifoldann_gb300 import synthetic
+
+    clouds = synthetic.manifold_clouds(3, 800, 1500, 16, seed=rule)
+    X = np.concatenate(clouds)
+    ids, _, offs = M.knn_graph_batched_arrays([c.T for c in clouds], 10, distance=M.SqEuclidean())
+    glob = (ids + np.repeat(offs[:-1], np.diff(offs))[:, None]).astype(np.int64)
+    glob[5, 3] = -1  # a missing edge gives NaN
+    method = M.PCAMethod(intrinsic_dim=2)
+    dims, eig, basis = M.fit_geometries(method, X.T, np.where(glob >= 0, glob + 1, 0),
+                                        centers=np.arange(len(X)) + 1)
+    rules = [M.EuclideanChord(), M.TangentProjectedSourceOnly(), M.TangentProjectedSymmetricMean(),
+             M.TangentProjectedSymmetricMax(), M.CurvatureFreeSymmetric()]
+    w, neg = M.compute_edge_weights(rules[rule], X.T, np.where(glob >= 0, glob + 1, 0), dims, basis)
+    bases = [basis[i].T.astype(np.float64) for i in range(len(X))]
+    w_o, neg_o = pca.edge_weights(rule, X, glob, bases, dims)
+    assert np.isnan(w[5, 3]) and np.isnan(w_o[5, 3])
+    ok = ~np.isnan(w_o)
+    assert np.allclose(w[ok], w_o[ok], rtol=1e-4, atol=1e-6)
+    assert neg == neg_o
+    if rule == 0:
+        with pytest.raises(M.ArgumentError):
+            M.compute_edge_weights(M.TangentProjectedSourceOnly(), X.T, glob + 1)
