@@ -125,6 +125,19 @@ mann_status mann_knn_graph_batched_device(const mann_knn_params* p, const float*
                                           int32_t nsets, int32_t d, int32_t include_self, int32_t* out_ids,
                                           float* out_dists, mann_knn_report* report, void* stream);
 
+/* Undirected kNN graph: _symmetrize_adjacency (src/graphs/knn_graph.jl:196-210)
+ * as CSR.  ids[n][k] 0-based (-1 = none); row i of the result is
+ * out(i) ∪ in(i), ascending, without repeats.  out_row_offsets[n+1];
+ * out_cols needs room for 2 n k entries; *out_nnz = entries written.
+ * MANN_EINVAL_ARG if a vertex has more than 16384 distinct neighbours. */
+mann_status mann_knn_graph_symmetrize(const int32_t* ids, int64_t n, int32_t k, int64_t* out_row_offsets,
+                                      int32_t* out_cols, int64_t* out_nnz);
+/* Same on device buffers (ids, out_row_offsets, out_cols); *out_nnz is a host
+ * pointer, written once the stream has finished. */
+mann_status mann_knn_graph_symmetrize_device(const int32_t* ids, int64_t n, int32_t k,
+                                             int64_t* out_row_offsets, int32_t* out_cols, int64_t* out_nnz,
+                                             void* stream);
+
 /* ------------------------------------------------------------ KMeans (KMeansTransform) */
 
 typedef struct {

@@ -10,7 +10,7 @@ from .distances import (CosineDist, Euclidean, SqEuclidean, cosine_distance, def
                         default_squared_distance, euclidean_distance)
 from .eval_utils import recall_at_k
 from .graphs import (KNNGraph, build_knn_graph, build_knn_graphs, graph_metadata, has_metadata,
-                     knn_graph_arrays, knn_graph_batched_arrays, node_metadata)
+                     knn_graph_arrays, knn_graph_batched_arrays, knn_graph_symmetrize_csr, node_metadata)
 from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, assign_arrays,
                          assign_clusters, fit, get_bucket_assignment, init_kmeans_plus_plus, lloyd,
                          pairwise_distances, take_pending_assignments, transform)
@@ -29,7 +29,7 @@ __all__ = [
     "default_squared_distance", "euclidean_distance",
     "recall_at_k",
     "KNNGraph", "build_knn_graph", "build_knn_graphs", "graph_metadata", "has_metadata", "knn_graph_arrays",
-    "knn_graph_batched_arrays", "node_metadata",
+    "knn_graph_batched_arrays", "knn_graph_symmetrize_csr", "node_metadata",
     "AbstractANNIndex", "BruteForceIndex", "Neighbor", "build_index", "configured_k",
     "index_distance", "insert", "knn_arrays", "neighbor_ids", "query", "supports_mutation",
     "KMeansAssignment", "KMeansTransform", "TransformResult", "assign_arrays", "assign_clusters", "fit",

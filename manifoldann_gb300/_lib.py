@@ -168,6 +168,8 @@ SIGNATURES = {
                                      _P, _P]),
     "mann_edge_weights": (_I32, [_I32, _P, _I64, _I32, _P, _I32, _P, _P, _I32, _P, _P]),
     "mann_edge_weights_device": (_I32, [_I32, _P, _I64, _I32, _P, _I32, _P, _P, _I32, _P, _P, _P]),
+    "mann_knn_graph_symmetrize": (_I32, [_P, _I64, _I32, _P, _P, _P]),
+    "mann_knn_graph_symmetrize_device": (_I32, [_P, _I64, _I32, _P, _P, _P, _P]),
     "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                     _I64, _P, _P, _P]),
 }

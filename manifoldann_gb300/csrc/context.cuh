@@ -78,6 +78,11 @@ enum ScratchSlot : int {
   SLOT_PCA_IDX,       // host-pointer local PCA: neighbour and centre ids, dimensions
   SLOT_PCA_BASIS,     // host-pointer local PCA: bases
   SLOT_EDGE_COUNT,    // edge weights: negative-fallback counter
+  SLOT_CSR_COUNTS,    // union graph: degrees, cursors, long rows
+  SLOT_CSR_OFFS,      // union graph: row capacities
+  SLOT_CSR_BUF,       // union graph: unsorted rows
+  SLOT_CSR_COLS,      // host-pointer union graph: columns
+  SLOT_CSR_ROWS,      // host-pointer union graph: row offsets
   SLOT_COUNT
 };
 

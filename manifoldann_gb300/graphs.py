@@ -134,6 +134,21 @@ def build_knn_graphs(clouds, *, k: int, distance=None, include_self: bool = Fals
     return out
 
 
+def knn_graph_symmetrize_csr(ids):
+    """Union (undirected) graph of a kNN id table [n][k] (0-based, -1 = none) on
+    the GPU as CSR: (row_offsets [n+1] int64, cols [nnz] int32 ascending per row)."""
+    import ctypes as C
+
+    a = np.ascontiguousarray(ids, dtype=np.int32)
+    n, k = a.shape
+    offs = np.empty(n + 1, np.int64)
+    cols = np.empty(max(2 * n * k, 1), np.int32)
+    nnz = C.c_int64(0)
+    _lib.check(_lib.load().mann_knn_graph_symmetrize(a.ctypes.data, n, k, offs.ctypes.data, cols.ctypes.data,
+                                                     C.byref(nnz)))
+    return offs, cols[:nnz.value].copy()
+
+
 def build_knn_graph(index, data, *, k: Optional[int] = None, include_self: bool = False,
                     directed: bool = True, metadata=None, **query_kwargs) -> KNNGraph:
     """``build_knn_graph(index, data; k, include_self, directed, metadata)``
@@ -155,7 +170,11 @@ def build_knn_graph(index, data, *, k: Optional[int] = None, include_self: bool 
         adjacency = index.build_adjacency(a, resolved_k, include_self, **query_kwargs)
     original_k = resolved_k
     if not directed:
-        adjacency = _symmetrize_adjacency(adjacency, n_points)
+        if isinstance(index, BruteForceIndex):
+            offs, cols = knn_graph_symmetrize_csr(ids)
+            adjacency = [(cols[offs[i]:offs[i + 1]].astype(np.int64) + 1).tolist() for i in range(n_points)]
+        else:
+            adjacency = _symmetrize_adjacency(adjacency, n_points)
         resolved_k = max(len(nb) for nb in adjacency)
     meta = _create_graph_metadata(original_k, directed, metadata, n_points)
     return KNNGraph(adjacency, resolved_k, include_self, meta)
