@@ -83,6 +83,30 @@ class IVFFlatIndex(AbstractANNIndex):
         return cls(Ct, norms, offs, ids, d, max(1, min(nprobe, nlist)), distance, centroid_metric,
                    int(it[0]))
 
+    def save(self, path) -> None:
+        """Write the index (centroids, norms, CSR lists, settings) to an .npz file."""
+        from .distances import metric_code
+
+        np.savez(path, format=np.array("manifoldann-gb300/ivf-flat/1"), centroids=self.centroids,
+                 centroid_norms=self.centroid_norms, list_offsets=self.list_offsets, list_ids=self.list_ids,
+                 dimension=np.int64(self.dimension), default_nprobe=np.int64(self.default_nprobe),
+                 distance=np.int64(metric_code(self.distance)),
+                 centroid_metric=np.int64(metric_code(self.centroid_metric)),
+                 kmeans_iters=np.int64(self.kmeans_iters))
+
+    @classmethod
+    def load(cls, path):
+        """Read an index written by ``save``."""
+        from .distances import CosineDist
+
+        metrics = {0: Euclidean, 1: SqEuclidean, 2: CosineDist}
+        with np.load(path) as z:
+            if str(z["format"]) != "manifoldann-gb300/ivf-flat/1":
+                raise ArgumentError(f"not an IVF-Flat index file: {path}")
+            return cls(np.asfortranarray(z["centroids"]), z["centroid_norms"].copy(), z["list_offsets"].copy(),
+                       z["list_ids"].copy(), int(z["dimension"]), int(z["default_nprobe"]),
+                       metrics[int(z["distance"])](), metrics[int(z["centroid_metric"])](), int(z["kmeans_iters"]))
+
     def _check(self, a: np.ndarray, qlen: int) -> None:
         """``_validate_dimensions`` (src/indices/ivf_flat.jl:95-101)."""
         if a.shape[0] != self.dimension:

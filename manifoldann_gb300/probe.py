@@ -71,6 +71,27 @@ class ProbeModel:
         _lib.check(_lib.load().mann_probe_get_params(self.handle, out.ctypes.data))
         return out
 
+    def save(self, path) -> None:
+        """Write the network (flat parameters, widths, settings, centroids of the prior) to an .npz file."""
+        p = self.p
+        np.savez(path, format=np.array("manifoldann-gb300/probe/1"), params=self.params(),
+                 dims=np.array(self.dims, np.int64), use_prior=np.int64(self.use_prior),
+                 centroids=self._cent if self._cent is not None else np.zeros((0, 0), np.float32),
+                 hyper=np.array([p.batch, p.lr, p.weight_decay, p.beta_init], np.float64), seed=np.uint64(p.seed))
+
+    @classmethod
+    def load(cls, path):
+        """Re-create a network written by ``save`` on the current device."""
+        with np.load(path) as z:
+            if str(z["format"]) != "manifoldann-gb300/probe/1":
+                raise ArgumentError(f"not a probe file: {path}")
+            din, h1, h2, nout = (int(v) for v in z["dims"])
+            batch, lr, wd, beta_init = z["hyper"].tolist()
+            prior = bool(int(z["use_prior"]))
+            return cls(din, nout, (h1, h2), use_prior=prior, centroids=z["centroids"] if prior else None,
+                       batch=int(batch), lr=lr, weight_decay=wd, beta_init=beta_init, seed=int(z["seed"]),
+                       params=z["params"])
+
     def train(self, queries, labels, epochs: int) -> np.ndarray:
         """queries [n][din] float32, labels [n][L] int32 list ids (-1 = none)."""
         q = np.ascontiguousarray(queries, np.float32)

@@ -158,3 +158,23 @@ def test_ivf_validation(gpu_lib):
         idx.query(np.zeros((5, 10), np.float32), np.zeros(5, np.float32), 3)
     with pytest.raises(M.DimensionMismatch):
         idx.query(np.zeros((4, 10), np.float32), np.zeros(3, np.float32), 3)
+
+
+def test_index_and_probe_persist(gpu_lib, tmp_path):
+    import manifoldann_gb300 as M
+
+    X = _data(8000, 24, 31)
+    Q = _data(200, 24, 32)
+    idx = M.build_index(M.IVFFlatIndex, X.T, nlist=32, nprobe=3, distance=M.SqEuclidean(), seed=2)
+    idx.save(tmp_path / "ivf.npz")
+    idx2 = M.IVFFlatIndex.load(tmp_path / "ivf.npz")
+    a, da = idx.search_arrays(X.T, Q.T, 7)
+    b, db = idx2.search_arrays(X.T, Q.T, 7)
+    assert np.array_equal(a, b) and np.array_equal(da, db)
+    assert idx2.distance == idx.distance and idx2.default_nprobe == 3
+    r = M.LearnedProbeRouting.train(idx, X.T, _data(3000, 24, 33).T, k=3, hidden=(128, 128), epochs=2, seed=1)
+    r.model.save(tmp_path / "probe.npz")
+    m2 = M.ProbeModel.load(tmp_path / "probe.npz")
+    assert np.array_equal(m2.params(), r.model.params())
+    r2 = M.LearnedProbeRouting(3, m2)
+    assert np.array_equal(M.ivf_search_learned(idx, r, X.T, Q.T, 7)[0], M.ivf_search_learned(idx2, r2, X.T, Q.T, 7)[0])
