@@ -390,13 +390,13 @@ def run_batched_leg(args, stream_ptr=0):
     glob = ids + torch.from_numpy(offs_rows).cuda()[:, None]
     cen = torch.arange(N, dtype=torch.int32, device="cuda")
     dims = torch.empty(N, dtype=torch.int32, device="cuda")
-    eig = torch.empty((N, 15), dtype=torch.float32, device="cuda")
-    basis = torch.empty((N, 15, 32), dtype=torch.float32, device="cuda")
+    eig = torch.empty((N, 2), dtype=torch.float32, device="cuda")  # slots for the 2 kept directions
+    basis = torch.empty((N, 2, 32), dtype=torch.float32, device="cuda")
     pp = _lib.PcaParams(2, 0, 0.95)
 
     def pca():
         _lib.check(lib.mann_local_pca_device(pp, X.data_ptr(), N, 32, cen.data_ptr(), None, N, glob.data_ptr(), 15,
-                                             15, dims.data_ptr(), eig.data_ptr(), basis.data_ptr(), stream_ptr))
+                                             2, dims.data_ptr(), eig.data_ptr(), basis.data_ptr(), stream_ptr))
 
     pca()
     torch.cuda.synchronize()
@@ -410,7 +410,7 @@ def run_batched_leg(args, stream_ptr=0):
 
     def weights():
         _lib.check(lib.mann_edge_weights_device(4, X.data_ptr(), N, 32, glob.data_ptr(), 15, dims.data_ptr(),
-                                                basis.data_ptr(), 15, wts.data_ptr(), None, stream_ptr))
+                                                basis.data_ptr(), 2, wts.data_ptr(), None, stream_ptr))
 
     weights()
     torch.cuda.synchronize()

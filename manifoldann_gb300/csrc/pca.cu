@@ -198,12 +198,160 @@ __global__ void __launch_bounds__(PCA_WARPS * 32)
   }
 }
 
+// Register form for d <= 32: lane a holds column a in registers and fetches
+// its partner's column by shuffles; no shared memory, no warp barriers.
+__global__ void __launch_bounds__(256)
+    local_pca_reg_kernel(const float* __restrict__ data, int64_t n, int d, const float* __restrict__ qpts,
+                         const int32_t* __restrict__ centres, int64_t m, const int32_t* __restrict__ nbrs, int k,
+                         int fixed_dim, float min_ratio, int maxd, int32_t* __restrict__ out_dim,
+                         float* __restrict__ out_eig, float* __restrict__ out_basis) {
+  constexpr int D = 32;
+  const int lane = threadIdx.x & 31;
+  const int64_t node = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (node >= m) return;  // warp-uniform
+  const int32_t ci = centres ? centres[node] : -1;
+  int32_t* odim = out_dim + node;
+  float* oeig = out_eig + node * maxd;
+  float* obas = out_basis + node * (int64_t)maxd * d;
+  if (ci >= n || (ci < 0 && !qpts)) {
+    if (lane == 0) *odim = 0;
+    for (int j = lane; j < maxd; j += 32) oeig[j] = 0.0f;
+    for (int e = lane; e < maxd * d; e += 32) obas[e] = 0.0f;
+    return;
+  }
+  const float* cp = ci >= 0 ? data + (int64_t)ci * d : qpts + node * d;
+  const int32_t nb = lane < k ? nbrs[node * k + lane] : -1;
+  const bool have = nb >= 0 && nb < n;
+  const unsigned have_mask = __ballot_sync(FULLM, have);
+  const int keff = __popc(have_mask);
+  if (keff < 2) {
+    const int dd = min(fixed_dim > 0 ? fixed_dim : 1, min(d, maxd));
+    if (lane == 0) *odim = dd;
+    for (int j = lane; j < maxd; j += 32) oeig[j] = j < dd ? 1.0f : 0.0f;
+    for (int e = lane; e < maxd * d; e += 32) obas[e] = (e / d < dd && e % d == e / d) ? 1.0f : 0.0f;
+    return;
+  }
+  // own centred neighbour, then compacted: lane a takes the a-th present neighbour
+  float v[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = (have && c < d) ? __fsub_rn(data[(int64_t)nb * d + c], cp[c]) : 0.0f;
+  const int src = lane < keff ? (int)__fns(have_mask, 0, lane + 1) : lane;
+  float w[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const float x = __shfl_sync(FULLM, v[c], src);
+    w[c] = lane < keff ? x : 0.0f;
+  }
+  const int kp = (keff + 1) & ~1;
+  const float tol = (float)(2 * (d + kp)) * 5.9604645e-08f;
+  for (int sweep = 0; sweep < PCA_MAX_SWEEPS; ++sweep) {
+    bool rotated = false;
+    for (int r = 0; r < kp - 1; ++r) {
+      int partner = lane;
+      if (lane < kp) {
+        const int pos = lane == 0 ? 0 : 1 + ((lane - 1 + r) % (kp - 1));
+        const int ppos = kp - 1 - pos;
+        partner = ppos == 0 ? 0 : 1 + ((ppos - 1 - r + (kp - 1)) % (kp - 1));
+      }
+      const bool act = lane < keff && partner < keff && partner != lane;
+      float p[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) p[c] = __shfl_sync(FULLM, w[c], act ? partner : lane);
+      if (act) {
+        const bool first = lane < partner;
+        // both lanes sum (lower column, higher column) in the same order
+        float alpha = 0.0f, beta = 0.0f, gamma = 0.0f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          const float x = first ? w[c] : p[c], y = first ? p[c] : w[c];
+          alpha = __fmaf_rn(x, x, alpha);
+          beta = __fmaf_rn(y, y, beta);
+          gamma = __fmaf_rn(x, y, gamma);
+        }
+        if (gamma != 0.0f && fabsf(gamma) > tol * sqrtf(alpha) * sqrtf(beta)) {
+          const float zeta = (beta - alpha) / (2.0f * gamma);
+          const float t = copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+          const float cth = 1.0f / sqrtf(1.0f + t * t);
+          const float sth = cth * t;
+          rotated = true;
+#pragma unroll
+          for (int c = 0; c < D; ++c)
+            w[c] = first ? __fsub_rn(__fmul_rn(cth, w[c]), __fmul_rn(sth, p[c]))
+                         : __fadd_rn(__fmul_rn(sth, p[c]), __fmul_rn(cth, w[c]));
+        }
+      }
+    }
+    if (!__any_sync(FULLM, rotated)) break;
+  }
+  float nrm2 = 0.0f;
+#pragma unroll
+  for (int c = 0; c < D; ++c) nrm2 = __fmaf_rn(w[c], w[c], nrm2);
+  if (lane >= keff) nrm2 = 0.0f;
+  int rank = 0;
+  float lmax = 0.0f;
+  for (int o = 0; o < keff; ++o) {
+    const float x = __shfl_sync(FULLM, nrm2, o);
+    lmax = fmaxf(lmax, x);
+    if (x > nrm2 || (x == nrm2 && o < lane)) ++rank;
+  }
+  const int maxdim = min(d, keff);
+  int dsel;
+  if (fixed_dim > 0) {
+    dsel = min(fixed_dim, maxdim);
+  } else {
+    float total = 0.0f, cum = 0.0f;
+    for (int rr = 0; rr < keff; ++rr) {
+      const unsigned who = __ballot_sync(FULLM, lane < keff && rank == rr);
+      total = __fadd_rn(total, __shfl_sync(FULLM, nrm2, __ffs(who) - 1));
+    }
+    dsel = maxdim;
+    if (total == 0.0f) {
+      dsel = 1;
+    } else {
+      for (int rr = 0; rr < maxdim; ++rr) {
+        const unsigned who = __ballot_sync(FULLM, lane < keff && rank == rr);
+        cum = __fadd_rn(cum, __shfl_sync(FULLM, nrm2, __ffs(who) - 1));
+        if (__fdiv_rn(cum, total) >= min_ratio) {
+          dsel = rr + 1;
+          break;
+        }
+      }
+    }
+  }
+  dsel = min(dsel, maxd);
+  if (lane == 0) *odim = dsel;
+  if (lane < keff && rank < maxd) {
+    oeig[rank] = rank < dsel ? nrm2 : 0.0f;
+    const float sg = sqrtf(nrm2);
+    const float tolz = 1.1920929e-07f * fmaxf(lmax, 1.0f) * (float)max(d, keff);
+    float* orow = obas + (int64_t)rank * d;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      if (c >= d) break;
+      float x = 0.0f;
+      if (rank < dsel) x = nrm2 > tolz ? __fdiv_rn(w[c], sg) : (c == rank ? 1.0f : 0.0f);
+      orow[c] = x;
+    }
+  }
+  for (int rr = keff + lane; rr < maxd; rr += 32) {
+    oeig[rr] = 0.0f;
+    for (int c = 0; c < d; ++c) obas[(int64_t)rr * d + c] = 0.0f;
+  }
+}
+
 }  // namespace
 
 mann_status local_pca_device(cudaStream_t s, const float* data, int64_t n, int d, const float* qpts,
                              const int32_t* centres, int64_t m, const int32_t* nbrs, int k, int fixed_dim,
                              double min_ratio, int maxd, int32_t* out_dim, float* out_eig, float* out_basis) {
   if (m <= 0) return MANN_OK;
+  if (d <= 32) {
+    local_pca_reg_kernel<<<(unsigned)ceil_div(m, 8), 256, 0, s>>>(data, n, d, qpts, centres, m, nbrs, k, fixed_dim,
+                                                                   (float)min_ratio, maxd, out_dim, out_eig,
+                                                                   out_basis);
+    MANN_CHECK_LAUNCH();
+    return MANN_OK;
+  }
   const size_t smem = sizeof(float) * PCA_WARPS * 32 * (size_t)(d + 1);
   if (smem > 200 * 1024) return fail(MANN_EINVAL_ARG, "local PCA supports d <= 800");
   if (smem > 48 * 1024)
@@ -297,7 +445,7 @@ mann_status mann_local_pca(const mann_pca_params* p, const float* data, int64_t 
 namespace mann {
 namespace {
 
-__device__ __forceinline__ float tangent_chord(const float* __restrict__ B, int dim, int d,
+__device__ __forceinline__ float tangent_chord(const float* __restrict__ B, int dim, int d, bool vec,
                                                const float* __restrict__ x, const float* __restrict__ y) {
   // the displacement's coordinates: with the geometry centred on an endpoint
   // this is project(y) - project(x) of the reference
@@ -305,7 +453,19 @@ __device__ __forceinline__ float tangent_chord(const float* __restrict__ B, int 
   for (int r = 0; r < dim; ++r) {
     const float* b = B + (int64_t)r * d;
     float t = 0.0f;
-    for (int c = 0; c < d; ++c) t = __fmaf_rn(b[c], __fsub_rn(y[c], x[c]), t);
+    if (vec) {
+      for (int c = 0; c < d; c += 4) {
+        const float4 bv = __ldg(reinterpret_cast<const float4*>(b + c));
+        const float4 xv = __ldg(reinterpret_cast<const float4*>(x + c));
+        const float4 yv = __ldg(reinterpret_cast<const float4*>(y + c));
+        t = __fmaf_rn(bv.x, __fsub_rn(yv.x, xv.x), t);
+        t = __fmaf_rn(bv.y, __fsub_rn(yv.y, xv.y), t);
+        t = __fmaf_rn(bv.z, __fsub_rn(yv.z, xv.z), t);
+        t = __fmaf_rn(bv.w, __fsub_rn(yv.w, xv.w), t);
+      }
+    } else {
+      for (int c = 0; c < d; ++c) t = __fmaf_rn(b[c], __fsub_rn(y[c], x[c]), t);
+    }
     s = __fmaf_rn(t, t, s);
   }
   return sqrtf(s);
@@ -324,20 +484,37 @@ __global__ void edge_weights_kernel(int rule, const float* __restrict__ data, in
     if (j >= 0 && j < n) {
       const float* x = data + i * d;
       const float* y = data + (int64_t)j * d;
+      // rows, basis rows and the base pointers are 16-byte aligned when d % 4 == 0
+      const bool vec = (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(data) | reinterpret_cast<uintptr_t>(basis)) & 15) == 0;
       float s = 0.0f;
-      for (int c = 0; c < d; ++c) {
-        const float t = __fsub_rn(y[c], x[c]);
-        s = __fmaf_rn(t, t, s);
+      if (vec) {
+        for (int c = 0; c < d; c += 4) {
+          const float4 xv = __ldg(reinterpret_cast<const float4*>(x + c));
+          const float4 yv = __ldg(reinterpret_cast<const float4*>(y + c));
+          float t = __fsub_rn(yv.x, xv.x);
+          s = __fmaf_rn(t, t, s);
+          t = __fsub_rn(yv.y, xv.y);
+          s = __fmaf_rn(t, t, s);
+          t = __fsub_rn(yv.z, xv.z);
+          s = __fmaf_rn(t, t, s);
+          t = __fsub_rn(yv.w, xv.w);
+          s = __fmaf_rn(t, t, s);
+        }
+      } else {
+        for (int c = 0; c < d; ++c) {
+          const float t = __fsub_rn(y[c], x[c]);
+          s = __fmaf_rn(t, t, s);
+        }
       }
       const float dE = sqrtf(s);
       if (rule == MANN_EDGE_EUCLIDEAN_CHORD) {
         wv = dE;
       } else {
-        const float dx = tangent_chord(basis + i * (int64_t)maxd * d, dims[i], d, x, y);
+        const float dx = tangent_chord(basis + i * (int64_t)maxd * d, dims[i], d, vec, x, y);
         if (rule == MANN_EDGE_TANGENT_SOURCE) {
           wv = dx;
         } else {
-          const float dy = tangent_chord(basis + (int64_t)j * maxd * d, dims[j], d, x, y);
+          const float dy = tangent_chord(basis + (int64_t)j * maxd * d, dims[j], d, vec, x, y);
           if (rule == MANN_EDGE_TANGENT_MEAN) {
             wv = 0.5f * (dx + dy);
           } else if (rule == MANN_EDGE_TANGENT_MAX) {
