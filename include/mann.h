@@ -49,6 +49,8 @@ typedef int32_t mann_status;
 #define MANN_FLAG_FP64_TIES 1u   /* order near-ties at the k-th boundary by FP64 distances */
 #define MANN_FLAG_TIME_KERNEL 2u /* time the call's dominant kernel into report->kernel_ms
                                     (synchronises the stream before returning) */
+#define MANN_FLAG_FP64_ERR 4u    /* report->max_abs_err_fp64 = max over the returned neighbours of
+                                    |returned distance - FP64 distance| (synchronises the stream) */
 
 typedef struct {
   int32_t metric;    /* MANN_METRIC_* */
@@ -66,7 +68,7 @@ typedef struct {
                                 certified and that were re-run by the exact FP32 scan */
   int64_t rows_fp64_ties;    /* rows where an FP64 recompute ordered a near-tie */
   int64_t candidates;        /* candidates reranked in exact FP32 */
-  double max_abs_err_fp64;   /* reserved (-1) */
+  double max_abs_err_fp64;   /* with MANN_FLAG_FP64_ERR: max |returned - FP64| distance; else -1 */
   int32_t precision_used;    /* MANN_PREC_* actually run */
   int32_t margin_used;       /* candidates kept beyond k by the reduced-precision form */
   double kernel_ms;          /* dominant kernel's CUDA-event time (MANN_FLAG_TIME_KERNEL), else -1 */

@@ -30,6 +30,7 @@ PREC_AUTO = 3
 
 FLAG_FP64_TIES = 1
 FLAG_TIME_KERNEL = 2
+FLAG_FP64_ERR = 4
 
 
 class DimensionMismatch(ValueError):

@@ -107,6 +107,8 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
                            SLOT_PARTIAL, SLOT_KEYS));
   }
   MANN_TRY(launch_finish(keys, nq, kreq, kout, graph_self, nullptr, ids, dists, s));
+  if (rep && (p->flags & MANN_FLAG_FP64_ERR))
+    MANN_TRY(fp64_max_error(ctx, s, base, qs, d, p->metric, nq, kout, ids, dists, &rep->max_abs_err_fp64));
   return MANN_OK;
 }
 

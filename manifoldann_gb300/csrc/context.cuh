@@ -83,6 +83,7 @@ enum ScratchSlot : int {
   SLOT_CSR_BUF,       // union graph: unsorted rows
   SLOT_CSR_COLS,      // host-pointer union graph: columns
   SLOT_CSR_ROWS,      // host-pointer union graph: row offsets
+  SLOT_FP64_ERR,      // maximum FP64 error of the returned distances
   SLOT_COUNT
 };
 

@@ -72,6 +72,8 @@ mann_status launch_k1_segmented(const float* data, const SegItem* items, int nit
 mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_knn_params* p, const float* data,
                                      const int64_t* offs, int nsets, int d, int include_self, int32_t* ids,
                                      float* dists, mann_knn_report* rep);
+mann_status fp64_max_error(Context* ctx, cudaStream_t s, const float* base, const float* qs, int d, int metric,
+                           int64_t nq, int kout, const int32_t* ids, const float* dists, double* out);
 mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, int k, uint64_t* out,
                                cudaStream_t s);
 

@@ -36,6 +36,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "kernels.cuh"
@@ -1003,6 +1004,43 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
 }
 
 }  // namespace
+
+namespace {
+
+// |returned FP32 distance - FP64 distance| of every returned neighbour; the
+// maximum as the bits of a non-negative double (which order as integers)
+__global__ void fp64_err_kernel(const float* __restrict__ base, const float* __restrict__ qs, int d, int metric,
+                                int64_t nq, int kout, const int32_t* __restrict__ ids,
+                                const float* __restrict__ dists, unsigned long long* __restrict__ max_bits) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nq * kout) return;
+  const int32_t id = ids[e];
+  if (id < 0) return;
+  const double ref = fp64_dist_row(qs + (e / kout) * d, base + (int64_t)id * d, d, metric);
+  const double err = fabs((double)dists[e] - ref);
+  if (err == err) atomicMax(max_bits, (unsigned long long)__double_as_longlong(err));
+}
+
+}  // namespace
+
+mann_status fp64_max_error(Context* ctx, cudaStream_t s, const float* base, const float* qs, int d, int metric,
+                           int64_t nq, int kout, const int32_t* ids, const float* dists, double* out) {
+  unsigned long long* bits = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_FP64_ERR, 1, &bits));
+  MANN_CUDA_TRY(cudaMemsetAsync(bits, 0, sizeof(unsigned long long), s));
+  if (nq > 0 && kout > 0) {
+    fp64_err_kernel<<<(unsigned)ceil_div(nq * kout, 256), 256, 0, s>>>(base, qs, d, metric, nq, kout, ids, dists,
+                                                                      bits);
+    MANN_CHECK_LAUNCH();
+  }
+  unsigned long long h = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(&h, bits, sizeof(h), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  double v;
+  std::memcpy(&v, &h, sizeof(v));
+  *out = v;
+  return MANN_OK;
+}
 
 mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,

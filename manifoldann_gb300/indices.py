@@ -109,9 +109,11 @@ def _validate(index: BruteForceIndex, data: np.ndarray, qlen: int) -> None:
 
 
 def knn_arrays(index: BruteForceIndex, data, queries, k: int, *, precision: str = "fp32",
-               fp64_ties: bool = False, margin: int = 0, report: bool = False):
+               fp64_ties: bool = False, margin: int = 0, report: bool = False, fp64_error: bool = False):
     """Batch exact kNN on the GPU; returns (ids [q, min(k,n)] 0-based int32,
-    dists [q, min(k,n)] float32[, report dict]).  ``queries`` is d x q."""
+    dists [q, min(k,n)] float32[, report dict]).  ``queries`` is d x q.
+    With ``fp64_error`` the report's ``max_abs_err_fp64`` holds the largest
+    |returned distance - FP64 distance| over all returned neighbours."""
     a = np.asarray(data)
     Q = np.asarray(queries)
     if Q.ndim == 1:
@@ -129,8 +131,8 @@ def knn_arrays(index: BruteForceIndex, data, queries, k: int, *, precision: str 
     qs = points_view(Q)
     ids = np.empty((nq, keff), np.int32)
     dists = np.empty((nq, keff), np.float32)
-    p = _lib.params(metric_code(index.distance), keff, PRECISIONS[precision], margin,
-                    _lib.FLAG_FP64_TIES if fp64_ties else 0)
+    flags = (_lib.FLAG_FP64_TIES if fp64_ties else 0) | (_lib.FLAG_FP64_ERR if fp64_error else 0)
+    p = _lib.params(metric_code(index.distance), keff, PRECISIONS[precision], margin, flags)
     rep = _lib.KnnReport()
     lib = _lib.load()
     _lib.check(lib.mann_knn(p, base.ctypes.data, n, qs.ctypes.data, nq, a.shape[0], ids.ctypes.data,

@@ -203,3 +203,32 @@ def test_bf16_cosine_full_size_equals_fp32_kernel(gpu_lib):
     ib, db, rep = gpu_knn(base, q, 20, M_COS, precision="bf16", report=True)
     assert np.array_equal(i32, ib) and same_bits(d32, db)
     assert rep["rows_fallback"] <= 100, rep
+
+
+def _fp64_dist(base, q, ids, metric):
+    b = base.astype(np.float64)[ids]                  # [nq][k][d]
+    x = q.astype(np.float64)[:, None, :]
+    if metric == M_COS:
+        r = 1.0 - (b * x).sum(-1) / (np.sqrt((b * b).sum(-1)) * np.sqrt((x * x).sum(-1)))
+        return np.maximum(r, 0.0)
+    s = ((b - x) ** 2).sum(-1)
+    return np.sqrt(s) if metric == M_EUC else s
+
+
+@pytest.mark.parametrize("metric", [M_SQ, M_EUC, M_COS])
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_report_max_fp64_error(gpu_lib, metric, precision):
+    # the report's max |returned - FP64| over every returned neighbour
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.iid_normal(6000, 160, seed=41)
+    q = synthetic.iid_normal(150, 160, seed=42)
+    ids, d, rep = gpu_knn(base, q, 12, metric, precision=precision, report=True, fp64_error=True)
+    want = np.abs(d.astype(np.float64) - _fp64_dist(base, q, ids, metric)).max()
+    got = rep["max_abs_err_fp64"]
+    assert got >= 0.0
+    assert abs(got - want) <= 1e-9 * max(1.0, float(np.abs(d).max()))
+    # FP32 distances of these sizes stay within a few ulps x d of FP64
+    assert got <= 1e-4 * max(1.0, float(np.abs(d).max()))
+    _, _, rep0 = gpu_knn(base, q, 12, metric, precision=precision, report=True)
+    assert rep0["max_abs_err_fp64"] == -1.0
