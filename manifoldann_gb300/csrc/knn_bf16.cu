@@ -36,6 +36,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -114,10 +115,6 @@ __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int
   }
 }
 
-__device__ __forceinline__ float round_up_f(double v) {
-  float f = __double2float_ru(v);
-  return f;
-}
 
 // scale / centre candidates tried on a sample of rows: the one whose BF16
 // rounding residual is smallest wins.  (1, mean) suits general data;
@@ -247,16 +244,18 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     f_c += __shfl_xor_sync(FULL, f_c, o);
     f_l += __shfl_xor_sync(FULL, f_l, o);
   }
-  const double s_b = f_b, s_r = f_r, s_c = f_c, s_l = f_l;
   if (lane == 0 && valid) {
-    const double rel = (double)((dp + 31) / 32 + 2 + 5) * 5.9604644775390625e-08;
+    // FP32 with directed rounding (FP64 is slow on this part): each bound is
+    // rounded up at every step, so it stays an upper bound of the FP64 value
+    const float rel = (float)((dp + 31) / 32 + 2 + 5) * 5.9604644775390625e-08f;  // exact
+    const float onep = __fadd_ru(1.0f, rel);
     RowInfo ri;
-    ri.nrm = __double2float_rn(s_b);
-    ri.xn_up = round_up_f(sqrt(s_b * (1.0 + rel)) * (1.0 + 1e-12));
+    ri.nrm = f_b;
+    ri.xn_up = __fsqrt_ru(__fmul_ru(f_b, onep));
     // ||s(x-mu)_exact - x~|| <= ||cv - x~|| + 2u ||cv|| (1+u), cv = fl(s fl(x-mu))
-    ri.r_up = round_up_f((sqrt(s_r * (1.0 + rel)) +
-                          2.0 * 5.9604645e-08 * 1.0000002 * sqrt(s_c * (1.0 + rel))) * (1.0 + 1e-9));
-    ri.lo_up = split ? round_up_f(sqrt(s_l * (1.0 + rel)) * (1.0 + 1e-12)) : 0.0f;
+    ri.r_up = __fadd_ru(__fsqrt_ru(__fmul_ru(f_r, onep)),
+                        __fmul_ru(__fmul_ru(1.1920928955078125e-07f, 1.0000002f), __fsqrt_ru(__fmul_ru(f_c, onep))));
+    ri.lo_up = split ? __fsqrt_ru(__fmul_ru(f_l, onep)) : 0.0f;
     info[row] = ri;
     if (norms) norms[row] = ri.nrm;
     if (bmax) {  // one global atomic per block and field, not per row
@@ -295,8 +294,18 @@ struct MainArgs {
   int* err;
 };
 
+// a * b / c for non-negative operands, without 128-bit division (a software
+// routine of hundreds of instructions) unless the product needs 64 bits
+__device__ __forceinline__ int64_t muldiv_nn(int64_t a, int64_t b, int64_t c) {
+  const uint64_t ua = (uint64_t)a, ub = (uint64_t)b, uc = (uint64_t)c;
+  if (__umul64hi(ua, ub) != 0) return (int64_t)((__int128)a * b / c);
+  const uint64_t p = ua * ub;
+  if (((p | uc) >> 32) == 0) return (int64_t)((uint32_t)p / (uint32_t)uc);
+  return (int64_t)(p / uc);
+}
+
 __device__ __forceinline__ int64_t chunk_begin(int c, int64_t work, int grid) {
-  return (int64_t)((__int128)c * work / grid);
+  return muldiv_nn(c, work, grid);
 }
 
 // Step s of CTA c's walk over its range [b0, b1) of (query block, point tile)
@@ -312,7 +321,7 @@ __device__ __forceinline__ int64_t walk_item(int64_t b0, int64_t b1, int tiles, 
 
 // the CTA whose work range contains item i
 __device__ __forceinline__ int cta_of(int64_t i, int64_t work, int grid) {
-  int c = (int)((__int128)i * grid / work);
+  int c = (int)muldiv_nn(i, grid, work);
   while (c + 1 < grid && chunk_begin(c + 1, work, grid) <= i) ++c;
   while (c > 0 && chunk_begin(c, work, grid) > i) --c;
   return c;
@@ -689,7 +698,7 @@ struct RerankArgs {
   // are reranked with the FP32 form's cosine on the original rows
   const float* cos_qn;  // [nq] squared norms of the original queries (FP32 form order)
   const float* cos_bn;  // [n]  squared norms of the original points
-  double eps_c;         // |FP32 cosine - ||q^ - p^||^2 / 2| bound
+  float eps_c;          // |FP32 cosine - ||q^ - p^||^2 / 2| bound (rounded up)
   int kdim;             // columns of the tensor-core dot (dp, or 3 dp in the split form)
 };
 
@@ -741,50 +750,59 @@ __global__ void k2_rerank(RerankArgs a) {
   const uint64_t* lst = a.lists + q * a.L;
   const uint64_t ek_key = lst[a.kreq - 1];
   const uint64_t last_key = lst[a.depth - 1];
-  // threshold: computed by lane 0 (FP64 is slow on this part), then broadcast
+  // threshold: computed by lane 0, then broadcast.  FP32 with directed
+  // rounding (FP64 is slow on this part): upper bounds round up, lower bounds
+  // round down, and est' + ||q~||^2 is rounded down where it is compared with
+  // T, so the candidate set only grows and the certificate stays rigorous.
   const bool cosine = a.metric == MANN_METRIC_COSINE;
-  const double qn = (double)a.qinfo[q].nrm;  // list keys hold est' = est - ||q~||^2
-  double T = 0.0, d_floor = 0.0;
+  const float qn = a.qinfo[q].nrm;  // list keys hold est' = est - ||q~||^2
+  float T = 0.0f, d_floor = 0.0f;
   int cert_i = 0, all_in_i = 0;
   if (lane == 0) {
     const RowInfo qi = a.qinfo[q];
-    const double bxn = (double)__uint_as_float(a.bmax->xn_bits);
-    const double br = (double)__uint_as_float(a.bmax->r_bits);
-    const double u = 5.9604644775390625e-08;
+    const float bxn = __uint_as_float(a.bmax->xn_bits);
+    const float br = __uint_as_float(a.bmax->r_bits);
+    const float u = 5.9604644775390625e-08f;
     // one FP32 rounding (or truncation) per 16-term MMA step, x2 margin
-    const double gam = (double)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07;
+    const float gam = (float)((a.kdim + 15) / 16 + 2) * 2.384185791015625e-07f;  // exact
     // + the relative error of the FP32-accumulated row norms (two of them)
     const int dpad = (a.d + 7) & ~7;
-    const double nerr = (double)((dpad + 31) / 32 + 2 + 5) * u;
-    const double c1 = 4.0 * u + 2.0 * gam + 2.0 * nerr;
+    const float nerr = (float)((dpad + 31) / 32 + 2 + 5) * u;  // exact
+    const float c1 = __fadd_ru(__fadd_ru(4.0f * u, 2.0f * gam), 2.0f * nerr);
     // split form: the MMA adds |hi| |lo| cross terms to the magnitudes it sums
-    // (<= (1 + 2^-7) |x~| per side) and leaves out 2 lo_q.lo_p of the estimate
-    const double blo = (double)__uint_as_float(a.bmax->lo_bits);
-    const double inflate = blo > 0.0 ? 1.0161 : 1.0;
-    const double A = ((double)qi.xn_up + bxn) * ((double)qi.xn_up + bxn) * inflate +
-                     2.0 * (double)qi.lo_up * blo / c1;
-    const double Rs = (double)qi.r_up + br;
-    const double ek = ek_key == KEY_NONE ? 0.0 : fmax((double)key_dist(ek_key) + qn, 0.0);
-    const double sc = (double)*a.scale;
-    double sU = sqrt(ek + c1 * A) + Rs;
+    // (<= (1 + 2^-7) |x~| per side, squared 1.01568) and leaves out 2 lo_q.lo_p
+    // of the estimate
+    const float blo = __uint_as_float(a.bmax->lo_bits);
+    const float inflate = blo > 0.0f ? 1.0161f : 1.0f;
+    const float xs = __fadd_ru(qi.xn_up, bxn);
+    const float A = __fadd_ru(__fmul_ru(__fmul_ru(xs, xs), inflate), __fdiv_ru(__fmul_ru(2.0f * qi.lo_up, blo), c1));
+    const float Rs = __fadd_ru(qi.r_up, br);
+    const float c1A = __fmul_ru(c1, A);
+    const float ek = ek_key == KEY_NONE ? 0.0f : fmaxf(__fadd_ru(key_dist(ek_key), qn), 0.0f);
+    const float sc = *a.scale;
+    const float sc2_up = __fmul_ru(sc, sc);
+    float sU = __fadd_ru(__fsqrt_ru(__fadd_ru(ek, c1A)), Rs);
     // cosine: every point of the FP32-form top-k has ||q^ - p^||^2 <= U / s^2 + 4 eps_c
-    if (cosine) sU = sqrt(sU * sU + 4.0 * a.eps_c * sc * sc);
-    const double U = sU * sU;
-    const double slack = 3.0 * (double)(a.d + 2) * u * U + 1e-6 * U + 1e-30;
-    T = ((sU + Rs) * (sU + Rs) + c1 * A + slack) * (1.0 + 1e-9);
+    if (cosine) sU = __fsqrt_ru(__fadd_ru(__fmul_ru(sU, sU), __fmul_ru(4.0f * a.eps_c, sc2_up)));
+    const float U = __fmul_ru(sU, sU);
+    const float rel3 = __fmul_ru((float)(3 * (a.d + 2)), u);
+    const float slack = __fadd_ru(__fadd_ru(__fmul_ru(rel3, U), __fmul_ru(1e-6f, U)), 1e-30f);
+    const float w = __fadd_ru(sU, Rs);
+    T = __fadd_ru(__fadd_ru(__fmul_ru(w, w), c1A), slack);
     // lower bound on the exact distance of any point outside the list's est <= T set
-    const double e_floor = fmax(T - c1 * A, 0.0);
-    const double s_floor = fmax(sqrt(e_floor) - Rs, 0.0);
-    d_floor = cosine ? 0.5 * s_floor * s_floor / (sc * sc) - a.eps_c
-                     : s_floor * s_floor * (1.0 - 3.0 * (double)(a.d + 2) * u) / (sc * sc);
+    const float e_floor = fmaxf(__fsub_rd(T, c1A), 0.0f);
+    const float s_floor = fmaxf(__fsub_rd(__fsqrt_rd(e_floor), Rs), 0.0f);
+    const float s_floor2 = __fmul_rd(s_floor, s_floor);
+    d_floor = cosine ? __fsub_rd(__fdiv_rd(0.5f * s_floor2, sc2_up), a.eps_c)
+                     : __fdiv_rd(__fmul_rd(s_floor2, __fsub_rd(1.0f, rel3)), sc2_up);
     // Every point outside the merged list has est' >= its depth-th entry, or >=
     // the seed when the list is not full; with neither, the list holds every point.
     const float sd = a.seed ? a.seed[q] : __int_as_float(0x7F800000);
     const bool all_in = (last_key == KEY_NONE) && !(sd < 3.0e38f);
-    const double beyond = last_key != KEY_NONE ? (double)key_dist(last_key) : (double)sd;
+    const float beyond = last_key != KEY_NONE ? key_dist(last_key) : sd;
     // without the row's k-th estimate (fewer than k points admitted below the
     // seed) the threshold is unknown: the row is not certified
-    bool certified = all_in || (ek_key != KEY_NONE && beyond + qn > T);
+    bool certified = all_in || (ek_key != KEY_NONE && __fadd_rd(beyond, qn) > T);
     // a zero-norm (or non-finite) query has no unit direction: the FP32 form answers it
     if (cosine && !(a.cos_qn[q] > 0.0f && a.cos_qn[q] < 3.0e38f)) certified = false;
     cert_i = certified ? 1 : 0;
@@ -797,7 +815,7 @@ __global__ void k2_rerank(RerankArgs a) {
   {
     // depth this row's certificate needs: one past its last est <= T entry
     const uint64_t kl = lst[lane];
-    const int le = __popc(__ballot_sync(FULL, kl != KEY_NONE && (double)key_dist(kl) + qn <= T));
+    const int le = __popc(__ballot_sync(FULL, kl != KEY_NONE && __fadd_rd(key_dist(kl), qn) <= T));
     if (lane == 0) atomicAdd(&a.depth_hist[certified ? min(le + 1, LIST) : LIST + 1], 1ull);
   }
   if (!certified) {
@@ -808,7 +826,7 @@ __global__ void k2_rerank(RerankArgs a) {
     }
     return;
   }
-  if (all_in) d_floor = 3.0e38;
+  if (all_in) d_floor = 3.0e38f;
   const float* qrow = a.qs + q * a.d;
   // candidates: entries with est <= T (the list is sorted by est)
   uint64_t key[2] = {KEY_NONE, KEY_NONE};
@@ -818,7 +836,7 @@ __global__ void k2_rerank(RerankArgs a) {
     const int e = s * 32 + lane;
     if (e < a.L) {
       const uint64_t k = lst[e];
-      if (k != KEY_NONE && (double)key_dist(k) + qn <= T) {
+      if (k != KEY_NONE && __fadd_rd(key_dist(k), qn) <= T) {
         const int id = key_id(k);
         const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
                                   : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
@@ -860,8 +878,8 @@ __global__ void k2_rerank(RerankArgs a) {
   for (int e = ncand + lane; e < a.L; e += 32) out[e] = KEY_NONE;
   if (lane == 0) {
     a.cand_count[q] = ncand;
-    float fl = cosine ? __double2float_rd(d_floor) : (float)d_floor;
-    if (a.metric == MANN_METRIC_EUCLIDEAN) fl = (float)sqrt(fmax(d_floor, 0.0)) * (1.0f - 1e-6f);
+    float fl = d_floor;
+    if (a.metric == MANN_METRIC_EUCLIDEAN) fl = __fmul_rd(__fsqrt_rd(fmaxf(d_floor, 0.0f)), 1.0f - 1e-6f);
     a.floor_val[q] = fl;
     atomicAdd(a.cand_total, (unsigned long long)ncand);
   }
@@ -1401,7 +1419,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   {
     const double u = 5.9604644775390625e-08;
     const double gd = (double)d * u / (1.0 - (double)d * u);
-    ra.eps_c = 1.25 * (4.0 * gd + 16.0 * u);
+    ra.eps_c = std::nextafter((float)(1.25 * (4.0 * gd + 16.0 * u)), 1.0f);
   }
   k2_rerank<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(ra);
   MANN_CHECK_LAUNCH();
