@@ -348,17 +348,35 @@ __device__ __forceinline__ void wl_insert(uint64_t (&Lr)[KW], uint64_t c, int la
   }
 }
 
+// ascending bitonic sort of one key per lane across the warp
+__device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint64_t o = __shfl_xor_sync(FULL, (unsigned long long)v, j);
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      v = keep_min ? (o < v ? o : v) : (o > v ? o : v);
+    }
+  }
+  return v;
+}
+
 // One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
 // rows: v holds the row's 32 accumulators of the chunk, nb the chunk's point
 // norms.  The row's list lives in shared memory, entry e at mylist[e * BM],
-// sorted by key; thr_key is its depth-th entry, or the row's seed key
-// (seed est', id 0) until the list is full, and thr_est that key's est'.  The common case -- no column of any row below
-// its threshold -- costs one FMA and one min per value and one vote; a lane
-// with candidates stashes its row in trow and inserts them one by one.
+// unsorted; lslot is the slot of its largest entry and thr_key that entry, or
+// the row's seed key (seed est', id 0) while the list has an empty slot, and
+// thr_est that key's est'.  The common case -- no column of any row below its
+// threshold -- costs one FMA and one min per value and one vote; a lane with
+// candidates stashes its row in trow and admits them one by one: the new key
+// replaces the largest entry and the `depth` entries are rescanned for the new
+// largest (independent loads, conflict-free while the lanes run in step; a
+// sorted insert would be a chain of dependent shared-memory loads).
 __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* __restrict__ nb,
                                           float* __restrict__ trow, uint64_t* __restrict__ mylist,
                                           uint64_t& thr_key, float& thr_est, uint64_t seed_key,
-                                          uint32_t col0, int depth) {
+                                          int& lslot, uint32_t col0, int depth) {
   const float4* nb4 = reinterpret_cast<const float4*>(nb);
   float e[32];
   float mn = __int_as_float(0x7F800000);
@@ -386,17 +404,19 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* 
       mask &= mask - 1;
       const uint64_t c = make_key(trow[j], col0 + (uint32_t)j);
       if (c < thr_key) {
-        // sorted insertion from the end; the depth-th entry drops out
-        int p = depth - 1;
-        while (p > 0) {
-          const uint64_t prev = mylist[(p - 1) * BM];
-          if (prev < c) break;
-          mylist[p * BM] = prev;
-          --p;
+        mylist[lslot * BM] = c;  // the largest entry (or an empty slot) drops out
+        uint64_t m = 0;
+        int ms = 0;
+#pragma unroll 8
+        for (int e2 = 0; e2 < depth; ++e2) {
+          const uint64_t v2 = mylist[e2 * BM];
+          if (v2 > m) {
+            m = v2;
+            ms = e2;
+          }
         }
-        mylist[p * BM] = c;
-        const uint64_t last = mylist[(depth - 1) * BM];
-        thr_key = last == KEY_NONE ? seed_key : last;
+        lslot = ms;
+        thr_key = m == KEY_NONE ? seed_key : m;
         thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
       }
     }
@@ -418,9 +438,11 @@ __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
 // premise); entries past `depth` are admitted points kept while space lasts.
 //
 // Warps: 0 = TMA producer, 1 = MMA issuer (and TMEM owner), then NSETS sets
-// of 4 epilogue warps.  With two sets, set h drains accumulator buffer h, so
-// each set has two tile-times per tile; each set keeps its own lists and
-// writes them to its own partial slot.
+// of 4 epilogue warps.  With two sets, set h drains columns [128h, 128h + 128)
+// of every tile, so a TMEM buffer is free again after half a tile of epilogue
+// work (the MMA of the tile after next reuses it one tile-time later); each
+// set keeps its own lists and writes them to its own partial slot.  A list is
+// sorted when it is written out.
 template <int CAP, int NSETS>
 __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
@@ -452,7 +474,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&tfull_bar[b], 1);
-      ptx::mbar_init(&tempty_bar[b], (NSETS == 2 ? 4 : NEPI) * 32);
+      ptx::mbar_init(&tempty_bar[b], NEPI * 32);
     }
     ptx::fence_mbar_init();
     ptx::prefetch_tensormap(&mapA);
@@ -529,16 +551,20 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
   } else {
     // ------------------------------------------------------------ epilogue
     const int ew = warp - 2;          // 0 .. NEPI-1
-    const int set = ew >> 2;          // which accumulator buffer this warp drains (two sets)
+    const int set = ew >> 2;          // which column half this warp drains (two sets)
     const int quad = warp & 3;        // TMEM lane quadrant this warp may access
     const int row = quad * 32 + lane; // this lane's row of the 128-query tile
+    constexpr int CPS = (BN / 32) / NSETS;  // 32-column chunks per set and tile
+    const int cbeg = set * CPS, cend = cbeg + CPS;
     float* nbw = nbs + ew * BN;       // point norms of the current tile
     float* trow = trans + (ew * 32 + lane) * TSTR;            // this lane's row buffer
-    uint64_t* mylist = lists + (size_t)set * CAP * BM + row;  // entry e at mylist[e * BM]
+    uint64_t* setlists = lists + (size_t)set * CAP * BM;      // entry e of row r at setlists[e * BM + r]
+    uint64_t* mylist = setlists + row;
     const float INF = __int_as_float(0x7F800000);
     uint64_t seed_key = KEY_NONE;
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
+    int lslot = 0;
     int tcount = 0;
     int cur_qb = -1;
     int seg_first_cta = 0;
@@ -546,7 +572,20 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 
     for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
 
-    // norms of this set's first tile; later tiles' norms are fetched one tile ahead
+    // write the warp's 32 row lists of a finished segment, each sorted across the lanes
+    auto flush = [&](int qb_, int slot_) {
+      __syncwarp();
+      const uint64_t* wl = setlists + quad * 32;
+      for (int r = 0; r < 32; ++r) {
+        uint64_t v = lane < CAP ? wl[lane * BM + r] : KEY_NONE;
+        v = warp_sort32(v, lane);
+        const int64_t gq = (int64_t)qb_ * BM + quad * 32 + r;
+        if (gq < a.nq && lane < CAP) a.partial[(gq * a.smax + slot_) * LIST + lane] = v;
+      }
+      __syncwarp();
+    };
+
+    // norms of the first tile; later tiles' norms are fetched one tile ahead
     float nbn[BN / 32];
     auto fetch_norms = [&](int64_t st_) {
       const int64_t item_ = walk_item(it0, it1, a.tiles, st_);
@@ -557,21 +596,16 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         nbn[i] = col < a.n ? __ldg(&a.bnorm[col * a.bstride]) : INF;
       }
     };
-    if (set < it1 - it0) fetch_norms(set);
+    if (it1 > it0) fetch_norms(0);
     for (int64_t st = 0; st < it1 - it0; ++st, ++tcount) {
       const int64_t item = walk_item(it0, it1, a.tiles, st);
       const int qb = (int)(item / a.tiles);
       const int t = (int)(item % a.tiles);
       if (qb != cur_qb) {
         if (cur_qb >= 0) {
-          // flush the finished segment's list (every set, even one that saw no tile)
-          const int slot = (cta - seg_first_cta) * NSETS + set;
-          const int64_t gq = (int64_t)cur_qb * BM + row;
-          uint64_t* dst = a.partial + (gq * a.smax + slot) * LIST;
-          for (int e = 0; e < CAP; ++e) {
-            if (gq < a.nq) dst[e] = mylist[e * BM];
-            mylist[e * BM] = KEY_NONE;
-          }
+          // flush the finished segment's lists (every set, even one that saw no candidate)
+          flush(cur_qb, (cta - seg_first_cta) * NSETS + set);
+          for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
         }
         cur_qb = qb;
         seg_first_cta = cta_of((int64_t)qb * a.tiles, a.work, a.grid);
@@ -579,50 +613,47 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         seed_key = (a.seed != nullptr && gq < a.nq) ? make_key(a.seed[gq], 0u) : KEY_NONE;
         thr_key = seed_key;
         thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
+        lslot = 0;
       }
       const int buf = tcount & 1;
-      if (NSETS == 2 && buf != set) continue;
       const int64_t col0 = (int64_t)t * BN;
       __syncwarp();
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) nbw[lane + 32 * i] = nbn[i];
       __syncwarp();
-      if (st + NSETS < it1 - it0) fetch_norms(st + NSETS);
+      if (st + 1 < it1 - it0) fetch_norms(st + 1);
       const uint32_t tph = (tcount >> 1) & 1;
       if (alive && !ptx::mbar_wait(&tfull_bar[buf], tph, a.err, ERR_TIMEOUT_EPI)) alive = false;
+      alive = __all_sync(FULL, alive);  // the warp leaves together
       if (!alive) break;
       ptx::tc_fence_after();
       const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
       uint32_t va[32], vb[32];
-      ptx::tmem_ld16(taddr, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
-      ptx::tmem_ld16(taddr + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
+      ptx::tmem_ld16(taddr + cbeg * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
+      ptx::tmem_ld16(taddr + cbeg * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
       ptx::tmem_ld_wait();
 #pragma unroll 1
-      for (int ch = 0; ch < BN / 32; ch += 2) {
+      for (int ch = cbeg; ch < cend; ch += 2) {
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, seed_key,
+        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, seed_key, lslot,
                   (uint32_t)(col0 + ch * 32), a.depth);
         ptx::tmem_ld_wait();
-        if (ch + 2 < BN / 32) {
+        if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
           ptx::tmem_ld16(taddr + (ch + 2) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
+        } else {
+          // every TMEM read of this tile is done: hand the buffer back before the last chunk
+          ptx::tc_fence_before();
+          ptx::mbar_arrive(&tempty_bar[buf]);
         }
-        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est, seed_key,
+        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est, seed_key, lslot,
                   (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
-      ptx::tc_fence_before();
-      ptx::mbar_arrive(&tempty_bar[buf]);
     }
-    if (alive && cur_qb >= 0) {
-      const int slot = (cta - seg_first_cta) * NSETS + set;
-      const int64_t gq = (int64_t)cur_qb * BM + row;
-      uint64_t* dst = a.partial + (gq * a.smax + slot) * LIST;
-      if (gq < a.nq)
-        for (int e = 0; e < CAP; ++e) dst[e] = mylist[e * BM];
-    }
+    if (alive && cur_qb >= 0) flush(cur_qb, (cta - seg_first_cta) * NSETS + set);
   }
 
   ptx::tc_fence_before();
