@@ -51,13 +51,12 @@ constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int BM = 128;          // queries per CTA tile (TMEM lanes)
 constexpr int BN = 256;          // points per tile (TMEM columns per accumulator)
 constexpr int BK = 64;           // BF16 elements per stage row (128 bytes, one swizzle span)
-constexpr int STAGES = 3;
+constexpr int STAGES = 4;
 constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int LIST = 32;                             // candidates kept per query row
-constexpr int TSTR = 36;                             // row stride of the per-lane row buffers (floats)
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
@@ -348,6 +347,15 @@ __device__ __forceinline__ void wl_insert(uint64_t (&Lr)[KW], uint64_t c, int la
   }
 }
 
+// a[i] for a run-time i without local memory
+template <int N>
+__device__ __forceinline__ float pick(const float (&a)[N], int i) {
+  float r = a[0];
+#pragma unroll
+  for (int u = 1; u < N; ++u) r = i == u ? a[u] : r;
+  return r;
+}
+
 // ascending bitonic sort of one key per lane across the warp
 __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 #pragma unroll
@@ -363,46 +371,41 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 }
 
 // One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
-// rows: v holds the row's 32 accumulators of the chunk, nb the chunk's point
-// norms.  The row's list lives in shared memory, entry e at mylist[e * BM],
-// unsorted; lslot is the slot of its largest entry and thr_key that entry, or
-// the row's seed key (seed est', id 0) while the list has an empty slot, and
-// thr_est that key's est'.  The common case -- no column of any row below its
-// threshold -- costs one FMA and one min per value and one vote; a lane with
-// candidates stashes its row in trow and admits them one by one: the new key
-// replaces the largest entry and the `depth` entries are rescanned for the new
-// largest (independent loads, conflict-free while the lanes run in step; a
-// sorted insert would be a chain of dependent shared-memory loads).
-__device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* __restrict__ nb,
-                                          float* __restrict__ trow, uint64_t* __restrict__ mylist,
+// rows: v holds the row's 32 accumulators of the chunk; lane j's nbv is the
+// norm of the chunk's point j (read by shuffle).  The row's list lives in
+// shared memory, entry e at mylist[e * BM], unsorted; lslot is the slot of its
+// largest entry and thr_key that entry, or the row's seed key (seed est', id 0)
+// while the list has an empty slot, and thr_est that key's est'.  The common
+// case -- no column of any row below its threshold -- costs a shuffle, an FMA
+// and a min per value and one vote; a lane with candidates admits them one by
+// one: the new key replaces the largest entry and the `depth` entries are
+// rescanned for the new largest (independent loads, conflict-free while the
+// lanes run in step; a sorted insert would be a chain of dependent
+// shared-memory loads).
+__device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, uint64_t* __restrict__ mylist,
                                           uint64_t& thr_key, float& thr_est, uint64_t seed_key,
                                           int& lslot, uint32_t col0, int depth) {
-  const float4* nb4 = reinterpret_cast<const float4*>(nb);
   float e[32];
-  float mn = __int_as_float(0x7F800000);
 #pragma unroll
-  for (int j4 = 0; j4 < 8; ++j4) {
-    const float4 n4 = nb4[j4];
-    e[4 * j4 + 0] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 0]), n4.x);
-    e[4 * j4 + 1] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 1]), n4.y);
-    e[4 * j4 + 2] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 2]), n4.z);
-    e[4 * j4 + 3] = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 3]), n4.w);
-    mn = fminf(mn, fminf(fminf(e[4 * j4 + 0], e[4 * j4 + 1]), fminf(e[4 * j4 + 2], e[4 * j4 + 3])));
-  }
+  for (int j = 0; j < 32; ++j) e[j] = __fmaf_rn(-2.0f, __uint_as_float(v[j]), __shfl_sync(FULL, nbv, j));
+  float m4[8];
+#pragma unroll
+  for (int j4 = 0; j4 < 8; ++j4)
+    m4[j4] = fminf(fminf(e[4 * j4 + 0], e[4 * j4 + 1]), fminf(e[4 * j4 + 2], e[4 * j4 + 3]));
+  const float mn = fminf(fminf(fminf(m4[0], m4[1]), fminf(m4[2], m4[3])),
+                         fminf(fminf(m4[4], m4[5]), fminf(m4[6], m4[7])));
   if (!__any_sync(FULL, mn < thr_est)) return;
   if (mn < thr_est) {
     unsigned mask = 0;
-    float4* t4 = reinterpret_cast<float4*>(trow);
 #pragma unroll
-    for (int j4 = 0; j4 < 8; ++j4) {
-      t4[j4] = make_float4(e[4 * j4 + 0], e[4 * j4 + 1], e[4 * j4 + 2], e[4 * j4 + 3]);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) mask |= (e[4 * j4 + u] < thr_est ? 1u : 0u) << (4 * j4 + u);
-    }
+    for (int j = 0; j < 32; ++j) mask |= (e[j] < thr_est ? 1u : 0u) << j;
     while (mask) {
       const int j = __ffs(mask) - 1;
       mask &= mask - 1;
-      const uint64_t c = make_key(trow[j], col0 + (uint32_t)j);
+      float val = e[0];
+#pragma unroll
+      for (int u = 1; u < 32; ++u) val = j == u ? e[u] : val;
+      const uint64_t c = make_key(val, col0 + (uint32_t)j);
       if (c < thr_key) {
         mylist[lslot * BM] = c;  // the largest entry (or an empty slot) drops out
         uint64_t m = 0;
@@ -426,9 +429,9 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], const float* 
 // Shared-memory footprint of k2_main<CAP, NSETS>.
 __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
   return 1024 /* alignment */ + (size_t)STAGES * STAGE_BYTES +
-         (size_t)nsets * BM * cap * 8 /* lists */ + (size_t)nsets * 4 * 32 * TSTR * 4 /* row buffers */ +
-         (size_t)nsets * 4 * BN * 4 /* norms */ + (2 * STAGES + 4) * 8 + 16;
+         (size_t)nsets * BM * cap * 8 /* lists */ + (2 * STAGES + 4) * 8 + 16;
 }
+static_assert(k2_smem_bytes(32, 1) <= 232448 && k2_smem_bytes(16, 2) <= 232448, "k2_main shared memory");
 
 // The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
 // ||q~||^2 is left out: it does not change the row's order).  A point is
@@ -453,9 +456,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       (reinterpret_cast<uintptr_t>(k2_smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* stage_base = smem;                                                   // STAGES * 48 KB
   uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [NSETS][CAP][BM]
-  float* trans = reinterpret_cast<float*>(lists + NSETS * BM * CAP);            // [NEPI][32][TSTR]
-  float* nbs = trans + NEPI * 32 * TSTR;                                         // [NEPI][BN]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(nbs + NEPI * BN);
+  uint64_t* bars = lists + NSETS * BM * CAP;
   uint64_t* full_bar = bars;
   uint64_t* empty_bar = bars + STAGES;
   uint64_t* tfull_bar = bars + 2 * STAGES;
@@ -556,8 +557,6 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     const int row = quad * 32 + lane; // this lane's row of the 128-query tile
     constexpr int CPS = (BN / 32) / NSETS;  // 32-column chunks per set and tile
     const int cbeg = set * CPS, cend = cbeg + CPS;
-    float* nbw = nbs + ew * BN;       // point norms of the current tile
-    float* trow = trans + (ew * 32 + lane) * TSTR;            // this lane's row buffer
     uint64_t* setlists = lists + (size_t)set * CAP * BM;      // entry e of row r at setlists[e * BM + r]
     uint64_t* mylist = setlists + row;
     const float INF = __int_as_float(0x7F800000);
@@ -585,8 +584,9 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       __syncwarp();
     };
 
-    // norms of the first tile; later tiles' norms are fetched one tile ahead
-    float nbn[BN / 32];
+    // point norms, lane j holding column 32 i + j of the tile in nbc[i]: the
+    // current tile's in nbc, the next tile's fetched into nbn one tile ahead
+    float nbn[BN / 32], nbc[BN / 32];
     auto fetch_norms = [&](int64_t st_) {
       const int64_t item_ = walk_item(it0, it1, a.tiles, st_);
       const int64_t c0 = (int64_t)(item_ % a.tiles) * BN;
@@ -617,10 +617,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       }
       const int buf = tcount & 1;
       const int64_t col0 = (int64_t)t * BN;
-      __syncwarp();
 #pragma unroll
-      for (int i = 0; i < BN / 32; ++i) nbw[lane + 32 * i] = nbn[i];
-      __syncwarp();
+      for (int i = 0; i < BN / 32; ++i) nbc[i] = nbn[i];
       if (st + 1 < it1 - it0) fetch_norms(st + 1);
       const uint32_t tph = (tcount >> 1) & 1;
       if (alive && !ptx::mbar_wait(&tfull_bar[buf], tph, a.err, ERR_TIMEOUT_EPI)) alive = false;
@@ -637,8 +635,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        epi_chunk(va, nbw + ch * 32, trow, mylist, thr_key, thr_est, seed_key, lslot,
-                  (uint32_t)(col0 + ch * 32), a.depth);
+        epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, (uint32_t)(col0 + ch * 32),
+                  a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
@@ -648,7 +646,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           ptx::tc_fence_before();
           ptx::mbar_arrive(&tempty_bar[buf]);
         }
-        epi_chunk(vb, nbw + (ch + 1) * 32, trow, mylist, thr_key, thr_est, seed_key, lslot,
+        epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot,
                   (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
