@@ -110,6 +110,26 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
                                   int32_t d, int32_t include_self, int32_t* out_ids,
                                   float* out_dists, mann_knn_report* report, void* stream);
 
+/* Device-resident point set.  The reference keeps the data matrix with the
+ * caller and passes it to every query (src/ann_index.jl:1-10); a dataset
+ * handle is the explicit device copy of such a matrix, so repeated searches
+ * over the same points copy only their queries.  The copy goes stale when the
+ * caller changes the points: re-upload after insert!
+ * (src/indices/bruteforce.jl:82-95).  A handle belongs to the device that
+ * was current at create; calls from another device fail with MANN_EINVAL_ARG. */
+typedef struct mann_dataset mann_dataset;
+/* data: host [n][d] FP32; copied to the device before the call returns. */
+mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_dataset** out);
+/* Replace the contents with n new rows of the same width (n may grow). */
+mann_status mann_dataset_upload(mann_dataset* ds, const float* data, int64_t n);
+mann_status mann_dataset_destroy(mann_dataset* ds);
+/* mann_knn / mann_knn_graph over a dataset's points: host queries and
+ * outputs, the points already on the device. */
+mann_status mann_knn_dataset(const mann_knn_params* p, const mann_dataset* ds, const float* queries,
+                             int64_t q, int32_t* out_ids, float* out_dists, mann_knn_report* report);
+mann_status mann_knn_graph_dataset(const mann_knn_params* p, const mann_dataset* ds, int32_t include_self,
+                                   int32_t* out_ids, float* out_dists, mann_knn_report* report);
+
 /* kNN graphs of nsets independent point sets stored back to back: set c is
  * rows [set_offsets[c], set_offsets[c+1]) of data (set_offsets[0] = 0, host
  * array of nsets+1).  Replaces a loop of build_knn_graph calls, one per set

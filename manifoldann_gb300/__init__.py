@@ -20,11 +20,11 @@ from .geometry import (CurvatureFreeSymmetric, EuclideanChord, PCAGeometry, PCAM
                        intrinsic_dimension, local_distance, project, reconstruct)
 from .ivf import IVFFlatIndex, TopKRouting, ivf_search_device, select_indices
 from .probe import LearnedProbeRouting, ProbeModel, ivf_search_learned, neighbour_list_labels
-from .indices import (AbstractANNIndex, BruteForceIndex, Neighbor, build_index, configured_k,
+from .indices import (AbstractANNIndex, BruteForceIndex, DeviceDataset, Neighbor, build_index, configured_k,
                       index_distance, insert, knn_arrays, neighbor_ids, query, supports_mutation)
 
 __all__ = [
-    "ArgumentError", "DimensionMismatch", "MannError",
+    "ArgumentError", "DimensionMismatch", "MannError", "DeviceDataset",
     "CosineDist", "Euclidean", "SqEuclidean", "cosine_distance", "default_distance",
     "default_squared_distance", "euclidean_distance",
     "recall_at_k",

@@ -136,6 +136,11 @@ SIGNATURES = {
     "mann_knn_graph": (_I32, [C.POINTER(KnnParams), _P, _I64, _I32, _I32, _P, _P, C.POINTER(KnnReport)]),
     "mann_knn_graph_device": (_I32, [C.POINTER(KnnParams), _P, _I64, _I32, _I32, _P, _P,
                                      C.POINTER(KnnReport), _P]),
+    "mann_dataset_create": (_I32, [_P, _I64, _I32, C.POINTER(_P)]),
+    "mann_dataset_upload": (_I32, [_P, _P, _I64]),
+    "mann_dataset_destroy": (_I32, [_P]),
+    "mann_knn_dataset": (_I32, [C.POINTER(KnnParams), _P, _P, _I64, _P, _P, C.POINTER(KnnReport)]),
+    "mann_knn_graph_dataset": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _P, C.POINTER(KnnReport)]),
     "mann_knn_device_noalloc": (_I32, [C.POINTER(KnnParams), _P, _I64, _P, _I64, _I32, _P, _P, _P]),
     "mann_pairwise_distances": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P]),
     "mann_kmeans_assign": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P, _P]),

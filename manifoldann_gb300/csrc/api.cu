@@ -1,4 +1,5 @@
 // api.cu -- extern "C" entry points of libmanngpu (declared in include/mann.h).
+#include <new>
 #include <string>
 
 #include "kernels.cuh"
@@ -177,6 +178,31 @@ mann_status graph_impl(const mann_knn_params* p, const float* data, int64_t n, i
   return MANN_OK;
 }
 
+// the points of a dataset handle are device memory; queries and outputs are host
+mann_status knn_dataset_impl(const mann_knn_params* p, const float* dbase, int64_t n, const float* qs,
+                             int64_t q, int32_t d, int64_t graph_self, int kreq, int32_t* ids, float* dists,
+                             mann_knn_report* rep) {
+  const int kout = p->k;
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  cudaStream_t s = ctx->stream;
+  CallScope scope(ctx, s);
+  const int64_t rows = qs ? q : n;
+  float *dq = nullptr, *dd = nullptr;
+  int32_t* di = nullptr;
+  if (qs) {
+    MANN_TRY(ctx->scratch_t(SLOT_QUERIES, (size_t)q * d, &dq));
+    MANN_CUDA_TRY(cudaMemcpyAsync(dq, qs, sizeof(float) * q * d, cudaMemcpyHostToDevice, s));
+  }
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_IDS, (size_t)rows * kout, &di));
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_DISTS, (size_t)rows * kout, &dd));
+  MANN_TRY(search_device(ctx, s, p, dbase, n, qs ? dq : dbase, rows, d, graph_self, kreq, kout, di, dd, rep));
+  MANN_CUDA_TRY(cudaMemcpyAsync(ids, di, sizeof(int32_t) * rows * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaMemcpyAsync(dists, dd, sizeof(float) * rows * kout, cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  return MANN_OK;
+}
+
 }  // namespace
 
 mann_status exact_search_device(Context* ctx, cudaStream_t s, const mann_knn_params* p,
@@ -222,6 +248,128 @@ mann_status mann_host_unregister(void* ptr) {
   if (!ptr) return fail(MANN_EINVAL_ARG, "bad buffer");
   MANN_CUDA_TRY(cudaHostUnregister(ptr));
   return MANN_OK;
+}
+
+}  // extern "C"
+
+struct mann_dataset {
+  float* dev = nullptr;
+  int64_t n = 0, cap = 0;
+  int32_t d = 0;
+  int device = -1;
+};
+
+namespace {
+
+mann_status dataset_device_check(const mann_dataset* ds) {
+  int dev = -1;
+  MANN_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != ds->device) return fail(MANN_EINVAL_ARG, "dataset belongs to another device");
+  return MANN_OK;
+}
+
+mann_status dataset_copy_in(mann_dataset* ds, const float* data, int64_t n) {
+  Context* ctx = nullptr;
+  MANN_TRY(get_context(&ctx));
+  if (n > ds->cap) {
+    if (ds->dev) MANN_CUDA_TRY(cudaFree(ds->dev));
+    ds->dev = nullptr;
+    ds->cap = 0;
+    if (cudaMalloc(&ds->dev, sizeof(float) * (size_t)n * ds->d) != cudaSuccess) {
+      (void)cudaGetLastError();
+      ds->dev = nullptr;
+      return fail(MANN_ENOMEM, "dataset: device allocation failed");
+    }
+    ds->cap = n;
+  }
+  CallScope scope(ctx, ctx->stream);
+  MANN_CUDA_TRY(cudaMemcpyAsync(ds->dev, data, sizeof(float) * (size_t)n * ds->d, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  MANN_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ds->n = n;
+  return MANN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_dataset** out) {
+  clear_error();
+  if (!out) return fail(MANN_EINVAL_ARG, "out must not be NULL");
+  *out = nullptr;
+  if (n <= 0 || d <= 0) return fail(MANN_EINVAL_ARG, "a dataset needs n > 0 points of d > 0 values");
+  if (!data) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  auto* ds = new (std::nothrow) mann_dataset();
+  if (!ds) return fail(MANN_ENOMEM, "dataset: host allocation failed");
+  ds->d = d;
+  if (cudaGetDevice(&ds->device) != cudaSuccess) {
+    (void)cudaGetLastError();
+    delete ds;
+    return fail(MANN_ECUDA, "no CUDA device");
+  }
+  const mann_status st = dataset_copy_in(ds, data, n);
+  if (st != MANN_OK) {
+    if (ds->dev) (void)cudaFree(ds->dev);
+    delete ds;
+    return st;
+  }
+  *out = ds;
+  return MANN_OK;
+}
+
+mann_status mann_dataset_upload(mann_dataset* ds, const float* data, int64_t n) {
+  clear_error();
+  if (!ds || !data) return fail(MANN_EINVAL_ARG, "NULL argument");
+  if (n <= 0) return fail(MANN_EINVAL_ARG, "a dataset needs n > 0 points");
+  MANN_TRY(dataset_device_check(ds));
+  return dataset_copy_in(ds, data, n);
+}
+
+mann_status mann_dataset_destroy(mann_dataset* ds) {
+  clear_error();
+  if (!ds) return MANN_OK;
+  if (ds->dev) {
+    int prev = -1;
+    (void)cudaGetDevice(&prev);
+    if (prev != ds->device) (void)cudaSetDevice(ds->device);
+    (void)cudaFree(ds->dev);
+    if (prev >= 0 && prev != ds->device) (void)cudaSetDevice(prev);
+  }
+  delete ds;
+  return MANN_OK;
+}
+
+mann_status mann_knn_dataset(const mann_knn_params* p, const mann_dataset* ds, const float* queries,
+                             int64_t q, int32_t* out_ids, float* out_dists, mann_knn_report* report) {
+  clear_error();
+  if (!ds) return fail(MANN_EINVAL_ARG, "NULL dataset");
+  MANN_TRY(check_common(p, ds->n, ds->d));
+  if (q < 0) return fail(MANN_EINVAL_ARG, "negative query count");
+  if (report) *report = mann_knn_report{};
+  if (p->k <= 0 || q == 0) return MANN_OK;
+  if (!queries || !out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  MANN_TRY(dataset_device_check(ds));
+  const int kreq = (int)std::min<int64_t>(p->k, ds->n);
+  return knn_dataset_impl(p, ds->dev, ds->n, queries, q, ds->d, -1, kreq, out_ids, out_dists, report);
+}
+
+mann_status mann_knn_graph_dataset(const mann_knn_params* p, const mann_dataset* ds, int32_t include_self,
+                                   int32_t* out_ids, float* out_dists, mann_knn_report* report) {
+  clear_error();
+  if (!ds) return fail(MANN_EINVAL_ARG, "NULL dataset");
+  MANN_TRY(check_common(p, ds->n, ds->d));
+  if (report) *report = mann_knn_report{};
+  const int64_t n = ds->n;
+  const int64_t max_neighbors = n - (include_self ? 0 : 1);
+  if (!(p->k > 0 && p->k <= max_neighbors))
+    return fail(MANN_EINVAL_ARG, "k must satisfy 0 < k <= " + std::to_string(max_neighbors) +
+                                     " for dataset with " + std::to_string(n) + " points");
+  if (!out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
+  MANN_TRY(dataset_device_check(ds));
+  const int kreq = p->k + (include_self ? 0 : 1);
+  return knn_dataset_impl(p, ds->dev, n, nullptr, n, ds->d, include_self ? -1 : 0, kreq, out_ids, out_dists,
+                          report);
 }
 
 mann_status mann_knn(const mann_knn_params* p, const float* base, int64_t n, const float* queries,

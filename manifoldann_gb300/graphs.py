@@ -15,7 +15,7 @@ import numpy as np
 from . import _lib
 from ._lib import ArgumentError
 from .distances import metric_code
-from .indices import PRECISIONS, BruteForceIndex, _validate, configured_k, points_view
+from .indices import PRECISIONS, BruteForceIndex, DeviceDataset, _validate, configured_k, points_view
 
 
 @dataclass
@@ -74,20 +74,26 @@ def _create_graph_metadata(original_k, directed, node_metadata, n_points):
 def knn_graph_arrays(index: BruteForceIndex, data, k: int, *, include_self: bool = False,
                      precision: str = "fp32", fp64_ties: bool = False, margin: int = 0,
                      report: bool = False):
-    """Self-kNN graph on the GPU: (ids [n, k] 0-based int32, dists [n, k])."""
-    a = np.asarray(data)
-    n = a.shape[1]
+    """Self-kNN graph on the GPU: (ids [n, k] 0-based int32, dists [n, k]);
+    ``data`` is the d x n matrix or a DeviceDataset of it."""
+    ds = data if isinstance(data, DeviceDataset) else None
+    a = None if ds is not None else np.asarray(data)
+    n = ds.n if ds is not None else a.shape[1]
     max_neighbors = n - (0 if include_self else 1)
     if not (0 < k <= max_neighbors):
         raise ArgumentError(f"k must satisfy 0 < k <= {max_neighbors} for dataset with {n} points")
-    pts = points_view(a)
     ids = np.empty((n, k), np.int32)
     dists = np.empty((n, k), np.float32)
     p = _lib.params(metric_code(index.distance), k, PRECISIONS[precision], margin,
                     _lib.FLAG_FP64_TIES if fp64_ties else 0)
     rep = _lib.KnnReport()
-    _lib.check(_lib.load().mann_knn_graph(p, pts.ctypes.data, n, a.shape[0], int(bool(include_self)),
-                                          ids.ctypes.data, dists.ctypes.data, rep))
+    if ds is not None:
+        _lib.check(_lib.load().mann_knn_graph_dataset(p, ds.handle, int(bool(include_self)), ids.ctypes.data,
+                                                      dists.ctypes.data, rep))
+    else:
+        pts = points_view(a)
+        _lib.check(_lib.load().mann_knn_graph(p, pts.ctypes.data, n, a.shape[0], int(bool(include_self)),
+                                              ids.ctypes.data, dists.ctypes.data, rep))
     if report:
         return ids, dists, rep.as_dict()
     return ids, dists

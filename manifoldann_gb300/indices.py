@@ -8,6 +8,7 @@ Float32 (other element types are converted).
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass
 from typing import Iterable, NamedTuple
 
@@ -98,6 +99,14 @@ def insert(index: BruteForceIndex, points) -> BruteForceIndex:
     return index
 
 
+class _ShapeOnly:
+    """Stands in for a matrix of the given shape in the argument checks."""
+
+    def __init__(self, shape):
+        self.shape = tuple(shape)
+        self.ndim = len(self.shape)
+
+
 def _validate(index: BruteForceIndex, data: np.ndarray, qlen: int) -> None:
     """``validate_index_dimensions`` (src/utils/validation.jl:8-18)."""
     if data.shape[0] != index.dimension:
@@ -108,13 +117,55 @@ def _validate(index: BruteForceIndex, data: np.ndarray, qlen: int) -> None:
         raise ArgumentError(f"Data contains {data.shape[1]} points but index tracks {index.n_points}")
 
 
+class DeviceDataset:
+    """Device copy of a d x N point matrix (an owned ``mann_dataset*``).
+
+    Searches given a DeviceDataset in place of the data matrix copy only
+    their queries.  The copy does not follow later changes of the host
+    matrix: call ``upload`` after ``insert`` (src/indices/bruteforce.jl:82-95)
+    or any other change of the points."""
+
+    def __init__(self, data):
+        pts = points_view(np.asarray(data))
+        self.n, self.d = int(pts.shape[0]), int(pts.shape[1])
+        h = C.c_void_p()
+        _lib.check(_lib.load().mann_dataset_create(pts.ctypes.data, self.n, self.d, C.byref(h)))
+        self.handle = h
+
+    @property
+    def shape(self):
+        """(d, N), the shape of the matrix it copies."""
+        return (self.d, self.n)
+
+    def upload(self, data) -> None:
+        pts = points_view(np.asarray(data))
+        if pts.shape[1] != self.d:
+            raise DimensionMismatch(f"Expected points of dimension {self.d}, got {pts.shape[1]}")
+        _lib.check(_lib.load().mann_dataset_upload(self.handle, pts.ctypes.data, int(pts.shape[0])))
+        self.n = int(pts.shape[0])
+
+    def close(self) -> None:
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            _lib.load().mann_dataset_destroy(h)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def knn_arrays(index: BruteForceIndex, data, queries, k: int, *, precision: str = "fp32",
                fp64_ties: bool = False, margin: int = 0, report: bool = False, fp64_error: bool = False):
     """Batch exact kNN on the GPU; returns (ids [q, min(k,n)] 0-based int32,
-    dists [q, min(k,n)] float32[, report dict]).  ``queries`` is d x q.
+    dists [q, min(k,n)] float32[, report dict]).  ``queries`` is d x q;
+    ``data`` the d x N matrix or a DeviceDataset of it.
     With ``fp64_error`` the report's ``max_abs_err_fp64`` holds the largest
     |returned distance - FP64 distance| over all returned neighbours."""
-    a = np.asarray(data)
+    ds = data if isinstance(data, DeviceDataset) else None
+    a = _ShapeOnly(ds.shape) if ds is not None else np.asarray(data)
     Q = np.asarray(queries)
     if Q.ndim == 1:
         Q = Q.reshape(-1, 1)
@@ -127,7 +178,6 @@ def knn_arrays(index: BruteForceIndex, data, queries, k: int, *, precision: str 
     if keff <= 0 or nq == 0:
         e = (np.empty((nq, 0), np.int32), np.empty((nq, 0), np.float32))
         return e + ({},) if report else e
-    base = points_view(a)
     qs = points_view(Q)
     ids = np.empty((nq, keff), np.int32)
     dists = np.empty((nq, keff), np.float32)
@@ -135,8 +185,13 @@ def knn_arrays(index: BruteForceIndex, data, queries, k: int, *, precision: str 
     p = _lib.params(metric_code(index.distance), keff, PRECISIONS[precision], margin, flags)
     rep = _lib.KnnReport()
     lib = _lib.load()
-    _lib.check(lib.mann_knn(p, base.ctypes.data, n, qs.ctypes.data, nq, a.shape[0], ids.ctypes.data,
-                            dists.ctypes.data, rep))
+    if ds is not None:
+        _lib.check(lib.mann_knn_dataset(p, ds.handle, qs.ctypes.data, nq, ids.ctypes.data, dists.ctypes.data,
+                                        rep))
+    else:
+        base = points_view(a)
+        _lib.check(lib.mann_knn(p, base.ctypes.data, n, qs.ctypes.data, nq, a.shape[0], ids.ctypes.data,
+                                dists.ctypes.data, rep))
     if report:
         return ids, dists, rep.as_dict()
     return ids, dists
