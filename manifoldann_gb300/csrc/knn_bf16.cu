@@ -729,7 +729,12 @@ struct RerankArgs {
   const float* cos_bn;  // [n]  squared norms of the original points
   float eps_c;          // |FP32 cosine - ||q^ - p^||^2 / 2| bound (rounded up)
   int kdim;             // columns of the tensor-core dot (dp, or 3 dp in the split form)
+  int coop;             // d % 4 == 0 and 16-byte aligned rows: warp-cooperative row loads
 };
+
+constexpr int RR_WARPS = 2;   // warps (queries) per rerank block
+constexpr int RR_CH = 64;     // dimensions per staged chunk
+constexpr int RR_STR = 68;    // staged row stride (floats): 16-byte aligned rows
 
 // sequential difference-form sum over dimensions 0..d-1 (the FP32 form's order)
 __device__ __forceinline__ float fp32_dist_row(const float* __restrict__ x,
@@ -860,16 +865,85 @@ __global__ void k2_rerank(RerankArgs a) {
   // candidates: entries with est <= T (the list is sorted by est)
   uint64_t key[2] = {KEY_NONE, KEY_NONE};
   int ncand = 0;
+  if (a.coop && a.L == 32) {
+    // The warp streams its candidates' rows through shared memory in chunks
+    // of RR_CH dimensions (cp.async, 16 bytes a lane, two chunks in flight);
+    // lane i then adds candidate i's chunk to its sequential FP32 sum, in the
+    // same order as the one-lane-per-row form.
+    __shared__ __align__(16) float rr_rows[RR_WARPS][2][32 * RR_STR];
+    __shared__ __align__(16) float rr_q[RR_WARPS][2][RR_CH];
+    __shared__ int rr_id[RR_WARPS][32];
+    const int w = threadIdx.x >> 5;
+    const uint64_t k0 = lst[lane];
+    const bool isc = k0 != KEY_NONE && __fadd_rd(key_dist(k0), qn) <= T;
+    const unsigned cm = __ballot_sync(FULL, isc);
+    const int nc = __popc(cm);
+    if (isc) rr_id[w][__popc(cm & ((1u << lane) - 1u))] = key_id(k0);
+    __syncwarp();
+    const int nch = (a.d + RR_CH - 1) / RR_CH;
+    auto issue = [&](int chunk, int b) {
+      const int c0 = chunk * RR_CH;
+      const int cw = min(RR_CH, a.d - c0);
+      const int c4 = lane & 15;
+      if (c4 * 4 < cw) {
+        for (int r = lane >> 4; r < nc; r += 2)
+          ptx::cp_async16(&rr_rows[w][b][r * RR_STR + c4 * 4], a.base + (int64_t)rr_id[w][r] * a.d + c0 + c4 * 4);
+        if (lane < 16) ptx::cp_async16(&rr_q[w][b][c4 * 4], qrow + c0 + c4 * 4);
+      }
+      ptx::cp_async_commit();
+    };
+    float acc = 0.0f;
+    issue(0, 0);
+    for (int chunk = 0; chunk < nch; ++chunk) {
+      const int b = chunk & 1;
+      if (chunk + 1 < nch) {
+        issue(chunk + 1, b ^ 1);
+        ptx::cp_async_wait<1>();
+      } else {
+        ptx::cp_async_wait<0>();
+      }
+      __syncwarp();
+      if (lane < nc) {
+        const float* row = &rr_rows[w][b][lane * RR_STR];
+        const float* qq = rr_q[w][b];
+        const int cw = min(RR_CH, a.d - chunk * RR_CH);
+        if (cosine) {
+#pragma unroll 8
+          for (int c = 0; c < cw; ++c) acc = __fmaf_rn(qq[c], row[c], acc);
+        } else {
+#pragma unroll 8
+          for (int c = 0; c < cw; ++c) {
+            const float t = __fsub_rn(qq[c], row[c]);
+            acc = __fmaf_rn(t, t, acc);
+          }
+        }
+      }
+      __syncwarp();  // the buffer is refilled two chunks on
+    }
+    if (lane < nc) {
+      const int id = rr_id[w][lane];
+      float dist;
+      if (cosine) {
+        const float den = __fmul_rn(__fsqrt_rn(a.cos_qn[q]), __fsqrt_rn(a.cos_bn[id]));
+        dist = __fsub_rn(1.0f, __fdiv_rn(acc, den));
+        if (dist < 0.0f) dist = 0.0f;
+      } else {
+        dist = a.metric == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc) : acc;
+      }
+      key[0] = make_key(dist, (uint32_t)id);
+    }
+  } else {
 #pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    const int e = s * 32 + lane;
-    if (e < a.L) {
-      const uint64_t k = lst[e];
-      if (k != KEY_NONE && __fadd_rd(key_dist(k), qn) <= T) {
-        const int id = key_id(k);
-        const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
-                                  : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
-        key[s] = make_key(dist, (uint32_t)id);
+    for (int s = 0; s < 2; ++s) {
+      const int e = s * 32 + lane;
+      if (e < a.L) {
+        const uint64_t k = lst[e];
+        if (k != KEY_NONE && __fadd_rd(key_dist(k), qn) <= T) {
+          const int id = key_id(k);
+          const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
+                                    : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
+          key[s] = make_key(dist, (uint32_t)id);
+        }
       }
     }
   }
@@ -1450,7 +1524,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     const double gd = (double)d * u / (1.0 - (double)d * u);
     ra.eps_c = std::nextafter((float)(1.25 * (4.0 * gd + 16.0 * u)), 1.0f);
   }
-  k2_rerank<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(ra);
+  ra.coop = (d % 4 == 0 && ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(qs)) & 15) == 0) ? 1 : 0;
+  k2_rerank<<<(unsigned)ceil_div(nq, RR_WARPS), 32 * RR_WARPS, 0, s>>>(ra);
   MANN_CHECK_LAUNCH();
 
   // ---- exact FP32 scan of uncertified rows (count known only on the device:
