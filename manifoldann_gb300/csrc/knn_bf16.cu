@@ -777,10 +777,11 @@ __device__ __forceinline__ float fp32_cos_row(const float* __restrict__ x, const
   return v;
 }
 
-__global__ void k2_rerank(RerankArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (q >= a.nq) return;
+// One query row (one warp): certify, then rerank the candidates.  The row's
+// certificate depth goes to the warp's histogram hist_w and its candidate
+// count to cand_sum (lane 0), flushed to global memory once per warp.
+__device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int lane, int* hist_w,
+                                           unsigned long long& cand_sum) {
   const uint64_t* lst = a.lists + q * a.L;
   const uint64_t ek_key = lst[a.kreq - 1];
   const uint64_t last_key = lst[a.depth - 1];
@@ -850,7 +851,7 @@ __global__ void k2_rerank(RerankArgs a) {
     // depth this row's certificate needs: one past its last est <= T entry
     const uint64_t kl = lst[lane];
     const int le = __popc(__ballot_sync(FULL, kl != KEY_NONE && __fadd_rd(key_dist(kl), qn) <= T));
-    if (lane == 0) atomicAdd(&a.depth_hist[certified ? min(le + 1, LIST) : LIST + 1], 1ull);
+    if (lane == 0) ++hist_w[certified ? min(le + 1, LIST) : LIST + 1];
   }
   if (!certified) {
     if (lane == 0) {
@@ -984,8 +985,24 @@ __global__ void k2_rerank(RerankArgs a) {
     float fl = d_floor;
     if (a.metric == MANN_METRIC_EUCLIDEAN) fl = __fmul_rd(__fsqrt_rd(fmaxf(d_floor, 0.0f)), 1.0f - 1e-6f);
     a.floor_val[q] = fl;
-    atomicAdd(a.cand_total, (unsigned long long)ncand);
+    cand_sum += (unsigned long long)ncand;
   }
+}
+
+// Warps stride over the query rows; per-warp histogram and candidate count
+// reach global memory with one set of atomics per warp, not per row.
+__global__ void __launch_bounds__(32 * RR_WARPS) k2_rerank(RerankArgs a) {
+  __shared__ int hist[RR_WARPS][LIST + 2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = lane; i < LIST + 2; i += 32) hist[w][i] = 0;
+  __syncwarp();
+  unsigned long long csum = 0;
+  const int64_t nw = (int64_t)gridDim.x * RR_WARPS;
+  for (int64_t q = (int64_t)blockIdx.x * RR_WARPS + w; q < a.nq; q += nw) rerank_row(a, q, lane, hist[w], csum);
+  __syncwarp();
+  for (int i = lane; i < LIST + 2; i += 32)
+    if (hist[w][i]) atomicAdd(&a.depth_hist[i], (unsigned long long)hist[w][i]);
+  if (lane == 0 && csum) atomicAdd(a.cand_total, csum);
 }
 
 // rows re-run by the FP32 scan: copy their sorted keys into the candidate table
@@ -1525,7 +1542,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     ra.eps_c = std::nextafter((float)(1.25 * (4.0 * gd + 16.0 * u)), 1.0f);
   }
   ra.coop = (d % 4 == 0 && ((reinterpret_cast<uintptr_t>(base) | reinterpret_cast<uintptr_t>(qs)) & 15) == 0) ? 1 : 0;
-  k2_rerank<<<(unsigned)ceil_div(nq, RR_WARPS), 32 * RR_WARPS, 0, s>>>(ra);
+  k2_rerank<<<(unsigned)std::min<int64_t>(ceil_div(nq, RR_WARPS), (int64_t)ctx->num_sms * 6), 32 * RR_WARPS, 0,
+              s>>>(ra);
   MANN_CHECK_LAUNCH();
 
   // ---- exact FP32 scan of uncertified rows (count known only on the device:

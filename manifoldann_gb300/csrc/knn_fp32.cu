@@ -488,7 +488,7 @@ __global__ void merge_lists_kernel(const uint64_t* __restrict__ partial, int64_t
   const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (q >= nq) return;
   const uint64_t* src = partial + q * (int64_t)nsplit * k;
-  constexpr int MAXL = 4;  // lists per lane (nsplit <= 128)
+  constexpr int MAXL = 8;  // lists per lane (nsplit <= 256)
   int head[MAXL];
   uint64_t cur[MAXL];
 #pragma unroll
@@ -653,7 +653,7 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
     return fail(MANN_EINVAL_ARG, "cosine search needs row norms");
   if (nq <= FEW_Q && kk <= 64) {
     // a handful of rows: one point per thread across the whole GPU
-    const int grid = (int)std::min<int64_t>(128, ceil_div(n, FEW_T));
+    const int grid = (int)std::min<int64_t>(256, ceil_div(n, FEW_T));  // one pass for n <= 65536
     uint64_t* partial = nullptr;
     MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * grid * kk, &partial));
     const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
