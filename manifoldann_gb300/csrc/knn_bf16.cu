@@ -58,6 +58,7 @@ constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
 constexpr int NUM_EPI_WARPS = 4;
 constexpr int LIST = 32;                             // candidates kept per query row
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
+constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
 
@@ -291,6 +292,7 @@ struct MainArgs {
   const float* seed;  // per query: admit only est' below this (NULL = no seed)
   uint64_t* partial;  // [nq][smax][L]
   int* err;
+  int seedmode;       // keep the SEED_DEPTH smallest 32-column chunk minima instead of points
 };
 
 // a * b / c for non-negative operands, without 128-bit division (a software
@@ -421,6 +423,38 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, ui
         lslot = ms;
         thr_key = m == KEY_NONE ? seed_key : m;
         thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
+      }
+    }
+  }
+}
+
+// Seed-pass form of epi_chunk: the row keeps, in registers and sorted, the
+// SEED_DEPTH smallest minima of its 32-column chunks (keyed by the chunk's
+// first column, so each comes from a distinct point).  SEED_DEPTH distinct
+// points lie at or below the SEED_DEPTH-th of them, so it bounds the row's
+// SEED_DEPTH-th smallest est' over the sample from above -- all a seed needs.
+__device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, uint64_t (&top)[SEED_DEPTH],
+                                           uint32_t col0) {
+  float m4[8];
+#pragma unroll
+  for (int j4 = 0; j4 < 8; ++j4) {
+    float e0 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 0]), __shfl_sync(FULL, nbv, 4 * j4 + 0));
+    float e1 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 1]), __shfl_sync(FULL, nbv, 4 * j4 + 1));
+    float e2 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 2]), __shfl_sync(FULL, nbv, 4 * j4 + 2));
+    float e3 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 3]), __shfl_sync(FULL, nbv, 4 * j4 + 3));
+    m4[j4] = fminf(fminf(e0, e1), fminf(e2, e3));
+  }
+  const float mn = fminf(fminf(fminf(m4[0], m4[1]), fminf(m4[2], m4[3])),
+                         fminf(fminf(m4[4], m4[5]), fminf(m4[6], m4[7])));
+  uint64_t c = make_key(mn, col0);
+  if (c < top[SEED_DEPTH - 1]) {
+    top[SEED_DEPTH - 1] = c;
+#pragma unroll
+    for (int i = SEED_DEPTH - 1; i > 0; --i) {
+      const uint64_t lo = top[i - 1], hi = top[i];
+      if (hi < lo) {
+        top[i - 1] = hi;
+        top[i] = lo;
       }
     }
   }
@@ -564,6 +598,9 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
     int lslot = 0;
+    uint64_t top[SEED_DEPTH];
+#pragma unroll
+    for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
     int tcount = 0;
     int cur_qb = -1;
     int seg_first_cta = 0;
@@ -573,6 +610,17 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 
     // write the warp's 32 row lists of a finished segment, each sorted across the lanes
     auto flush = [&](int qb_, int slot_) {
+      if (a.seedmode) {
+        const int64_t gq = (int64_t)qb_ * BM + row;
+        if (gq < a.nq) {
+          uint64_t* dst = a.partial + (gq * a.smax + slot_) * LIST;
+#pragma unroll
+          for (int i = 0; i < SEED_DEPTH; ++i) dst[i] = top[i];
+        }
+#pragma unroll
+        for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
+        return;
+      }
       __syncwarp();
       const uint64_t* wl = setlists + quad * 32;
       for (int r = 0; r < 32; ++r) {
@@ -635,8 +683,11 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, (uint32_t)(col0 + ch * 32),
-                  a.depth);
+        if (a.seedmode)
+          seed_chunk(va, pick(nbc, ch), top, (uint32_t)(col0 + ch * 32));
+        else
+          epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, (uint32_t)(col0 + ch * 32),
+                    a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
@@ -646,8 +697,11 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           ptx::tc_fence_before();
           ptx::mbar_arrive(&tempty_bar[buf]);
         }
-        epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot,
-                  (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+        if (a.seedmode)
+          seed_chunk(vb, pick(nbc, ch + 1), top, (uint32_t)(col0 + (ch + 1) * 32));
+        else
+          epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot,
+                    (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
     }
@@ -1290,7 +1344,7 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
                           const CUtensorMap& mapB, const RowInfo* qinfo, const RowInfo* binfo,
                           const float* bnorm, int64_t bstride, int64_t n, int64_t nq, int d, int dp, int depth,
                           const float* seed, int* err, int slot_partial, int slot_lists, bool timed,
-                          uint64_t** lists_out) {
+                          uint64_t** lists_out, int seedmode = 0) {
   const int64_t qblocks = ceil_div(nq, BM);
   const int tiles = (int)ceil_div(n, BN);
   const int64_t work = qblocks * tiles;
@@ -1326,6 +1380,7 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.seed = seed;
   ma.partial = partial;
   ma.err = err;
+  ma.seedmode = seedmode;
   const size_t smem = nsets == 2 ? k2_smem_bytes(16, 2) : k2_smem_bytes(32, 1);
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
   if (nsets == 2) {
@@ -1478,20 +1533,22 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   CUtensorMap mapA;
   MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM));
 
-  // ---- seed pass: the 5th smallest est' of each query over an evenly spaced
-  // sample of SEED_SAMPLE points becomes its admission seed in the main pass
-  // (roughly its 5n/SEED_SAMPLE-th neighbour), which spares most insertions.
-  // A seed below the row's k-th estimate leaves the row uncertified.
+  // ---- seed pass: over an evenly spaced sample of SEED_SAMPLE points, the
+  // SEED_DEPTH-th smallest 32-column chunk minimum of each query (an upper
+  // bound of its SEED_DEPTH-th smallest est' there, roughly its
+  // 5n/SEED_SAMPLE-th neighbour) becomes its admission seed in the main pass,
+  // which spares most insertions.  A seed below the row's k-th estimate
+  // leaves the row uncertified.
   float* seed = nullptr;
   if (n >= 16 * SEED_SAMPLE) {
     const int64_t bstride = n / SEED_SAMPLE;
     CUtensorMap mapS;
     MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dpe, BN, bstride));
     uint64_t* slists = nullptr;
-    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dpe, 5,
-                           nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists));
+    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dpe,
+                           SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
-    seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, 4, seed);
+    seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, SEED_DEPTH - 1, seed);
     MANN_CHECK_LAUNCH();
   }
 
