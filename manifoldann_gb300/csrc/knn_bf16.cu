@@ -55,7 +55,7 @@ constexpr int STAGES = 4;
 constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
 constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
-constexpr int NUM_EPI_WARPS = 4;
+
 constexpr int LIST = 32;                             // candidates kept per query row
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
@@ -959,16 +959,31 @@ __device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int l
       }
       __syncwarp();
       if (lane < nc) {
-        const float* row = &rr_rows[w][b][lane * RR_STR];
-        const float* qq = rr_q[w][b];
-        const int cw = min(RR_CH, a.d - chunk * RR_CH);
+        // float4 reads: a quarter-warp's rows start 272 bytes apart, so its
+        // 16-byte reads fall in distinct banks; the query chunk is a broadcast
+        const float4* row = reinterpret_cast<const float4*>(&rr_rows[w][b][lane * RR_STR]);
+        const float4* qq = reinterpret_cast<const float4*>(rr_q[w][b]);
+        const int cw4 = min(RR_CH, a.d - chunk * RR_CH) >> 2;  // d % 4 == 0 here
         if (cosine) {
-#pragma unroll 8
-          for (int c = 0; c < cw; ++c) acc = __fmaf_rn(qq[c], row[c], acc);
+#pragma unroll 4
+          for (int c = 0; c < cw4; ++c) {
+            const float4 x = qq[c], y = row[c];
+            acc = __fmaf_rn(x.x, y.x, acc);
+            acc = __fmaf_rn(x.y, y.y, acc);
+            acc = __fmaf_rn(x.z, y.z, acc);
+            acc = __fmaf_rn(x.w, y.w, acc);
+          }
         } else {
-#pragma unroll 8
-          for (int c = 0; c < cw; ++c) {
-            const float t = __fsub_rn(qq[c], row[c]);
+#pragma unroll 4
+          for (int c = 0; c < cw4; ++c) {
+            const float4 x = qq[c], y = row[c];
+            float t = __fsub_rn(x.x, y.x);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(x.y, y.y);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(x.z, y.z);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(x.w, y.w);
             acc = __fmaf_rn(t, t, acc);
           }
         }
