@@ -259,14 +259,23 @@ __device__ __forceinline__ void k1_body(const float* __restrict__ base, int64_t 
       const int row = warp * RPW + r;
       const float* drow = Dt + row * BSTR;
       uint64_t thr = list_get<KW>(L[r], k - 1);
+      // keys are built only for distances at or below the threshold's (the
+      // exact key order decides); a list that is not full, or whose threshold
+      // is NaN, takes every key through the exact comparison
+      const float thr_f = thr == KEY_NONE ? 0.0f : key_dist(thr);
+      const bool exact = thr == KEY_NONE || !(thr_f == thr_f);
       uint64_t key[4];
       unsigned pend = 0;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int col = lane + 32 * j;
         const int64_t gid = t0 + col;
-        key[j] = (gid < tend) ? make_key(drow[col], (uint32_t)gid) : KEY_NONE;
-        if (key[j] < thr) pend |= 1u << j;
+        const float dv = drow[col];
+        key[j] = KEY_NONE;
+        if (gid < tend && (exact || dv <= thr_f)) {
+          key[j] = make_key(dv, (uint32_t)gid);
+          if (key[j] < thr) pend |= 1u << j;
+        }
       }
       for (;;) {
         const unsigned any = __ballot_sync(FULL, pend != 0);
@@ -325,7 +334,7 @@ __global__ void __launch_bounds__(K1_THREADS, 1)
 // against that set's points [nb0, nb1) (global rows, so the keys carry global
 // ids), writing split slot `split` of each query's lists.
 template <int METRIC, int BQ, bool VEC>
-__global__ void __launch_bounds__(K1_THREADS, 1)
+__global__ void __launch_bounds__(K1_THREADS, 2)
     k1_segmented(const float* __restrict__ data, const SegItem* __restrict__ items, int d, int k, int nsplit,
                  uint64_t* __restrict__ partial) {
   extern __shared__ float4 k1_smem[];
