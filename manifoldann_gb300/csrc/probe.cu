@@ -642,9 +642,11 @@ __global__ void __launch_bounds__(ROUTE_THREADS)
 }
 
 // Warp per query for small nprobe: every lane keeps the NP best keys of its
-// columns (key = score order << 32 | list id) and an online softmax sum; the
-// warp then pops the nprobe smallest heads.
-template <int NP>
+// columns (key = score order << 32 | list id) and, when coverage is asked for
+// (COV), an online softmax sum; the warp then pops the nprobe smallest heads.
+// Without the distance prior the logits are read as float4, four per lane in
+// flight (a lane's columns are 4g .. 4g+3 for its groups g).
+template <int NP, bool COV>
 __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int noutp, const float* __restrict__ D,
                                        const float* __restrict__ theta, int nout, int64_t nq, int nprobe,
                                        int32_t* __restrict__ probes, float* __restrict__ coverage) {
@@ -658,14 +660,14 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
   float mx = -INFINITY, sm = 0.0f;
   const float* lrow = logits + q * noutp;
   const float* drow = D ? D + q * nout : nullptr;
-  for (int c = lane; c < nout; c += 32) {
-    float sc = lrow[c];
-    if (D) sc -= beta * drow[c];
-    if (sc > mx) {
-      sm = (mx == -INFINITY ? 0.0f : sm * expf(mx - sc)) + 1.0f;
-      mx = sc;
-    } else if (sc > -INFINITY) {
-      sm += expf(sc - mx);
+  auto consider = [&](float sc, int c) {
+    if (COV) {
+      if (sc > mx) {
+        sm = (mx == -INFINITY ? 0.0f : sm * expf(mx - sc)) + 1.0f;
+        mx = sc;
+      } else if (sc > -INFINITY) {
+        sm += expf(sc - mx);
+      }
     }
     const uint64_t key = ((uint64_t)score_key(sc) << 32) | (uint32_t)c;
     if (key < lst[NP - 1]) {
@@ -678,11 +680,40 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
           lst[i - 1] = x;
         }
     }
+  };
+  if (!D) {
+    const float4* l4 = reinterpret_cast<const float4*>(lrow);  // noutp % 4 == 0, rows 16-byte aligned
+    const int n4 = (nout + 3) >> 2;
+    constexpr int U = 4;
+    for (int g0 = lane; g0 < n4; g0 += 32 * U) {
+      float4 v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int g = g0 + 32 * u;
+        v[u] = g < n4 ? __ldg(l4 + g) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int g = g0 + 32 * u;
+        if (g < n4) {
+          const int c = 4 * g;
+          consider(v[u].x, c);
+          if (c + 1 < nout) consider(v[u].y, c + 1);
+          if (c + 2 < nout) consider(v[u].z, c + 2);
+          if (c + 3 < nout) consider(v[u].w, c + 3);
+        }
+      }
+    }
+  } else {
+    for (int c = lane; c < nout; c += 32) consider(lrow[c] - beta * drow[c], c);
   }
-  float gmx = mx;
-  for (int o = 16; o; o >>= 1) gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
-  float gs = (mx == -INFINITY) ? 0.0f : sm * expf(mx - gmx);
-  for (int o = 16; o; o >>= 1) gs += __shfl_xor_sync(0xffffffffu, gs, o);
+  float gmx = 0.0f, gs = 1.0f;
+  if (COV) {
+    gmx = mx;
+    for (int o = 16; o; o >>= 1) gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
+    gs = (mx == -INFINITY) ? 0.0f : sm * expf(mx - gmx);
+    for (int o = 16; o; o >>= 1) gs += __shfl_xor_sync(0xffffffffu, gs, o);
+  }
   float cov = 0.0f;
   for (int r = 0; r < nprobe; ++r) {
     uint64_t m = lst[0];
@@ -698,12 +729,14 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
     if (lane == 0) {
       const int id = (int)(uint32_t)(m & 0xFFFFFFFFu);
       probes[q * nprobe + r] = id;
-      float sc = lrow[id];
-      if (D) sc -= beta * drow[id];
-      cov += expf(sc - gmx);
+      if (COV) {
+        float sc = lrow[id];
+        if (D) sc -= beta * drow[id];
+        cov += expf(sc - gmx);
+      }
     }
   }
-  if (coverage && lane == 0) coverage[q] = cov / gs;
+  if (COV && lane == 0) coverage[q] = cov / gs;
 }
 
 // ------------------------------------------------------------ host model
@@ -1003,9 +1036,19 @@ mann_status probe_route_device(Context* ctx, ProbeModel* m, cudaStream_t s, cons
     float* cv = coverage ? coverage + r0 : nullptr;
     const unsigned wgrid = (unsigned)ceil_div(nb, 8);
     if (nprobe <= 8) {
-      route_topk_warp_kernel<8><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe, pr, cv);
+      if (cv)
+        route_topk_warp_kernel<8, true><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe,
+                                                              pr, cv);
+      else
+        route_topk_warp_kernel<8, false><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe,
+                                                               pr, cv);
     } else if (nprobe <= 16) {
-      route_topk_warp_kernel<16><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe, pr, cv);
+      if (cv)
+        route_topk_warp_kernel<16, true><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb, nprobe,
+                                                               pr, cv);
+      else
+        route_topk_warp_kernel<16, false><<<wgrid, 256, 0, s>>>(logits, P.noutp, D, w + P.theta, P.nout, nb,
+                                                                nprobe, pr, cv);
     } else {
       const size_t smem = sizeof(uint32_t) * P.nout;
       if (smem > 48 * 1024)
