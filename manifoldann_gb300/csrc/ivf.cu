@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "f32x2.cuh"
 #include "kernels.cuh"
 #include "warp_list.cuh"
 
@@ -26,7 +27,7 @@ namespace {
 
 constexpr int SCAN_Q = 32;    // queries per CTA (at most)
 constexpr int SCAN_T = 256;   // threads = points per pass
-constexpr int SCAN_DC = 32;   // dimensions per stage
+constexpr int SCAN_DC = 32;   // dimensions per register batch of a point row
 
 __global__ void ivf_lists_kernel(const int64_t* __restrict__ start, const int64_t* __restrict__ members,
                                  int k, int64_t n, int64_t* __restrict__ offsets,
@@ -123,7 +124,11 @@ __global__ void __launch_bounds__(SCAN_T, QC == 16 ? 3 : 2)
                     const int64_t* __restrict__ qoff, const int32_t* __restrict__ pair_q,
                     const int32_t* __restrict__ pair_r, const int64_t* __restrict__ choff, int nlist,
                     int k, int nprobe, uint64_t* __restrict__ partial) {
-  __shared__ __align__(16) float qsm[QC][SCAN_DC];
+  // queries staged transposed, [dimension][query] with a padded stride, so one
+  // 16-byte broadcast read gives four queries' value at one dimension
+  constexpr int SDQ = QC == 16 ? 128 : 64;  // dimensions per stage
+  constexpr int QS = QC + 4;                // stride (floats), a multiple of 4
+  __shared__ __align__(16) float qsm[SDQ * QS];
   __shared__ float dsm[QC][SCAN_T + 1];
   __shared__ int32_t s_q[QC];
 
@@ -154,52 +159,58 @@ __global__ void __launch_bounds__(SCAN_T, QC == 16 ? 3 : 2)
     const int64_t pi = p0 + t;
     const bool valid = pi < p_end;
     const float* prow = data + (valid ? (int64_t)lids[pi] : 0) * d;
-    float acc[QC];
+    // queries 2i and 2i+1 in one f32x2 pair: each lane rounds as the scalar
+    // difference form, dimension by dimension in order
+    uint64_t acc2[QC / 2];
 #pragma unroll
-    for (int j = 0; j < QC; ++j) acc[j] = 0.0f;
-    for (int c0 = 0; c0 < d; c0 += SCAN_DC) {
-      const int dc = min(SCAN_DC, d - c0);
+    for (int i = 0; i < QC / 2; ++i) acc2[i] = 0ull;
+    const int ng4 = (nqe + 3) >> 2;  // groups of four staged queries in use
+    for (int c0 = 0; c0 < d; c0 += SDQ) {
+      const int dq = min(SDQ, d - c0);
       __syncthreads();
-      for (int e = t; e < QC * SCAN_DC; e += SCAN_T) {
-        const int r = e / SCAN_DC, c = e % SCAN_DC;
-        qsm[r][c] = (r < nqe && c < dc) ? __ldg(&qs[(int64_t)s_q[r] * d + c0 + c]) : 0.0f;
-      }
-      float pv[SCAN_DC];
-      if (VEC && dc == SCAN_DC) {
-#pragma unroll
-        for (int c = 0; c < SCAN_DC; c += 4) {
-          const float4 v = valid ? __ldg(reinterpret_cast<const float4*>(prow + c0 + c)) : make_float4(0, 0, 0, 0);
-          pv[c] = v.x;
-          pv[c + 1] = v.y;
-          pv[c + 2] = v.z;
-          pv[c + 3] = v.w;
-        }
-      } else {
-#pragma unroll
-        for (int c = 0; c < SCAN_DC; ++c) pv[c] = (valid && c < dc) ? __ldg(prow + c0 + c) : 0.0f;
+      for (int e = t; e < QC * SDQ; e += SCAN_T) {
+        const int r = e / SDQ, c = e % SDQ;
+        qsm[c * QS + r] = (r < nqe && c < dq) ? __ldg(&qs[(int64_t)s_q[r] * d + c0 + c]) : 0.0f;
       }
       __syncthreads();
-      // dimensions past d are zero in both operands: (0 - 0)^2 adds nothing
-#pragma unroll
-      for (int j = 0; j < QC; ++j) {
-        if (j < nqe) {
-          float a = acc[j];
+      for (int cb = 0; cb < dq; cb += SCAN_DC) {
+        const int dc = min(SCAN_DC, dq - cb);
+        float pv[SCAN_DC];
+        if (VEC && dc == SCAN_DC) {
 #pragma unroll
           for (int c = 0; c < SCAN_DC; c += 4) {
-            const float4 q4 = *reinterpret_cast<const float4*>(&qsm[j][c]);
-            float u = __fsub_rn(q4.x, pv[c]);
-            a = __fmaf_rn(u, u, a);
-            u = __fsub_rn(q4.y, pv[c + 1]);
-            a = __fmaf_rn(u, u, a);
-            u = __fsub_rn(q4.z, pv[c + 2]);
-            a = __fmaf_rn(u, u, a);
-            u = __fsub_rn(q4.w, pv[c + 3]);
-            a = __fmaf_rn(u, u, a);
+            const float4 v =
+                valid ? __ldg(reinterpret_cast<const float4*>(prow + c0 + cb + c)) : make_float4(0, 0, 0, 0);
+            pv[c] = v.x;
+            pv[c + 1] = v.y;
+            pv[c + 2] = v.z;
+            pv[c + 3] = v.w;
           }
-          acc[j] = a;
+        } else {
+#pragma unroll
+          for (int c = 0; c < SCAN_DC; ++c) pv[c] = (valid && c < dc) ? __ldg(prow + c0 + cb + c) : 0.0f;
+        }
+        // dimensions past d are zero in both operands: (0 - 0)^2 adds nothing
+#pragma unroll
+        for (int c = 0; c < SCAN_DC; ++c) {
+          const uint64_t x2 = f2::pack(pv[c], pv[c]);
+          const float4* qrow4 = reinterpret_cast<const float4*>(&qsm[(cb + c) * QS]);
+#pragma unroll
+          for (int g = 0; g < QC / 4; ++g) {
+            if (g < ng4) {  // block-uniform
+              const float4 q4 = qrow4[g];
+              uint64_t u = f2::sub(f2::pack(q4.x, q4.y), x2);
+              acc2[2 * g] = f2::fma(u, u, acc2[2 * g]);
+              u = f2::sub(f2::pack(q4.z, q4.w), x2);
+              acc2[2 * g + 1] = f2::fma(u, u, acc2[2 * g + 1]);
+            }
+          }
         }
       }
     }
+    float acc[QC];
+#pragma unroll
+    for (int i = 0; i < QC / 2; ++i) f2::unpack(acc2[i], acc[2 * i], acc[2 * i + 1]);
 #pragma unroll
     for (int j = 0; j < QC; ++j)
       if (j < nqe) dsm[j][t] = METRIC == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc[j]) : acc[j];
