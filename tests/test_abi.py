@@ -119,3 +119,25 @@ def test_recall_at_k():
     assert M.recall_at_k([1], []) == 0.0
     with pytest.raises(M.ArgumentError):
         M.recall_at_k([[1]], [[1], [2]])
+
+
+def test_dataset_handle_rejects_bad_arguments_without_gpu():
+    # argument checks run before any CUDA call
+    from manifoldann_gb300 import _lib
+
+    lib = _lib.load()
+    h = C.c_void_p()
+    x = np.zeros((4, 3), np.float32)
+    assert lib.mann_dataset_create(x.ctypes.data, 0, 3, C.byref(h)) == _lib.MANN_EINVAL_ARG
+    assert lib.mann_dataset_create(x.ctypes.data, 4, 0, C.byref(h)) == _lib.MANN_EINVAL_ARG
+    assert lib.mann_dataset_create(None, 4, 3, C.byref(h)) == _lib.MANN_EINVAL_ARG
+    assert lib.mann_dataset_create(x.ctypes.data, 4, 3, None) == _lib.MANN_EINVAL_ARG
+    assert lib.mann_dataset_upload(None, x.ctypes.data, 4) == _lib.MANN_EINVAL_ARG
+    assert lib.mann_dataset_destroy(None) == 0
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, 3, _lib.PREC_FP32)
+    ids = np.zeros((4, 3), np.int32)
+    d = np.zeros((4, 3), np.float32)
+    assert lib.mann_knn_dataset(p, None, x.ctypes.data, 4, ids.ctypes.data, d.ctypes.data, None) == \
+        _lib.MANN_EINVAL_ARG
+    assert lib.mann_knn_graph_dataset(p, None, 0, ids.ctypes.data, d.ctypes.data, None) == _lib.MANN_EINVAL_ARG
+    assert "dataset" in _lib.last_error()
