@@ -375,9 +375,10 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 // One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
 // rows: v holds the row's 32 accumulators of the chunk; lane j's nbv is the
 // norm of the chunk's point j (read by shuffle).  The row's list lives in
-// shared memory, entry e at mylist[e * BM], unsorted; lslot is the slot of its
-// largest entry and thr_key that entry, or the row's seed key (seed est', id 0)
-// while the list has an empty slot, and thr_est that key's est'.  The common
+// shared memory, entry e at mylist[e * BM], unsorted, filled in slot order
+// (nfill slots in use); lslot is the slot of its largest entry and thr_key
+// that entry, or the row's seed key (seed est', id 0) while the list has an
+// empty slot, and thr_est that key's est'.  The common
 // case -- no column of any row below its threshold -- costs a shuffle, an FMA
 // and a min per value and one vote; a lane with candidates admits them one by
 // one: the new key replaces the largest entry and the `depth` entries are
@@ -386,7 +387,7 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 // shared-memory loads).
 __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, uint64_t* __restrict__ mylist,
                                           uint64_t& thr_key, float& thr_est, uint64_t seed_key,
-                                          int& lslot, uint32_t col0, int depth) {
+                                          int& lslot, int& nfill, uint32_t col0, int depth) {
   float e[32];
 #pragma unroll
   for (int j = 0; j < 32; ++j) e[j] = __fmaf_rn(-2.0f, __uint_as_float(v[j]), __shfl_sync(FULL, nbv, j));
@@ -409,7 +410,13 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, ui
       for (int u = 1; u < 32; ++u) val = j == u ? e[u] : val;
       const uint64_t c = make_key(val, col0 + (uint32_t)j);
       if (c < thr_key) {
-        mylist[lslot * BM] = c;  // the largest entry (or an empty slot) drops out
+        if (nfill < depth) {
+          // an empty slot: the threshold stays the seed until the list is full
+          mylist[nfill * BM] = c;
+          if (++nfill < depth) continue;
+        } else {
+          mylist[lslot * BM] = c;  // the largest entry drops out
+        }
         uint64_t m = 0;
         int ms = 0;
 #pragma unroll 8
@@ -597,7 +604,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     uint64_t seed_key = KEY_NONE;
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
-    int lslot = 0;
+    int lslot = 0, nfill = 0;
     uint64_t top[SEED_DEPTH];
 #pragma unroll
     for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
@@ -662,6 +669,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         thr_key = seed_key;
         thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
         lslot = 0;
+        nfill = 0;
       }
       const int buf = tcount & 1;
       const int64_t col0 = (int64_t)t * BN;
@@ -686,8 +694,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         if (a.seedmode)
           seed_chunk(va, pick(nbc, ch), top, (uint32_t)(col0 + ch * 32));
         else
-          epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, (uint32_t)(col0 + ch * 32),
-                    a.depth);
+          epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                    (uint32_t)(col0 + ch * 32), a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
@@ -700,7 +708,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         if (a.seedmode)
           seed_chunk(vb, pick(nbc, ch + 1), top, (uint32_t)(col0 + (ch + 1) * 32));
         else
-          epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot,
+          epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot, nfill,
                     (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
