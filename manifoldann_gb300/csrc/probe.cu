@@ -660,6 +660,9 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
   float mx = -INFINITY, sm = 0.0f;
   const float* lrow = logits + q * noutp;
   const float* drow = D ? D + q * nout : nullptr;
+  // wthr: the NP-th smallest of the lanes' best keys -- NP distinct columns
+  // are at or below it, so no larger key can be among the warp's NP best
+  uint64_t wthr = KEY_NONE;
   auto consider = [&](float sc, int c) {
     if (COV) {
       if (sc > mx) {
@@ -670,7 +673,7 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
       }
     }
     const uint64_t key = ((uint64_t)score_key(sc) << 32) | (uint32_t)c;
-    if (key < lst[NP - 1]) {
+    if (key < lst[NP - 1] && key < wthr) {
       lst[NP - 1] = key;
 #pragma unroll
       for (int i = NP - 1; i > 0; --i)
@@ -703,6 +706,18 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
           if (c + 3 < nout) consider(v[u].w, c + 3);
         }
       }
+      // tighten the warp bound: sort the lanes' best keys across the warp
+      uint64_t h = lst[0];
+#pragma unroll
+      for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+          const uint64_t o = __shfl_xor_sync(0xffffffffu, (unsigned long long)h, j);
+          const bool keep_min = ((lane & j) == 0) == ((lane & kk) == 0);
+          h = keep_min ? (o < h ? o : h) : (o > h ? o : h);
+        }
+      }
+      wthr = __shfl_sync(0xffffffffu, (unsigned long long)h, NP - 1);
     }
   } else {
     for (int c = lane; c < nout; c += 32) consider(lrow[c] - beta * drow[c], c);
