@@ -1,6 +1,7 @@
 // knn_bf16.cu -- exact kNN through BF16 tensor-core tiles (tcgen05 / TMEM),
 // a certified top-(k+m) candidate set, exact FP32 rerank and FP64 near-tie
-// resolution.  Metrics: SqEuclidean and Euclidean.
+// resolution.  Metrics: SqEuclidean, Euclidean, and CosineDist (the passes run
+// on unit-normalised rows; the rerank uses the FP32 form's cosine).
 //
 // Replaces the same reference sites as the FP32 form
 // (src/indices/bruteforce.jl:59-65, src/ann_index.jl:91-98,
