@@ -116,7 +116,9 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
  * over the same points copy only their queries.  The copy goes stale when the
  * caller changes the points: re-upload after insert!
  * (src/indices/bruteforce.jl:82-95).  A handle belongs to the device that
- * was current at create; calls from another device fail with MANN_EINVAL_ARG. */
+ * was current at create; calls from another device fail with MANN_EINVAL_ARG.
+ * Searches may share a handle across threads; an upload or destroy must not
+ * overlap a search on the same handle (the handle has no lock). */
 typedef struct mann_dataset mann_dataset;
 /* data: host [n][d] FP32; copied to the device before the call returns. */
 mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_dataset** out);
