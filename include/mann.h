@@ -73,6 +73,11 @@ typedef struct {
   int32_t margin_used;       /* candidates kept beyond k by the reduced-precision form */
   double kernel_ms;          /* dominant kernel's CUDA-event time (MANN_FLAG_TIME_KERNEL), else -1 */
   int64_t launches;          /* kernels this call launched */
+  int64_t rows_ties_widened; /* MANN_FLAG_FP64_TIES: rows whose tie at the k-th distance reached
+                                past the candidate list and were re-ordered from their exact
+                                FP32 top-256 */
+  int64_t rows_unresolved;   /* MANN_FLAG_FP64_TIES: rows whose tie cluster is longer than that
+                                (they keep the FP32 (distance, id) order); 0 in every test */
 } mann_knn_report;
 
 const char* mann_version(void);
@@ -350,6 +355,25 @@ mann_status mann_edge_weights_device(int32_t rule, const float* data, int64_t n,
                                      const float* basis, int32_t maxd, float* out_weights,
                                      int64_t* out_negative, void* stream);
 
+/* Measured FP32 fused multiply-add rate of the current device (TFLOP/s,
+ * 2 flops per FMA): independent fma.rn.f32x2 / fmaf chains on every lane,
+ * timed with CUDA events, the faster form reported.  The denominator of the
+ * FP32 kernels' rooflines.  No reference counterpart (device
+ * characterisation).  out_ms (nullable): the timed launch. */
+mann_status mann_measure_fp32_peak(double* out_tflops, double* out_ms);
+
+/* Host-side fault injection for tests (no reference counterpart; the
+ * reference reports failures as Julia exceptions, src/utils/validation.jl).
+ * MANN_INJECT_ALLOC: the next `count` requests for the library's device
+ * scratch fail as an out-of-memory cudaMalloc would (the call returns
+ * MANN_ENOMEM; buffers already held stay valid).
+ * MANN_INJECT_LAUNCH: the next `count` checked kernel launches report a CUDA
+ * error (the call returns MANN_ECUDA; the work already enqueued completes).
+ * count = 0 clears the kind.  Nothing touches the GPU. */
+#define MANN_INJECT_ALLOC 1
+#define MANN_INJECT_LAUNCH 2
+mann_status mann_debug_inject(int32_t kind, int32_t count);
+
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.
  * No counterpart in the reference: it is an addition of this library for
  * hosts that own all device memory through their own pool (a Julia or Python
@@ -362,7 +386,9 @@ mann_status mann_edge_weights_device(int32_t rule, const float* data, int64_t n,
  * MANN_EINVAL_ARG (pass fewer queries per call).  The first call on a device
  * looks up that array's address and should come before any stream capture.
  * All calls on a device share the array, so calls that overlap on the GPU
- * race: serialise them. */
+ * race: serialise them.  The array's address is looked up once per device
+ * and kept for the life of the process: after a cudaDeviceReset the process
+ * must be restarted before this entry point is called again. */
 mann_status mann_knn_device_noalloc(const mann_knn_params* p, const float* base, int64_t n,
                                     const float* queries, int64_t q, int32_t d, int32_t* out_ids,
                                     float* out_dists, void* stream);

@@ -31,6 +31,8 @@ PREC_AUTO = 3
 FLAG_FP64_TIES = 1
 FLAG_TIME_KERNEL = 2
 FLAG_FP64_ERR = 4
+INJECT_ALLOC = 1
+INJECT_LAUNCH = 2
 
 
 class DimensionMismatch(ValueError):
@@ -67,6 +69,8 @@ class KnnReport(C.Structure):
         ("margin_used", C.c_int32),
         ("kernel_ms", C.c_double),
         ("launches", C.c_int64),
+        ("rows_ties_widened", C.c_int64),
+        ("rows_unresolved", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -178,6 +182,8 @@ SIGNATURES = {
     "mann_knn_graph_symmetrize_device": (_I32, [_P, _I64, _I32, _P, _P, _P, _P]),
     "mann_ivf_scan_device": (_I32, [C.POINTER(KnnParams), _P, _I32, _P, _I64, _I32, _I32, _P, _P, _P,
                                     _I64, _P, _P, _P]),
+    "mann_measure_fp32_peak": (_I32, [C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mann_debug_inject": (_I32, [_I32, _I32]),
 }
 
 _lib = None

@@ -102,7 +102,7 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
     uint64_t* fkeys = nullptr;
     MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kk, nullptr, qn, bn, &fkeys,
                            SLOT_PARTIAL, SLOT_KEYS));
-    MANN_TRY(fp32_then_resolve(ctx, s, base, qs, n, nq, d, p->metric, kk, kreq, fkeys, &keys, rep));
+    MANN_TRY(fp32_then_resolve(ctx, s, base, qs, n, nq, d, p->metric, kk, kreq, fkeys, qn, bn, &keys, rep));
   } else {
     MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, nullptr, qn, bn, &keys,
                            SLOT_PARTIAL, SLOT_KEYS));

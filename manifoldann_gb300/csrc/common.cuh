@@ -17,6 +17,8 @@ void clear_error();
 
 // kernels launched by the calling thread (reported per call)
 void note_launch();
+// true once per failure requested through mann_debug_inject(MANN_INJECT_LAUNCH, n)
+bool injected_launch_error();
 int64_t launch_count();
 
 struct Status {
@@ -36,10 +38,12 @@ struct Status {
   } while (0)
 
 // after every kernel launch: count it and surface launch errors
-#define MANN_CHECK_LAUNCH()                   \
-  do {                                        \
-    ::mann::note_launch();                    \
-    MANN_CUDA_TRY(cudaGetLastError());        \
+#define MANN_CHECK_LAUNCH()                                                         \
+  do {                                                                              \
+    ::mann::note_launch();                                                          \
+    MANN_CUDA_TRY(cudaGetLastError());                                              \
+    if (::mann::injected_launch_error())                                            \
+      return ::mann::fail(MANN_ECUDA, "CUDA error (injected by mann_debug_inject)"); \
   } while (0)
 
 #define MANN_TRY(expr)                 \

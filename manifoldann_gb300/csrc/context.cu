@@ -1,4 +1,5 @@
 // context.cu -- error reporting and per-device contexts.
+#include <atomic>
 #include <memory>
 
 #include "context.cuh"
@@ -10,16 +11,31 @@ thread_local std::string g_last_error;
 thread_local int64_t g_launches = 0;
 std::mutex g_ctx_mu;
 std::unique_ptr<Context> g_ctx[64];
+// host-side fault injection (mann_debug_inject): pending failures per kind
+std::atomic<int> g_inject_alloc{0};
+std::atomic<int> g_inject_launch{0};
+
+// true once for each pending injected failure of `counter`
+bool take_injected(std::atomic<int>& counter) {
+  int c = counter.load();
+  while (c > 0)
+    if (counter.compare_exchange_weak(c, c - 1)) return true;
+  return false;
+}
 }  // namespace
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 void note_launch() { ++g_launches; }
+bool injected_launch_error() { return take_injected(g_inject_launch); }
 int64_t launch_count() { return g_launches; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 
 mann_status Context::scratch(int slot, size_t bytes, void** out) {
   if (bytes == 0) bytes = 256;
+  if (take_injected(g_inject_alloc))
+    return fail(MANN_ENOMEM, "cudaMalloc of " + std::to_string(bytes) +
+                                 " bytes of scratch failed (out of memory, injected by mann_debug_inject)");
   if (slot_bytes[slot] < bytes) {
     if (slot_ptr[slot]) {
       MANN_CUDA_TRY(cudaFree(slot_ptr[slot]));
@@ -94,3 +110,16 @@ CallScope::CallScope(Context* ctx, cudaStream_t s) : ctx_(ctx), s_(s), lock_(ctx
 CallScope::~CallScope() { cudaEventRecord(ctx_->last_use, s_); }
 
 }  // namespace mann
+
+extern "C" mann_status mann_debug_inject(int32_t kind, int32_t count) {
+  mann::clear_error();
+  if (count < 0) return mann::fail(MANN_EINVAL_ARG, "count must be >= 0");
+  if (kind == MANN_INJECT_ALLOC) {
+    mann::g_inject_alloc.store(count);
+  } else if (kind == MANN_INJECT_LAUNCH) {
+    mann::g_inject_launch.store(count);
+  } else {
+    return mann::fail(MANN_EINVAL_ARG, "unknown injection kind");
+  }
+  return MANN_OK;
+}

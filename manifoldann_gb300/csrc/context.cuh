@@ -84,6 +84,12 @@ enum ScratchSlot : int {
   SLOT_CSR_COLS,      // host-pointer union graph: columns
   SLOT_CSR_ROWS,      // host-pointer union graph: row offsets
   SLOT_FP64_ERR,      // maximum FP64 error of the returned distances
+  SLOT_TIES_ROWS,     // FP64 ties: rows whose boundary tie reached past the candidates
+  SLOT_TIES_PARTIAL,  // FP64 ties: their wider FP32 lists (per split)
+  SLOT_TIES_KEYS,     // FP64 ties: their wider FP32 lists (merged)
+  SLOT_TIES_CNT,      // FP64 ties: candidate counts of the wider lists
+  SLOT_TIES_FLOOR,    // FP64 ties: floors of the wider lists
+  SLOT_TIES_COUNTERS, // FP64 ties: counters of the second resolve
   SLOT_COUNT
 };
 

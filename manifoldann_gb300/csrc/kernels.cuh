@@ -35,16 +35,28 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
 // Orders near-ties of sorted FP32 candidate lists by FP64 distance (when fp64)
 // and truncates them to kreq keys.  counters[0] += rows re-ordered,
-// counters[1] += rows whose boundary tie could not be settled.
+// counters[1] += rows whose boundary tie could not be settled (their query
+// rows appended to unres_rows when it is not NULL).  Candidate row i belongs
+// to query / output row rows[i] (identity when rows is NULL).
 mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
-                           cudaStream_t s);
+                           cudaStream_t s, const int32_t* rows = nullptr, int32_t* unres_rows = nullptr);
 
-// Exact FP32 top-kk lists -> FP64-ordered near-ties, truncated to kreq.
+// Exact FP32 top-kk lists -> FP64-ordered near-ties, truncated to kreq; rows
+// whose boundary tie reaches past kk are widened to the top-KMAX_FUSED.
+// Cosine needs the squared row norms (qn, bn) for that widening.
 mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, const float* qs,
                               int64_t n, int64_t nq, int d, int metric, int kk, int kreq,
-                              const uint64_t* fkeys, uint64_t** out_keys, mann_knn_report* rep);
+                              const uint64_t* fkeys, const float* qn, const float* bn,
+                              uint64_t** out_keys, mann_knn_report* rep);
+
+// Rows listed in unres_rows (h_unres, device) re-resolved from their exact
+// FP32 top-min(n, KMAX_FUSED); the rows still unsettled are counted.
+mann_status widen_unresolved(Context* ctx, cudaStream_t s, const float* base, const float* qs,
+                             int64_t n, int d, int metric, int kreq, const float* qn,
+                             const float* bn, const int32_t* unres_rows, int64_t h_unres,
+                             uint64_t* keys_out, int64_t* still_unresolved);
 
 // Plan and scratch-free variant of knn_fp32_keys (caller supplies `words`
 // uint64 of device scratch).

@@ -1128,22 +1128,29 @@ __device__ __forceinline__ double fp64_dist_row(const float* __restrict__ x,
   return metric == MANN_METRIC_EUCLIDEAN ? sqrt(s) : s;
 }
 
-// One warp per query.  cand[q][0..count) sorted by (fp32, id).  Writes the
-// first kreq keys to keys_out, ordering near-tie clusters by FP64 when asked.
+// One warp per candidate row i.  cand[i][0..count) sorted by (fp32, id);
+// the row belongs to query (and output row) q = rows[i] (rows == NULL: q = i).
+// Writes the first kreq keys to keys_out[q], ordering near-tie clusters by
+// FP64 when asked.  A row whose boundary tie cluster may reach past its
+// candidates is counted in n_unresolved and, when unres_rows is given, its q
+// is appended there (the caller widens those rows' candidates and resolves
+// them again).
 __global__ void resolve_kernel(const float* __restrict__ base, const float* __restrict__ qs,
                                int d, int metric, int64_t nq, int L, int kreq, int fp64,
                                const uint64_t* __restrict__ cand, const int* __restrict__ cand_count,
                                const float* __restrict__ floor_val, uint64_t* __restrict__ keys_out,
                                unsigned long long* __restrict__ n_fp64_rows,
-                               unsigned long long* __restrict__ n_unresolved) {
+                               unsigned long long* __restrict__ n_unresolved,
+                               const int32_t* __restrict__ rows, int32_t* __restrict__ unres_rows) {
   __shared__ uint64_t s_key[4][256];
   __shared__ double s_val[4][256];
   __shared__ int s_cl[4][256];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t q = (int64_t)blockIdx.x * 4 + w;
-  if (q >= nq) return;
-  const uint64_t* cq = cand + q * L;
-  const int c = min(cand_count[q], L);
+  const int64_t i = (int64_t)blockIdx.x * 4 + w;
+  if (i >= nq) return;
+  const int64_t q = rows ? (int64_t)rows[i] : i;
+  const uint64_t* cq = cand + i * L;
+  const int c = min(cand_count[i], L);
   uint64_t* out = keys_out + q * kreq;
   if (!fp64 || c <= 1) {
     for (int e = lane; e < kreq; e += 32) out[e] = e < c ? cq[e] : KEY_NONE;
@@ -1175,7 +1182,7 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
   bool resolvable = true;
   if (end == cm - 1) {
     const double lastv = (double)key_dist(s_key[w][cm - 1]);
-    const double fl = (double)floor_val[q];
+    const double fl = (double)floor_val[i];
     const bool clear = metric == MANN_METRIC_COSINE ? lastv + 2.0 * eps + 4.8e-7 < fl
                                                     : lastv * (1.0 + eps) < fl * (1.0 - eps);
     resolvable = clear || fl >= 3.0e38;
@@ -1184,7 +1191,10 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
   for (int p = 1; p <= end; ++p)
     if (s_cl[w][p] != p) { any_tie = true; break; }
   if (!resolvable) {
-    if (lane == 0) atomicAdd(n_unresolved, 1ull);
+    if (lane == 0) {
+      const unsigned long long slot = atomicAdd(n_unresolved, 1ull);
+      if (unres_rows) unres_rows[slot] = (int32_t)q;
+    }
   } else if (any_tie) {
     const float* qrow = qs + q * d;
     for (int p = lane; p <= end; p += 32) {
@@ -1261,11 +1271,11 @@ mann_status fp64_max_error(Context* ctx, cudaStream_t s, const float* base, cons
 mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
-                           cudaStream_t s) {
+                           cudaStream_t s, const int32_t* rows, int32_t* unres_rows) {
   if (nq <= 0) return MANN_OK;
   resolve_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(base, qs, d, metric, nq, L, kreq, fp64,
                                                             cand, cand_count, floor_val, keys_out,
-                                                            counters, counters + 1);
+                                                            counters, counters + 1, rows, unres_rows);
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
@@ -1287,29 +1297,72 @@ __global__ void fp32_lists_to_cand_kernel(const uint64_t* __restrict__ keys, int
 
 }  // namespace
 
+// Rows whose boundary tie cluster reached past their candidates (listed in
+// unres_rows, h_unres of them): the exact FP32 top-min(n, KMAX_FUSED) of each
+// such row, then the FP64 near-tie order again, written over those rows of
+// keys_out.  Rows still unsettled (a tie cluster longer than that list) are
+// returned in *still_unresolved; they keep the FP32 (distance, id) order.
+mann_status widen_unresolved(Context* ctx, cudaStream_t s, const float* base, const float* qs,
+                             int64_t n, int d, int metric, int kreq, const float* qn,
+                             const float* bn, const int32_t* unres_rows, int64_t h_unres,
+                             uint64_t* keys_out, int64_t* still_unresolved) {
+  *still_unresolved = 0;
+  if (h_unres <= 0) return MANN_OK;
+  const int kk = (int)std::min<int64_t>(n, KMAX_FUSED);
+  if (kk <= kreq) {  // every point is already a candidate: nothing lies beyond the list
+    return MANN_OK;
+  }
+  uint64_t* fkeys = nullptr;
+  MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_unres, d, metric, kk, unres_rows, qn, bn, &fkeys,
+                         SLOT_TIES_PARTIAL, SLOT_TIES_KEYS));
+  int* cand_count = nullptr;
+  float* floor_val = nullptr;
+  unsigned long long* counters = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_TIES_CNT, (size_t)h_unres, &cand_count));
+  MANN_TRY(ctx->scratch_t(SLOT_TIES_FLOOR, (size_t)h_unres, &floor_val));
+  MANN_TRY(ctx->scratch_t(SLOT_TIES_COUNTERS, 4, &counters));
+  MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+  fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(h_unres, 128), 128, 0, s>>>(fkeys, h_unres, kk, cand_count,
+                                                                            floor_val);
+  MANN_CHECK_LAUNCH();
+  MANN_TRY(launch_resolve(base, qs, d, metric, h_unres, kk, kreq, 1, fkeys, cand_count, floor_val, keys_out,
+                          counters, s, unres_rows, nullptr));
+  unsigned long long h[2] = {0, 0};
+  MANN_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  *still_unresolved = (int64_t)h[1];
+  return MANN_OK;
+}
+
 mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, const float* qs,
                               int64_t n, int64_t nq, int d, int metric, int kk, int kreq,
-                              const uint64_t* fkeys, uint64_t** out_keys, mann_knn_report* rep) {
-  (void)n;
+                              const uint64_t* fkeys, const float* qn, const float* bn,
+                              uint64_t** out_keys, mann_knn_report* rep) {
   int* cand_count = nullptr;
   float* floor_val = nullptr;
   unsigned long long* counters = nullptr;
   uint64_t* keys = nullptr;
+  int32_t* unres = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_MISC0, (size_t)nq, &cand_count));
   MANN_TRY(ctx->scratch_t(SLOT_MISC1, (size_t)nq, &floor_val));
   MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
   MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)nq * kreq, &keys));
+  MANN_TRY(ctx->scratch_t(SLOT_TIES_ROWS, (size_t)nq, &unres));
   MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
   fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(fkeys, nq, kk, cand_count,
                                                                        floor_val);
   MANN_CHECK_LAUNCH();
   MANN_TRY(launch_resolve(base, qs, d, metric, nq, kk, kreq, 1, fkeys, cand_count, floor_val, keys,
-                          counters + 4, s));
+                          counters + 4, s, nullptr, unres));
+  unsigned long long h[2] = {0, 0};
+  MANN_CUDA_TRY(cudaMemcpyAsync(h, counters + 4, sizeof(h), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  int64_t left = 0;
+  MANN_TRY(widen_unresolved(ctx, s, base, qs, n, d, metric, kreq, qn, bn, unres, (int64_t)h[1], keys, &left));
   if (rep) {
-    unsigned long long h[2] = {0, 0};
-    MANN_CUDA_TRY(cudaMemcpyAsync(h, counters + 4, sizeof(h), cudaMemcpyDeviceToHost, s));
-    MANN_CUDA_TRY(cudaStreamSynchronize(s));
     rep->rows_fp64_ties = (int64_t)h[0];
+    rep->rows_ties_widened = (int64_t)h[1];
+    rep->rows_unresolved = left;
   }
   *out_keys = keys;
   return MANN_OK;
@@ -1670,18 +1723,28 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
   // ---- resolve + truncate
   uint64_t* keys = nullptr;
+  int32_t* unres = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)nq * kreq, &keys));
+  if (fp64) MANN_TRY(ctx->scratch_t(SLOT_TIES_ROWS, (size_t)nq, &unres));
   MANN_TRY(launch_resolve(base, qs, d, metric, nq, L, kreq, fp64 ? 1 : 0, cand, cand_count, floor_val,
-                          keys, counters + 4, s));
-  if (rep) {
+                          keys, counters + 4, s, nullptr, unres));
+  if (rep || fp64) {
     unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
     MANN_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s));
     MANN_CUDA_TRY(cudaStreamSynchronize(s));
-    rep->rows_fallback = h_fb;
-    rep->candidates = (int64_t)h[2];
-    rep->rows_fp64_ties = (int64_t)h[4];
-    rep->precision_used = MANN_PREC_BF16;
-    rep->margin_used = depth - kreq;
+    int64_t left = 0;
+    if (fp64)
+      MANN_TRY(widen_unresolved(ctx, s, base, qs, n, d, metric, kreq, cosine ? cos_qn : nullptr,
+                                cosine ? cos_bn : nullptr, unres, (int64_t)h[5], keys, &left));
+    if (rep) {
+      rep->rows_fallback = h_fb;
+      rep->candidates = (int64_t)h[2];
+      rep->rows_fp64_ties = (int64_t)h[4];
+      rep->rows_ties_widened = fp64 ? (int64_t)h[5] : 0;
+      rep->rows_unresolved = left;
+      rep->precision_used = MANN_PREC_BF16;
+      rep->margin_used = depth - kreq;
+    }
   }
   *out_keys = keys;
   return MANN_OK;

@@ -745,18 +745,26 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
 namespace mann {
 
-// Split count of the FP32 form for (n, nq, kk) on a device with num_sms SMs,
-// and the uint64 words of scratch it needs (per-split lists, then merged lists
-// when there is more than one split).  Same plan as knn_fp32_keys.
+// Plan of the FP32 form for (n, nq, kk) on a device with num_sms SMs, as
+// knn_fp32_keys makes it: a few rows (nq <= FEW_Q, kk <= 64) go to the
+// few-row kernel with `*nsplit_out` = its grid of point slices; otherwise the
+// tile kernel with `*nsplit_out` point splits.  `*words_out` = the uint64
+// words of scratch (per-split lists, then merged lists when there is more
+// than one split).
 void knn_fp32_plan(int num_sms, int64_t n, int64_t nq, int kk, int* nsplit_out,
                    size_t* words_out) {
-  const int bq = nq <= 32 ? 32 : (kk <= 64 ? 128 : (kk <= 128 ? 64 : 32));
-  const int64_t qblocks = ceil_div(nq, bq);
-  const int64_t tiles = ceil_div(n, K1_BN);
-  int64_t want = std::max<int64_t>(1, ceil_div(num_sms, qblocks));
-  want = std::min<int64_t>(want, std::min<int64_t>(tiles, 128));
-  const int64_t tiles_per = ceil_div(tiles, want);
-  const int nsplit = (int)ceil_div(tiles, tiles_per);
+  int nsplit = 1;
+  if (nq <= FEW_Q && kk <= 64) {
+    nsplit = (int)std::min<int64_t>(256, ceil_div(n, FEW_T));
+  } else {
+    const int bq = nq <= 32 ? 32 : (kk <= 64 ? 128 : (kk <= 128 ? 64 : 32));
+    const int64_t qblocks = ceil_div(nq, bq);
+    const int64_t tiles = ceil_div(n, K1_BN);
+    int64_t want = std::max<int64_t>(1, ceil_div(num_sms, qblocks));
+    want = std::min<int64_t>(want, std::min<int64_t>(tiles, 128));
+    const int64_t tiles_per = ceil_div(tiles, want);
+    nsplit = (int)ceil_div(tiles, tiles_per);
+  }
   *nsplit_out = nsplit;
   *words_out = (size_t)nq * nsplit * kk + (nsplit > 1 ? (size_t)nq * kk : 0);
 }
@@ -776,34 +784,53 @@ mann_status knn_fp32_keys_on(int num_sms, cudaStream_t s, const float* base, int
   size_t need = 0;
   knn_fp32_plan(num_sms, n, nq, kk, &nsplit, &need);
   if (need > words) return fail(MANN_EINVAL_ARG, "scratch too small for this search");
-  const int64_t tiles = ceil_div(n, K1_BN);
-  const int64_t tiles_per = ceil_div(tiles, nsplit);
-  const int64_t split_len = tiles_per * K1_BN;
   uint64_t* partial = scratch;
-  Context plain;  // carries the SM count; no timing, no scratch
-  plain.num_sms = num_sms;
-  const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0) &&
-                   ((reinterpret_cast<uintptr_t>(qs) & 15) == 0);
   mann_status st;
-  switch (metric) {
-    case MANN_METRIC_EUCLIDEAN:
-      st = vec ? dispatch_k1<MANN_METRIC_EUCLIDEAN, true>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
-                                                          bn, split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_EUCLIDEAN, false>(&plain, kk, base, n, qs, nullptr, nq, d,
-                                                           qn, bn, split_len, nsplit, partial, s);
-      break;
-    case MANN_METRIC_SQEUCLIDEAN:
-      st = vec ? dispatch_k1<MANN_METRIC_SQEUCLIDEAN, true>(&plain, kk, base, n, qs, nullptr, nq, d,
-                                                            qn, bn, split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_SQEUCLIDEAN, false>(&plain, kk, base, n, qs, nullptr, nq, d,
+  if (nq <= FEW_Q && kk <= 64) {
+    // the few-row kernel, exactly as knn_fp32_keys runs it (grid = nsplit)
+    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0);
+    switch (metric) {
+      case MANN_METRIC_EUCLIDEAN:
+        st = vec4 ? launch_few_m<MANN_METRIC_EUCLIDEAN, true>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s)
+                  : launch_few_m<MANN_METRIC_EUCLIDEAN, false>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s);
+        break;
+      case MANN_METRIC_SQEUCLIDEAN:
+        st = vec4 ? launch_few_m<MANN_METRIC_SQEUCLIDEAN, true>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s)
+                  : launch_few_m<MANN_METRIC_SQEUCLIDEAN, false>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s);
+        break;
+      default:
+        st = vec4 ? launch_few_m<MANN_METRIC_COSINE, true>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s)
+                  : launch_few_m<MANN_METRIC_COSINE, false>(nsplit, base, n, qs, nullptr, (int)nq, d, qn, bn, kk, partial, s);
+        break;
+    }
+  } else {
+    const int64_t tiles = ceil_div(n, K1_BN);
+    const int64_t tiles_per = ceil_div(tiles, nsplit);
+    const int64_t split_len = tiles_per * K1_BN;
+    Context plain;  // carries the SM count; no timing, no scratch
+    plain.num_sms = num_sms;
+    const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(base) & 15) == 0) &&
+                     ((reinterpret_cast<uintptr_t>(qs) & 15) == 0);
+    switch (metric) {
+      case MANN_METRIC_EUCLIDEAN:
+        st = vec ? dispatch_k1<MANN_METRIC_EUCLIDEAN, true>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
+                                                            bn, split_len, nsplit, partial, s)
+                 : dispatch_k1<MANN_METRIC_EUCLIDEAN, false>(&plain, kk, base, n, qs, nullptr, nq, d,
                                                              qn, bn, split_len, nsplit, partial, s);
-      break;
-    default:
-      st = vec ? dispatch_k1<MANN_METRIC_COSINE, true>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
-                                                       bn, split_len, nsplit, partial, s)
-               : dispatch_k1<MANN_METRIC_COSINE, false>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
-                                                        bn, split_len, nsplit, partial, s);
-      break;
+        break;
+      case MANN_METRIC_SQEUCLIDEAN:
+        st = vec ? dispatch_k1<MANN_METRIC_SQEUCLIDEAN, true>(&plain, kk, base, n, qs, nullptr, nq, d,
+                                                              qn, bn, split_len, nsplit, partial, s)
+                 : dispatch_k1<MANN_METRIC_SQEUCLIDEAN, false>(&plain, kk, base, n, qs, nullptr, nq, d,
+                                                               qn, bn, split_len, nsplit, partial, s);
+        break;
+      default:
+        st = vec ? dispatch_k1<MANN_METRIC_COSINE, true>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
+                                                         bn, split_len, nsplit, partial, s)
+                 : dispatch_k1<MANN_METRIC_COSINE, false>(&plain, kk, base, n, qs, nullptr, nq, d, qn,
+                                                          bn, split_len, nsplit, partial, s);
+        break;
+    }
   }
   MANN_TRY(st);
   if (nsplit == 1) {

@@ -14,7 +14,9 @@
 // Rules of use:
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture;
+//     before any stream capture.  The address is kept for the life of the
+//     process, so a cudaDeviceReset (which drops the device's module and
+//     its arrays) needs a process restart before the next call;
 //   * every call on a device shares the one array: calls whose work overlaps
 //     on the GPU (different streams, or threads racing on one stream) corrupt
 //     each other's results -- serialise them;

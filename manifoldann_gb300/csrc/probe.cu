@@ -688,7 +688,10 @@ __global__ void route_topk_warp_kernel(const float* __restrict__ logits, int nou
     const float4* l4 = reinterpret_cast<const float4*>(lrow);  // noutp % 4 == 0, rows 16-byte aligned
     const int n4 = (nout + 3) >> 2;
     constexpr int U = 4;
-    for (int g0 = lane; g0 < n4; g0 += 32 * U) {
+    // every lane runs the same number of passes (the bitonic exchange below
+    // uses full-mask shuffles); lanes past the end only skip their loads
+    for (int b = 0; b < n4; b += 32 * U) {
+      const int g0 = b + lane;
       float4 v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {

@@ -28,6 +28,8 @@ _SIGS = {
     "orc_knn_f64": (_I32, [_P, _I64, _P, _I64, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_knn_graph_f32": (_I32, [_P, _I64, _I32, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_knn_graph_f64": (_I32, [_P, _I64, _I32, _I32, _I32, _I32, _P, _P, _I32]),
+    "orc_knn_graph_rows_f32": (_I32, [_P, _I64, _I32, _I32, _I32, _I32, _P, _I64, _P, _P, _I32]),
+    "orc_knn_graph_rows_f64": (_I32, [_P, _I64, _I32, _I32, _I32, _I32, _P, _I64, _P, _P, _I32]),
     "orc_kmeans_assign_gemm_f32": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_kmeans_assign_f64": (_I32, [_P, _I64, _P, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_topk_route": (_I32, [_P, _I32, _I32, _I32, _P]),
@@ -118,6 +120,19 @@ def knn_graph_f64(data, k, metric, include_self=False, threads=0):
     d = np.empty((n, k), np.float64)
     _check(load().orc_knn_graph_f64(data.ctypes.data, n, data.shape[1], k, int(include_self), metric,
                                     ids.ctypes.data, d.ctypes.data, threads))
+    return ids, d
+
+
+def knn_graph_rows(data, rows, k, metric, include_self=False, fp64=False, threads=0):
+    """Rows `rows` of the kNN graph of `data` (row i of the result = point
+    rows[i]), with the same semantics as knn_graph_f32 / knn_graph_f64."""
+    data = _f32(data)
+    rows = np.ascontiguousarray(rows, dtype=np.int32)
+    ids = np.empty((len(rows), k), np.int32)
+    d = np.empty((len(rows), k), np.float64 if fp64 else np.float32)
+    fn = load().orc_knn_graph_rows_f64 if fp64 else load().orc_knn_graph_rows_f32
+    _check(fn(data.ctypes.data, data.shape[0], data.shape[1], k, int(include_self), metric,
+              rows.ctypes.data, len(rows), ids.ctypes.data, d.ctypes.data, threads))
     return ids, d
 
 

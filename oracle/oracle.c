@@ -145,11 +145,111 @@ static inline double key_to_f64(uint64_t k) {
 
 /* ------------------------------------------------------------- exact kNN */
 
+/* Four pairs at a time: the same sequential per-pair sums as orc_dist_f32 /
+ * orc_dist_f64 (one fused multiply-add per dimension, in dimension order),
+ * interleaved so four independent chains are in flight.  Results are those
+ * of four separate orc_dist_* calls. */
+static void dist4_f32(const float* b0, const float* b1, const float* b2, const float* b3,
+                      const float* y, int32_t d, int32_t metric, float* out) {
+  if (metric == ORC_COSINE) {
+    float ab0 = 0.0f, ab1 = 0.0f, ab2 = 0.0f, ab3 = 0.0f;
+    float aa0 = 0.0f, aa1 = 0.0f, aa2 = 0.0f, aa3 = 0.0f, bb = 0.0f;
+    for (int32_t i = 0; i < d; ++i) {
+      const float yi = y[i];
+      ab0 = fmaf(b0[i], yi, ab0);
+      ab1 = fmaf(b1[i], yi, ab1);
+      ab2 = fmaf(b2[i], yi, ab2);
+      ab3 = fmaf(b3[i], yi, ab3);
+      aa0 = fmaf(b0[i], b0[i], aa0);
+      aa1 = fmaf(b1[i], b1[i], aa1);
+      aa2 = fmaf(b2[i], b2[i], aa2);
+      aa3 = fmaf(b3[i], b3[i], aa3);
+      bb = fmaf(yi, yi, bb);
+    }
+    const float ab[4] = {ab0, ab1, ab2, ab3}, aa[4] = {aa0, aa1, aa2, aa3};
+    for (int j = 0; j < 4; ++j) {
+      float r = 1.0f - ab[j] / (sqrtf(aa[j]) * sqrtf(bb));
+      if (r < 0.0f) r = 0.0f;
+      out[j] = r;
+    }
+    return;
+  }
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+  for (int32_t i = 0; i < d; ++i) {
+    const float yi = y[i];
+    const float t0 = b0[i] - yi, t1 = b1[i] - yi, t2 = b2[i] - yi, t3 = b3[i] - yi;
+    s0 = fmaf(t0, t0, s0);
+    s1 = fmaf(t1, t1, s1);
+    s2 = fmaf(t2, t2, s2);
+    s3 = fmaf(t3, t3, s3);
+  }
+  out[0] = s0;
+  out[1] = s1;
+  out[2] = s2;
+  out[3] = s3;
+  if (metric == ORC_EUCLIDEAN)
+    for (int j = 0; j < 4; ++j) out[j] = sqrtf(out[j]);
+}
+
+static void dist4_f64(const float* b0, const float* b1, const float* b2, const float* b3,
+                      const float* y, int32_t d, int32_t metric, double* out) {
+  if (metric == ORC_COSINE) {
+    double ab0 = 0.0, ab1 = 0.0, ab2 = 0.0, ab3 = 0.0;
+    double aa0 = 0.0, aa1 = 0.0, aa2 = 0.0, aa3 = 0.0, bb = 0.0;
+    for (int32_t i = 0; i < d; ++i) {
+      const double yi = (double)y[i];
+      const double x0 = (double)b0[i], x1 = (double)b1[i], x2 = (double)b2[i], x3 = (double)b3[i];
+      ab0 = fma(x0, yi, ab0);
+      ab1 = fma(x1, yi, ab1);
+      ab2 = fma(x2, yi, ab2);
+      ab3 = fma(x3, yi, ab3);
+      aa0 = fma(x0, x0, aa0);
+      aa1 = fma(x1, x1, aa1);
+      aa2 = fma(x2, x2, aa2);
+      aa3 = fma(x3, x3, aa3);
+      bb = fma(yi, yi, bb);
+    }
+    const double ab[4] = {ab0, ab1, ab2, ab3}, aa[4] = {aa0, aa1, aa2, aa3};
+    for (int j = 0; j < 4; ++j) {
+      double r = 1.0 - ab[j] / (sqrt(aa[j]) * sqrt(bb));
+      if (r < 0.0) r = 0.0;
+      out[j] = r;
+    }
+    return;
+  }
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  for (int32_t i = 0; i < d; ++i) {
+    const double yi = (double)y[i];
+    const double t0 = (double)b0[i] - yi, t1 = (double)b1[i] - yi;
+    const double t2 = (double)b2[i] - yi, t3 = (double)b3[i] - yi;
+    s0 = fma(t0, t0, s0);
+    s1 = fma(t1, t1, s1);
+    s2 = fma(t2, t2, s2);
+    s3 = fma(t3, t3, s3);
+  }
+  out[0] = s0;
+  out[1] = s1;
+  out[2] = s2;
+  out[3] = s3;
+  if (metric == ORC_EUCLIDEAN)
+    for (int j = 0; j < 4; ++j) out[j] = sqrt(out[j]);
+}
+
 static void knn_row_f32(const float* base, int64_t n, const float* qv, int32_t d, int32_t k,
                         int32_t metric, int32_t* ids, float* dists, kv_t* scratch) {
   int32_t ke = (int32_t)(k < n ? k : n);
   int32_t cnt = 0;
-  for (int64_t j = 0; j < n; ++j) {
+  int64_t j = 0;
+  for (; j + 4 <= n; j += 4) {
+    float v[4];
+    const float* b = base + j * (int64_t)d;
+    dist4_f32(b, b + d, b + 2 * (int64_t)d, b + 3 * (int64_t)d, qv, d, metric, v);
+    for (int u = 0; u < 4; ++u) {
+      kv_t c = {fkey32(v[u]), j + u};
+      topk_push(scratch, ke, &cnt, c);
+    }
+  }
+  for (; j < n; ++j) {
     float v = orc_dist_f32(base + j * (int64_t)d, qv, d, metric);
     kv_t c = {fkey32(v), j};
     topk_push(scratch, ke, &cnt, c);
@@ -169,7 +269,17 @@ static void knn_row_f64(const float* base, int64_t n, const float* qv, int32_t d
                         int32_t metric, int32_t* ids, double* dists, kv_t* scratch) {
   int32_t ke = (int32_t)(k < n ? k : n);
   int32_t cnt = 0;
-  for (int64_t j = 0; j < n; ++j) {
+  int64_t j = 0;
+  for (; j + 4 <= n; j += 4) {
+    double v[4];
+    const float* b = base + j * (int64_t)d;
+    dist4_f64(b, b + d, b + 2 * (int64_t)d, b + 3 * (int64_t)d, qv, d, metric, v);
+    for (int u = 0; u < 4; ++u) {
+      kv_t c = {fkey64(v[u]), j + u};
+      topk_push(scratch, ke, &cnt, c);
+    }
+  }
+  for (; j < n; ++j) {
     double v = orc_dist_f64(base + j * (int64_t)d, qv, d, metric);
     kv_t c = {fkey64(v), j};
     topk_push(scratch, ke, &cnt, c);
@@ -234,20 +344,26 @@ static void prepare_row_i(const int32_t* in_ids, int32_t in_k, int64_t self, int
   }
 }
 
+/* rows == NULL: every point, output row i = point i; otherwise output row i
+ * = point rows[i] (nrows rows) */
 #define GRAPH_BODY(TYPE, ROWFN)                                                              \
   if (d <= 0 || n <= 0) return 2;                                                            \
   int64_t maxk = n - (include_self ? 0 : 1);                                                 \
   if (!(k > 0 && k <= maxk)) return 2;                                                       \
   int32_t req = k + (include_self ? 0 : 1);                                                  \
   int nt = resolve_threads(nthreads);                                                        \
+  const int64_t nout = rows ? nrows : n;                                                     \
+  for (int64_t i = 0; rows && i < nrows; ++i)                                                \
+    if (rows[i] < 0 || rows[i] >= n) return 2;                                               \
   _Pragma("omp parallel num_threads(nt)") {                                                  \
     kv_t* scratch = (kv_t*)malloc(sizeof(kv_t) * (size_t)req);                               \
     int32_t* tid = (int32_t*)malloc(sizeof(int32_t) * (size_t)req);                          \
     TYPE* td = (TYPE*)malloc(sizeof(TYPE) * (size_t)req);                                    \
     int32_t* pos = (int32_t*)malloc(sizeof(int32_t) * (size_t)req);                          \
-    _Pragma("omp for schedule(dynamic, 4)") for (int64_t i = 0; i < n; ++i) {                \
-      ROWFN(data, n, data + i * (int64_t)d, d, req, metric, tid, td, scratch);               \
-      prepare_row_i(tid, req, i, k, include_self, ids + i * (int64_t)k, pos);                \
+    _Pragma("omp for schedule(dynamic, 1)") for (int64_t i = 0; i < nout; ++i) {             \
+      const int64_t r = rows ? (int64_t)rows[i] : i;                                         \
+      ROWFN(data, n, data + r * (int64_t)d, d, req, metric, tid, td, scratch);               \
+      prepare_row_i(tid, req, r, k, include_self, ids + i * (int64_t)k, pos);                \
       for (int32_t j = 0; j < k; ++j) dists[i * (int64_t)k + j] = td[pos[j]];                \
     }                                                                                        \
     free(scratch);                                                                           \
@@ -259,11 +375,29 @@ static void prepare_row_i(const int32_t* in_ids, int32_t in_k, int64_t self, int
 
 int orc_knn_graph_f32(const float* data, int64_t n, int32_t d, int32_t k, int32_t include_self,
                       int32_t metric, int32_t* ids, float* dists, int32_t nthreads) {
+  const int32_t* rows = NULL;
+  const int64_t nrows = 0;
   GRAPH_BODY(float, knn_row_f32)
 }
 
 int orc_knn_graph_f64(const float* data, int64_t n, int32_t d, int32_t k, int32_t include_self,
                       int32_t metric, int32_t* ids, double* dists, int32_t nthreads) {
+  const int32_t* rows = NULL;
+  const int64_t nrows = 0;
+  GRAPH_BODY(double, knn_row_f64)
+}
+
+int orc_knn_graph_rows_f32(const float* data, int64_t n, int32_t d, int32_t k,
+                           int32_t include_self, int32_t metric, const int32_t* rows,
+                           int64_t nrows, int32_t* ids, float* dists, int32_t nthreads) {
+  if (!rows) return 2;
+  GRAPH_BODY(float, knn_row_f32)
+}
+
+int orc_knn_graph_rows_f64(const float* data, int64_t n, int32_t d, int32_t k,
+                           int32_t include_self, int32_t metric, const int32_t* rows,
+                           int64_t nrows, int32_t* ids, double* dists, int32_t nthreads) {
+  if (!rows) return 2;
   GRAPH_BODY(double, knn_row_f64)
 }
 

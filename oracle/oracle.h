@@ -50,6 +50,14 @@ int orc_knn_graph_f32(const float* data, int64_t n, int32_t d, int32_t k, int32_
                       int32_t metric, int32_t* ids, float* dists, int32_t nthreads);
 int orc_knn_graph_f64(const float* data, int64_t n, int32_t d, int32_t k, int32_t include_self,
                       int32_t metric, int32_t* ids, double* dists, int32_t nthreads);
+/* The same rows of the graph for the points rows[0..nrows) only (output row
+ * i = point rows[i]): sampled rows of a graph too large for the full oracle. */
+int orc_knn_graph_rows_f32(const float* data, int64_t n, int32_t d, int32_t k,
+                           int32_t include_self, int32_t metric, const int32_t* rows,
+                           int64_t nrows, int32_t* ids, float* dists, int32_t nthreads);
+int orc_knn_graph_rows_f64(const float* data, int64_t n, int32_t d, int32_t k,
+                           int32_t include_self, int32_t metric, const int32_t* rows,
+                           int64_t nrows, int32_t* ids, double* dists, int32_t nthreads);
 
 /* KMeans assignment.
  * _gemm_f32: the reference's GEMM-form distances (src/transforms/kmeans/distance.jl:68-143:

@@ -141,3 +141,17 @@ def test_dataset_handle_rejects_bad_arguments_without_gpu():
         _lib.MANN_EINVAL_ARG
     assert lib.mann_knn_graph_dataset(p, None, 0, ids.ctypes.data, d.ctypes.data, None) == _lib.MANN_EINVAL_ARG
     assert "dataset" in _lib.last_error()
+
+
+def test_fault_injection_hook_arguments_without_gpu():
+    from manifoldann_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.mann_debug_inject(99, 1) == _lib.MANN_EINVAL_ARG
+    assert b"unknown injection kind" in lib.mann_last_error()
+    assert lib.mann_debug_inject(_lib.INJECT_ALLOC, -1) == _lib.MANN_EINVAL_ARG
+    # arming and clearing touch no device
+    assert lib.mann_debug_inject(_lib.INJECT_ALLOC, 2) == _lib.MANN_OK
+    assert lib.mann_debug_inject(_lib.INJECT_ALLOC, 0) == _lib.MANN_OK
+    assert lib.mann_debug_inject(_lib.INJECT_LAUNCH, 0) == _lib.MANN_OK
+

@@ -20,3 +20,8 @@ def test_reference_arm_line():
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert "workload" in line["config"]
+    # both arms describe the workload with the same config dict
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert line["config"] == json.loads(json.dumps(bench.CONFIG))

@@ -103,6 +103,33 @@ def test_route_topk_order_and_ties(gpu_lib):
     assert (pr_t.cpu().numpy() == np.arange(9)).all()
 
 
+@pytest.mark.parametrize("nout", [64, 100, 576, 4100])
+def test_route_topk_uneven_list_counts(gpu_lib, nout):
+    """List counts whose float4 groups do not fill whole 128-group passes
+    (nout mod 512 in 1..124): every lane still takes the warp-wide exchange
+    the same number of times, so the order equals the oracle's."""
+    import torch
+
+    dims = (32, 128, 128, nout)
+    rng = np.random.default_rng(nout)
+    params = _rand_params(dims, rng, scale=3.0)
+    X = rng.standard_normal((301, 32)).astype(np.float32)
+    m = _model(dims, False, params=params)
+    S = m.scores(X)
+    qd = torch.from_numpy(X).cuda()
+    order = np.stack([np.lexsort((np.arange(nout), -S[i])) for i in range(len(X))])
+    e = np.exp(S - S.max(1, keepdims=True))
+    for nprobe in (1, 4, 16):
+        pr = torch.empty((len(X), nprobe), dtype=torch.int32, device="cuda")
+        cov = torch.empty(len(X), dtype=torch.float32, device="cuda")
+        m.route_device(qd, nprobe, pr, cov)
+        torch.cuda.synchronize()
+        want = order[:, :nprobe]
+        assert np.array_equal(pr.cpu().numpy(), want), nprobe
+        cov_o = np.take_along_axis(e, want, 1).sum(1) / e.sum(1)
+        assert np.allclose(cov.cpu().numpy(), cov_o, rtol=1e-4, atol=1e-6), nprobe
+
+
 def test_training_is_deterministic_and_lowers_loss(gpu_lib):
     dims = (32, 128, 128, 64)
     rng = np.random.default_rng(5)

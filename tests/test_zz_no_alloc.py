@@ -39,8 +39,9 @@ def test_noalloc_matches_regular_entry_point(gpu_lib, metric):
 
     rng = np.random.default_rng(100 + metric)
     stream = torch.cuda.current_stream().cuda_stream
-    # two calls in a row with different shapes: the second must not see the first's scratch
-    for n, nq, d, k in [(20000, 700, 64, 10), (5003, 41, 37, 33)]:
+    # calls in a row with different shapes: a later call must not see an earlier one's
+    # scratch; the last two are few-row batches (q <= 32), which run the few-row kernel
+    for n, nq, d, k in [(20000, 700, 64, 10), (5003, 41, 37, 33), (70000, 5, 64, 10), (3001, 32, 19, 64)]:
         base = torch.from_numpy(rng.standard_normal((n, d)).astype(np.float32)).cuda()
         q = torch.from_numpy(rng.standard_normal((nq, d)).astype(np.float32)).cuda()
         ids_r, d_r = _run(gpu_lib, "regular", base, q, k, metric, stream, noalloc=False)
