@@ -16,8 +16,11 @@ from .transforms import (KMeansAssignment, KMeansTransform, TransformResult, ass
                          pairwise_distances, take_pending_assignments, transform)
 from .geometry import (CurvatureFreeSymmetric, EuclideanChord, PCAGeometry, PCAMethod,
                        TangentProjectedSourceOnly, TangentProjectedSymmetricMax,
-                       TangentProjectedSymmetricMean, compute_edge_weights, fit_geometries, fit_geometry,
+                       TangentProjectedSymmetricMean, WeightedKNNGraph, build_weighted_graph,
+                       candidate_neighbors, compute_edge_weights, fit_geometries, fit_geometry,
                        intrinsic_dimension, local_distance, project, reconstruct)
+from .multilevel import (DisjointMerge, MultiLevelIndex, SimpleMerge, TerminalConfig, TransformedConfig,
+                         TransformedIndex, build_multilevel_index, merge_results, multilevel_query)
 from .ivf import IVFFlatIndex, TopKRouting, ivf_search_device, select_indices
 from .probe import LearnedProbeRouting, ProbeModel, ivf_search_learned, neighbour_list_labels
 from .indices import (AbstractANNIndex, BruteForceIndex, DeviceDataset, Neighbor, build_index, configured_k,
@@ -40,4 +43,7 @@ __all__ = [
     "PCAGeometry", "PCAMethod", "fit_geometries", "fit_geometry", "intrinsic_dimension", "local_distance",
     "project", "reconstruct", "CurvatureFreeSymmetric", "EuclideanChord", "TangentProjectedSourceOnly",
     "TangentProjectedSymmetricMax", "TangentProjectedSymmetricMean", "compute_edge_weights",
+    "WeightedKNNGraph", "build_weighted_graph", "candidate_neighbors",
+    "DisjointMerge", "MultiLevelIndex", "SimpleMerge", "TerminalConfig", "TransformedConfig", "TransformedIndex",
+    "build_multilevel_index", "merge_results", "multilevel_query",
 ]

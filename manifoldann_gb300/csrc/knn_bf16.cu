@@ -52,16 +52,25 @@ constexpr unsigned FULL = 0xFFFFFFFFu;
 constexpr int BM = 128;          // queries per CTA tile (TMEM lanes)
 constexpr int BN = 256;          // points per tile (TMEM columns per accumulator)
 constexpr int BK = 64;           // BF16 elements per stage row (128 bytes, one swizzle span)
-constexpr int STAGES = 4;
 constexpr int A_STAGE_BYTES = BM * BK * 2;  // 16 KB
-constexpr int B_STAGE_BYTES = BN * BK * 2;  // 32 KB
-constexpr int STAGE_BYTES = A_STAGE_BYTES + B_STAGE_BYTES;
+// One CTA: A 128 x 64 + B 256 x 64 per stage (48 KB), 4 stages.  A CTA pair
+// (cta_group::2, M = 256): each CTA stages its own 128 query rows and half of
+// the tile's 256 point rows (32 KB per stage), 6 stages.
+template <bool PAIR>
+struct Stg {
+  static constexpr int B_ROWS = PAIR ? BN / 2 : BN;
+  static constexpr int B_BYTES = B_ROWS * BK * 2;
+  static constexpr int BYTES = A_STAGE_BYTES + B_BYTES;
+  static constexpr int N = PAIR ? 6 : 4;
+};
 
 constexpr int LIST = 32;                             // candidates kept per query row
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
+constexpr double BAND_MIN_BYTES = 96.0 * (1 << 20);  // point operands above this are walked in bands
+constexpr double BAND_BYTES = 48.0 * (1 << 20);      // point-operand bytes per band
 
 enum : int { ERR_TIMEOUT_PRODUCER = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_EPI = 3 };
 
@@ -277,12 +286,55 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
 
 // ---------------------------------------------------------------- main kernel
 
+// Order of the (query block, point tile) items.  With one band the items
+// are query-block-major (item = qb * tiles + t).  With several bands the point
+// tiles are cut into bands of band_tiles tiles (the last one shorter) and the
+// items of band b -- every query block against the band's tiles, query-block
+// major inside the band -- come before those of band b + 1, so all CTAs work
+// inside one band at a time and a point operand larger than L2 is read from
+// DRAM about once per launch instead of once per query block.  A segment is
+// the run of one (band, query block) inside one CTA's range; each segment
+// writes one partial list per epilogue set, at slot
+// (band * span + (cta - first CTA of the (band, query block) run)) * nsets + set.
+struct Walk {
+  int64_t work;   // qblocks * tiles
+  int grid;       // CTAs
+  int tiles;      // point tiles of BN
+  int qblocks;    // query blocks of BM
+  int band_tiles; // tiles per band (== tiles: one band)
+  int nbands;
+  int span;       // most CTAs any (band, query block) run touches
+  int qrows;      // query rows per query block (BM, or 2 BM for CTA pairs)
+};
+
+__host__ __device__ __forceinline__ int band_len(const Walk& w, int b) {
+  return b == w.nbands - 1 ? w.tiles - b * w.band_tiles : w.band_tiles;
+}
+// first item of the (band b, query block qb) run
+__host__ __device__ __forceinline__ int64_t run_begin(const Walk& w, int b, int qb) {
+  return (int64_t)b * w.qblocks * w.band_tiles + (int64_t)qb * band_len(w, b);
+}
+// (query block, tile, band) of item i
+__host__ __device__ __forceinline__ void item_pos(const Walk& w, int64_t i, int& qb, int& t, int& b) {
+  if (w.nbands == 1) {
+    qb = (int)(i / w.tiles);
+    t = (int)(i % w.tiles);
+    b = 0;
+    return;
+  }
+  const int64_t per = (int64_t)w.qblocks * w.band_tiles;
+  b = (int)(i / per);
+  if (b > w.nbands - 1) b = w.nbands - 1;
+  const int64_t r = i - (int64_t)b * per;
+  const int tb = band_len(w, b);
+  qb = (int)(r / tb);
+  t = b * w.band_tiles + (int)(r % tb);
+}
+
 struct MainArgs {
   int64_t nq, n;
   int d, dp, nkb;
-  int tiles;          // point tiles of BN
-  int64_t work;       // qblocks * tiles
-  int grid;           // CTAs
+  Walk w;
   int smax;           // partial-list slots per query
   int L;              // list capacity (32)
   int depth;          // admission depth = k + margin (<= L)
@@ -310,11 +362,14 @@ __device__ __forceinline__ int64_t chunk_begin(int c, int64_t work, int grid) {
   return muldiv_nn(c, work, grid);
 }
 
-// Step s of CTA c's walk over its range [b0, b1) of (query block, point tile)
-// items.  The walk starts at the range's first item of tile 0 and wraps, so
-// all CTAs stream the same point tiles at the same time (L2 reuse); each query
-// block's items stay contiguous in the walk.
-__device__ __forceinline__ int64_t walk_item(int64_t b0, int64_t b1, int tiles, int64_t s) {
+// Step s of CTA c's walk over its range [b0, b1) of items.  With one band
+// the walk starts at the range's first item of tile 0 and wraps, so all CTAs
+// stream the same point tiles at the same time (L2 reuse); each query block's
+// items stay contiguous in the walk.  With several bands the walk is the
+// range in order (a band fits in L2).
+__device__ __forceinline__ int64_t walk_item(int64_t b0, int64_t b1, const Walk& w, int64_t s) {
+  if (w.nbands > 1) return b0 + s;
+  const int tiles = w.tiles;
   const int64_t f = ((b0 + tiles - 1) / tiles) * tiles;
   if (f >= b1 || f == b0) return b0 + s;
   const int64_t head = b1 - f;
@@ -469,11 +524,13 @@ __device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, u
 }
 
 // Shared-memory footprint of k2_main<CAP, NSETS>.
+template <bool PAIR>
 __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
-  return 1024 /* alignment */ + (size_t)STAGES * STAGE_BYTES +
-         (size_t)nsets * BM * cap * 8 /* lists */ + (2 * STAGES + 4) * 8 + 16;
+  return 1024 /* alignment */ + (size_t)Stg<PAIR>::N * Stg<PAIR>::BYTES +
+         (size_t)nsets * BM * cap * 8 /* lists */ + (2 * Stg<PAIR>::N + 4) * 8 + 16;
 }
-static_assert(k2_smem_bytes(32, 1) <= 232448 && k2_smem_bytes(16, 2) <= 232448, "k2_main shared memory");
+static_assert(k2_smem_bytes<false>(32, 1) <= 232448 && k2_smem_bytes<false>(16, 2) <= 232448, "k2_main shared memory");
+static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2) <= 232448, "k2_main shared memory");
 
 // The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
 // ||q~||^2 is left out: it does not change the row's order).  A point is
@@ -488,15 +545,28 @@ static_assert(k2_smem_bytes(32, 1) <= 232448 && k2_smem_bytes(16, 2) <= 232448, 
 // work (the MMA of the tile after next reuses it one tile-time later); each
 // set keeps its own lists and writes them to its own partial slot.  A list is
 // sorted when it is written out.
-template <int CAP, int NSETS>
+//
+// PAIR: the kernel runs as clusters of two CTAs on two SMs that compute one
+// 256-query x 256-point tile with tcgen05.mma.cta_group::2 (M = 256): CTA
+// rank r stages query rows [128r, 128r + 128) of the pair's block and point
+// rows [128r, 128r + 128) of the tile, so each SM writes and feeds the tensor
+// core 32 KB per K-stage instead of 48 KB; the even CTA's thread issues the
+// MMAs, both CTAs' TMA loads complete on the even CTA's full barrier, its
+// commits arrive on the stage and accumulator barriers of both CTAs, and both
+// CTAs' epilogue warps release an accumulator on the even CTA's barrier.  The
+// work unit (a walk item) is then one pair tile and `a.w.grid` counts pairs.
+template <int CAP, int NSETS, bool PAIR>
 __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
             MainArgs a) {
   constexpr int NEPI = 4 * NSETS;
+  constexpr int STAGES = Stg<PAIR>::N;
+  constexpr int STAGE_BYTES = Stg<PAIR>::BYTES;
+  constexpr int QROWS = PAIR ? 2 * BM : BM;  // query rows of one work unit
   extern __shared__ __align__(1024) uint8_t k2_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(k2_smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* stage_base = smem;                                                   // STAGES * 48 KB
+  uint8_t* stage_base = smem;                                                   // STAGES * STAGE_BYTES
   uint64_t* lists = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);  // [NSETS][CAP][BM]
   uint64_t* bars = lists + NSETS * BM * CAP;
   uint64_t* full_bar = bars;
@@ -506,9 +576,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cta = blockIdx.x;
-  const int64_t it0 = chunk_begin(cta, a.work, a.grid);
-  const int64_t it1 = chunk_begin(cta + 1, a.work, a.grid);
+  const uint32_t rank = PAIR ? ptx::cluster_ctarank() : 0u;
+  const int cta = PAIR ? (int)ptx::cluster_id_x() : (int)blockIdx.x;  // work unit: pair or CTA
+  const int64_t it0 = chunk_begin(cta, a.w.work, a.w.grid);
+  const int64_t it1 = chunk_begin(cta + 1, a.w.work, a.w.grid);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -517,18 +588,27 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(&tfull_bar[b], 1);
-      ptx::mbar_init(&tempty_bar[b], NEPI * 32);
+      // one arrival per epilogue warp of both CTAs (PAIR) or per epilogue thread
+      ptx::mbar_init(&tempty_bar[b], PAIR ? 2 * NEPI : NEPI * 32);
     }
     ptx::fence_mbar_init();
     ptx::prefetch_tensormap(&mapA);
     ptx::prefetch_tensormap(&mapB);
   }
   if (warp == 1) {
-    ptx::tmem_alloc(tmem_slot, TMEM_COLS);
-    ptx::tmem_relinquish();
+    if (PAIR) {
+      ptx::tmem_alloc_pair(tmem_slot, TMEM_COLS);
+      ptx::tmem_relinquish_pair();
+    } else {
+      ptx::tmem_alloc(tmem_slot, TMEM_COLS);
+      ptx::tmem_relinquish();
+    }
   }
   ptx::tc_fence_before();
-  __syncthreads();
+  if (PAIR)
+    ptx::cluster_sync();  // both CTAs' barriers initialised before any cross-CTA arrival
+  else
+    __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
@@ -537,10 +617,11 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     if (lane == 0) {
       uint32_t it = 0;
       bool ok = true;
+      const uint32_t full0 = PAIR ? ptx::mapa(ptx::smem_u32(&full_bar[0]), 0) : 0u;  // even CTA's full_bar[0]
       for (int64_t st = 0; st < it1 - it0 && ok; ++st) {
-        const int64_t item = walk_item(it0, it1, a.tiles, st);
-        const int qb = (int)(item / a.tiles);
-        const int t = (int)(item % a.tiles);
+        const int64_t item = walk_item(it0, it1, a.w, st);
+        int qb, t, band;
+        item_pos(a.w, item, qb, t, band);
         for (int kb = 0; kb < a.nkb; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
@@ -550,23 +631,32 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           }
           uint8_t* sa = stage_base + s * STAGE_BYTES;
           uint8_t* sb = sa + A_STAGE_BYTES;
-          ptx::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-          ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * BK, qb * BM);
-          ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * BK, t * BN);
+          if (PAIR) {
+            if (rank == 0) ptx::mbar_arrive_expect_tx(&full_bar[s], 2 * STAGE_BYTES);
+            const uint32_t fb = full0 + (uint32_t)s * 8u;
+            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * BK, qb * QROWS + (int)rank * BM);
+            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * BK, t * BN + (int)rank * Stg<PAIR>::B_ROWS);
+          } else {
+            ptx::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
+            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * BK, qb * BM);
+            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * BK, t * BN);
+          }
         }
       }
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
-      constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN);
+    if (lane == 0 && rank == 0) {
+      constexpr uint32_t idesc = ptx::idesc_bf16_f32(QROWS, BN);
       uint32_t it = 0;
       int tcount = 0;
       bool ok = true;
       for (int64_t st = 0; st < it1 - it0 && ok; ++st, ++tcount) {
         const int buf = tcount & 1;
         const uint32_t tph = (tcount >> 1) & 1;
-        if (!ptx::mbar_wait(&tempty_bar[buf], tph ^ 1, a.err, ERR_TIMEOUT_MMA)) break;
+        const bool freed = PAIR ? ptx::mbar_wait_cluster(&tempty_bar[buf], tph ^ 1, a.err, ERR_TIMEOUT_MMA)
+                                : ptx::mbar_wait(&tempty_bar[buf], tph ^ 1, a.err, ERR_TIMEOUT_MMA);
+        if (!freed) break;
         ptx::tc_fence_after();
         const uint32_t dcol = tmem_base + (uint32_t)(buf * BN);
         for (int kb = 0; kb < a.nkb; ++kb, ++it) {
@@ -584,11 +674,23 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           for (int kk = 0; kk < ksteps; ++kk) {
             const uint64_t ad = ptx::sw128_desc(sa + kk * 32);
             const uint64_t bd = ptx::sw128_desc(sb + kk * 32);
-            ptx::mma_f16(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            if (PAIR)
+              ptx::mma_f16_pair(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            else
+              ptx::mma_f16(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
           }
-          ptx::mma_commit(&empty_bar[s]);  // frees the stage when these MMAs finish
+          // frees the stage (in both CTAs of a pair) when these MMAs finish
+          if (PAIR)
+            ptx::mma_commit_pair_mc(&empty_bar[s], 0x3);
+          else
+            ptx::mma_commit(&empty_bar[s]);
         }
-        if (ok) ptx::mma_commit(&tfull_bar[buf]);
+        if (ok) {
+          if (PAIR)
+            ptx::mma_commit_pair_mc(&tfull_bar[buf], 0x3);
+          else
+            ptx::mma_commit(&tfull_bar[buf]);
+        }
       }
     }
   } else {
@@ -610,16 +712,18 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 #pragma unroll
     for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
     int tcount = 0;
-    int cur_qb = -1;
-    int seg_first_cta = 0;
+    int cur_qb = -1, cur_band = -1;
+    int seg_slot = 0;
     bool alive = true;
 
     for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
 
     // write the warp's 32 row lists of a finished segment, each sorted across the lanes
+    const int64_t row0 = (int64_t)rank * BM;  // this CTA's rows inside a work unit's query block
+    const uint32_t tempty0 = PAIR ? ptx::mapa(ptx::smem_u32(&tempty_bar[0]), 0) : 0u;
     auto flush = [&](int qb_, int slot_) {
       if (a.seedmode) {
-        const int64_t gq = (int64_t)qb_ * BM + row;
+        const int64_t gq = (int64_t)qb_ * QROWS + row0 + row;
         if (gq < a.nq) {
           uint64_t* dst = a.partial + (gq * a.smax + slot_) * LIST;
 #pragma unroll
@@ -634,7 +738,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       for (int r = 0; r < 32; ++r) {
         uint64_t v = lane < CAP ? wl[lane * BM + r] : KEY_NONE;
         v = warp_sort32(v, lane);
-        const int64_t gq = (int64_t)qb_ * BM + quad * 32 + r;
+        const int64_t gq = (int64_t)qb_ * QROWS + row0 + quad * 32 + r;
         if (gq < a.nq && lane < CAP) a.partial[(gq * a.smax + slot_) * LIST + lane] = v;
       }
       __syncwarp();
@@ -644,8 +748,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     // current tile's in nbc, the next tile's fetched into nbn one tile ahead
     float nbn[BN / 32], nbc[BN / 32];
     auto fetch_norms = [&](int64_t st_) {
-      const int64_t item_ = walk_item(it0, it1, a.tiles, st_);
-      const int64_t c0 = (int64_t)(item_ % a.tiles) * BN;
+      const int64_t item_ = walk_item(it0, it1, a.w, st_);
+      int qb_, t_, b_;
+      item_pos(a.w, item_, qb_, t_, b_);
+      const int64_t c0 = (int64_t)t_ * BN;
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) {
         const int64_t col = c0 + lane + 32 * i;
@@ -654,18 +760,19 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     };
     if (it1 > it0) fetch_norms(0);
     for (int64_t st = 0; st < it1 - it0; ++st, ++tcount) {
-      const int64_t item = walk_item(it0, it1, a.tiles, st);
-      const int qb = (int)(item / a.tiles);
-      const int t = (int)(item % a.tiles);
-      if (qb != cur_qb) {
+      const int64_t item = walk_item(it0, it1, a.w, st);
+      int qb, t, band;
+      item_pos(a.w, item, qb, t, band);
+      if (qb != cur_qb || band != cur_band) {
         if (cur_qb >= 0) {
           // flush the finished segment's lists (every set, even one that saw no candidate)
-          flush(cur_qb, (cta - seg_first_cta) * NSETS + set);
+          flush(cur_qb, seg_slot);
           for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
         }
         cur_qb = qb;
-        seg_first_cta = cta_of((int64_t)qb * a.tiles, a.work, a.grid);
-        const int64_t gq = (int64_t)qb * BM + row;
+        cur_band = band;
+        seg_slot = (band * a.w.span + (cta - cta_of(run_begin(a.w, band, qb), a.w.work, a.w.grid))) * NSETS + set;
+        const int64_t gq = (int64_t)qb * QROWS + row0 + row;
         seed_key = (a.seed != nullptr && gq < a.nq) ? make_key(a.seed[gq], 0u) : KEY_NONE;
         thr_key = seed_key;
         thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
@@ -704,7 +811,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         } else {
           // every TMEM read of this tile is done: hand the buffer back before the last chunk
           ptx::tc_fence_before();
-          ptx::mbar_arrive(&tempty_bar[buf]);
+          if (PAIR) {
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive_cluster(tempty0 + (uint32_t)buf * 8u);
+          } else {
+            ptx::mbar_arrive(&tempty_bar[buf]);
+          }
         }
         if (a.seedmode)
           seed_chunk(vb, pick(nbc, ch + 1), top, (uint32_t)(col0 + (ch + 1) * 32));
@@ -714,14 +826,18 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         ptx::tmem_ld_wait();
       }
     }
-    if (alive && cur_qb >= 0) flush(cur_qb, (cta - seg_first_cta) * NSETS + set);
+    if (alive && cur_qb >= 0) flush(cur_qb, seg_slot);
   }
 
   ptx::tc_fence_before();
   __syncthreads();
+  if (PAIR) ptx::cluster_sync();  // no CTA leaves while the pair's MMAs may touch its memory
   if (warp == 1) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem_base, TMEM_COLS);
+    if (PAIR)
+      ptx::tmem_dealloc_pair(tmem_base, TMEM_COLS);
+    else
+      ptx::tmem_dealloc(tmem_base, TMEM_COLS);
   }
 }
 
@@ -729,20 +845,38 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 
 // The `depth` smallest keys over the CTA segments of each query (warp per
 // query); only the first `depth` entries of every segment list take part.
-__global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int smax, int tiles,
-                         int64_t work, int grid, int depth, int nsets, uint64_t* __restrict__ out) {
+// Segment g of a query enumerates its slots band by band: the CTAs of the
+// (band, query block) run in order, each with its nsets lists.
+__global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int smax, Walk w, int depth,
+                         int nsets, uint64_t* __restrict__ out) {
   constexpr int L = LIST;
   const int lane = threadIdx.x & 31;
   const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (q >= nq) return;
-  const int64_t qb = q / BM;
-  const int c0 = cta_of(qb * tiles, work, grid);
-  const int c1 = cta_of(qb * tiles + tiles - 1, work, grid);
-  const int nseg = (c1 - c0 + 1) * nsets;
-  uint64_t Lr = lane < depth ? partial[(q * smax + 0) * L + lane] : KEY_NONE;
+  const int qb = (int)(q / w.qrows);
+  // slots of this query, at most 64 bands x span x nsets (checked on the host)
+  int nseg = 0;
+  int band_first_slot[64], band_nslots[64];
+  for (int b = 0; b < w.nbands; ++b) {
+    const int64_t r0 = run_begin(w, b, qb);
+    const int c0 = cta_of(r0, w.work, w.grid);
+    const int c1 = cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
+    band_first_slot[b] = b * w.span * nsets;
+    band_nslots[b] = (c1 - c0 + 1) * nsets;
+    nseg += band_nslots[b];
+  }
+  auto slot_of = [&](int g) {
+    int b = 0;
+    while (g >= band_nslots[b]) {
+      g -= band_nslots[b];
+      ++b;
+    }
+    return band_first_slot[b] + g;
+  };
+  uint64_t Lr = lane < depth ? partial[(q * smax + slot_of(0)) * L + lane] : KEY_NONE;
   uint64_t pre[4];  // the next lists, one coalesced load each, issued together
 #pragma unroll
-  for (int u = 0; u < 4; ++u) pre[u] = 1 + u < nseg ? partial[(q * smax + 1 + u) * L + lane] : KEY_NONE;
+  for (int u = 0; u < 4; ++u) pre[u] = 1 + u < nseg ? partial[(q * smax + slot_of(1 + u)) * L + lane] : KEY_NONE;
   for (int g = 1; g < nseg; ++g) {
     // entries then come by shuffle
     uint64_t mine;
@@ -752,7 +886,7 @@ __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int s
       for (int u = 1; u < 4; ++u)
         if (g == 1 + u) mine = pre[u];
     } else {
-      mine = partial[(q * smax + g) * L + lane];
+      mine = partial[(q * smax + slot_of(g)) * L + lane];
     }
     uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
     for (int e = 0; e < depth; ++e) {
@@ -1415,38 +1549,114 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
   return c;
 }
 
+// Launch of one k2_main instance: `units` CTAs, or `units` clusters of two CTAs (PAIR).
+template <int CAP, int NSETS, bool PAIR>
+mann_status launch_k2(const CUtensorMap& mapA, const CUtensorMap& mapB, const MainArgs& ma, int units, size_t smem,
+                      cudaStream_t s) {
+  auto fn = k2_main<CAP, NSETS, PAIR>;
+  MANN_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(PAIR ? 2 * units : units));
+  cfg.blockDim = dim3(64 + 128 * NSETS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  if (PAIR) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  MANN_CUDA_TRY(cudaLaunchKernelEx(&cfg, fn, mapA, mapB, ma));
+  return MANN_OK;
+}
+
+// Clusters of two k2_main CTAs (one per SM) that can be resident at once on
+// this device (0 when pairs cannot run); asked once per context and instance.
+template <int CAP, int NSETS>
+int k2_pair_capacity(Context* ctx) {
+  const uint64_t key = 0xC2A1F00000000000ull | ((uint64_t)CAP << 8) | (uint64_t)NSETS;
+  auto it = ctx->tune.find(key);
+  if (it != ctx->tune.end()) return (int)it->second;
+  int n = 0;
+  auto fn = k2_main<CAP, NSETS, true>;
+  const size_t smem = k2_smem_bytes<true>(CAP, NSETS);
+  if (smem <= ctx->smem_optin &&
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(2 * ctx->num_sms));
+    cfg.blockDim = dim3(64 + 128 * NSETS);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) n = 0;
+  }
+  (void)cudaGetLastError();
+  ctx->tune[key] = (uint64_t)std::max(n, 0);
+  return std::max(n, 0);
+}
+
 // One tensor-core pass (k2_main + k2_merge): the `depth` smallest est' of
 // every query over n points (binfo row p * bstride), as sorted lists [nq][LIST].
-mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
-                          const CUtensorMap& mapB, const RowInfo* qinfo, const RowInfo* binfo,
-                          const float* bnorm, int64_t bstride, int64_t n, int64_t nq, int d, int dp, int depth,
-                          const float* seed, int* err, int slot_partial, int slot_lists, bool timed,
-                          uint64_t** lists_out, int seedmode = 0) {
-  const int64_t qblocks = ceil_div(nq, BM);
-  const int tiles = (int)ceil_div(n, BN);
-  const int64_t work = qblocks * tiles;
-  const int grid = (int)std::min<int64_t>(ctx->num_sms, work);
-  int smax = 1;
-  for (int64_t qb = 0; qb < qblocks; ++qb) {
-    const int c0 = h_cta_of(qb * tiles, work, grid);
-    const int c1 = h_cta_of(qb * tiles + tiles - 1, work, grid);
-    smax = std::max(smax, c1 - c0 + 1);
-  }
+// mapA: the queries' operand (128-row boxes); binfo_map: the points' operand
+// (pass its buffer, rows and row step; the box height follows the form).
+mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA, const void* bxb, int64_t bstride,
+                          const RowInfo* qinfo, const RowInfo* binfo, const float* bnorm, int64_t n, int64_t nq,
+                          int d, int dp, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
+                          bool timed, uint64_t** lists_out, int seedmode = 0) {
   // two epilogue sets with 16-entry lists when the depth allows it; each set
   // writes its own slot
   const int nsets = depth <= 16 ? 2 : 1;
-  smax *= nsets;
+  // CTA pairs (cta_group::2) when there are at least two 128-row query blocks
+  const int pairs = nq > BM ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx)) : 0;
+  const bool pair = pairs >= 1;
+  const int qrows = pair ? 2 * BM : BM;
+  const int64_t qblocks = ceil_div(nq, qrows);
+  const int tiles = (int)ceil_div(n, BN);
+  Walk w;
+  w.tiles = tiles;
+  w.qblocks = (int)qblocks;
+  w.qrows = qrows;
+  w.work = qblocks * tiles;
+  w.grid = (int)std::min<int64_t>(pair ? pairs : ctx->num_sms, w.work);
+  // bands: a point operand above BAND_MIN_BYTES is walked in bands of about
+  // BAND_BYTES so each band stays in L2 while every query block passes over it
+  const double tile_bytes = (double)BN * dp * 2.0;
+  w.band_tiles = tiles;
+  if (bstride == 1 && (double)n * dp * 2.0 > BAND_MIN_BYTES && ceil_div(nq, BM) >= 8)
+    w.band_tiles = std::max(1, std::min(tiles, (int)(BAND_BYTES / tile_bytes)));
+  w.nbands = (int)ceil_div(tiles, w.band_tiles);
+  if (w.nbands > 64) {  // the merge enumerates at most 64 bands
+    w.band_tiles = (int)ceil_div(tiles, 64);
+    w.nbands = (int)ceil_div(tiles, w.band_tiles);
+  }
+  w.span = 1;
+  for (int b = 0; b < w.nbands; ++b)
+    for (int64_t qb = 0; qb < qblocks; ++qb) {
+      const int64_t r0 = run_begin(w, b, (int)qb);
+      const int c0 = h_cta_of(r0, w.work, w.grid);
+      const int c1 = h_cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
+      w.span = std::max(w.span, c1 - c0 + 1);
+    }
+  const int smax = w.nbands * w.span * nsets;
   uint64_t* partial = nullptr;
   MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * smax * LIST, &partial));
+  CUtensorMap mapB;
+  MANN_TRY(make_map(&mapB, bxb, n, dp, pair ? Stg<true>::B_ROWS : Stg<false>::B_ROWS, bstride));
   MainArgs ma;
   ma.nq = nq;
   ma.n = n;
   ma.d = d;
   ma.dp = dp;
   ma.nkb = (int)ceil_div(dp, BK);
-  ma.tiles = tiles;
-  ma.work = work;
-  ma.grid = grid;
+  ma.w = w;
   ma.smax = smax;
   ma.L = LIST;
   ma.depth = depth;
@@ -1458,23 +1668,26 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.partial = partial;
   ma.err = err;
   ma.seedmode = seedmode;
-  const size_t smem = nsets == 2 ? k2_smem_bytes(16, 2) : k2_smem_bytes(32, 1);
+  const size_t smem = pair ? k2_smem_bytes<true>(nsets == 2 ? 16 : 32, nsets)
+                           : k2_smem_bytes<false>(nsets == 2 ? 16 : 32, nsets);
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
-  if (nsets == 2) {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (timed) ctx->time_begin(s);
-    k2_main<16, 2><<<grid, 64 + 256, smem, s>>>(mapA, mapB, ma);
+  if (timed) ctx->time_begin(s);
+  if (pair) {
+    if (nsets == 2)
+      MANN_TRY((launch_k2<16, 2, true>(mapA, mapB, ma, w.grid, smem, s)));
+    else
+      MANN_TRY((launch_k2<32, 1, true>(mapA, mapB, ma, w.grid, smem, s)));
   } else {
-    MANN_CUDA_TRY(cudaFuncSetAttribute(k2_main<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (timed) ctx->time_begin(s);
-    k2_main<32, 1><<<grid, 64 + 128, smem, s>>>(mapA, mapB, ma);
+    if (nsets == 2)
+      MANN_TRY((launch_k2<16, 2, false>(mapA, mapB, ma, w.grid, smem, s)));
+    else
+      MANN_TRY((launch_k2<32, 1, false>(mapA, mapB, ma, w.grid, smem, s)));
   }
   if (timed) ctx->time_end(s);
   MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
   MANN_TRY(ctx->scratch_t(slot_lists, (size_t)nq * LIST, &lists));
-  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, tiles, work, grid, depth,
-                                                     nsets, lists);
+  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, w, depth, nsets, lists);
   MANN_CHECK_LAUNCH();
   *lists_out = lists;
   return MANN_OK;
@@ -1619,10 +1832,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   float* seed = nullptr;
   if (n >= 16 * SEED_SAMPLE) {
     const int64_t bstride = n / SEED_SAMPLE;
-    CUtensorMap mapS;
-    MANN_TRY(make_map(&mapS, B.xb, SEED_SAMPLE, dpe, BN, bstride));
     uint64_t* slists = nullptr;
-    MANN_TRY(run_main_pass(ctx, s, mapA, mapS, Q.info, B.info, B.norms, bstride, SEED_SAMPLE, nq, d, dpe,
+    MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, bstride, Q.info, B.info, B.norms, SEED_SAMPLE, nq, d, dpe,
                            SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
     seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, SEED_DEPTH - 1, seed);
@@ -1630,10 +1841,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   }
 
   // ---- main pass over every point
-  CUtensorMap mapB;
-  MANN_TRY(make_map(&mapB, B.xb, n, dpe, BN));
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, mapB, Q.info, B.info, B.norms, 1, n, nq, d, dpe, depth, seed, err,
+  MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, 1, Q.info, B.info, B.norms, n, nq, d, dpe, depth, seed, err,
                          SLOT_PARTIAL, SLOT_KEYS, true, &lists));
 
   // ---- certify + rerank

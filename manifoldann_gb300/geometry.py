@@ -166,3 +166,53 @@ def compute_edge_weights(rule: AbstractEdgeWeight, data, neighbors, dims=None, b
         rule.code, X.ctypes.data, n, d, nb0.ctypes.data, k, dd.ctypes.data if dd is not None else None,
         bb.ctypes.data if bb is not None else None, maxd, out.ctypes.data, C.byref(neg)))
     return out, int(neg.value)
+
+
+# ---------------------------------------------------------------- weighted graphs
+def candidate_neighbors(index, data, candidate_k: int) -> np.ndarray:
+    """The candidate lists of ``build_weighted_graph_with_candidates``
+    (src/graphs/weighted_knn_graph.jl:497-524): for every node i the 1-based ids
+    of ``query(index, data, x_i, candidate_k + 1)`` without i, the first
+    ``candidate_k`` of them (``_candidates(i)``, :502-509).  That is the kNN
+    graph's own rule (_prepare_neighbors), so all nodes come from one batched
+    self-graph search instead of one query per node.  Returns [n][candidate_k]."""
+    from .graphs import knn_graph_arrays
+
+    ids, _ = knn_graph_arrays(index, data, int(candidate_k))
+    return ids.astype(np.int64) + 1
+
+
+@dataclass
+class WeightedKNNGraph:
+    """``WeightedKNNGraph`` (src/graphs/weighted_knn_graph.jl): the kNN graph
+    (0-based ids [n][k] and distances), every node's fitted geometry in the
+    batched form of ``fit_geometries`` (dims [n], eigenvalues [n][maxd], bases
+    [n][maxd][d]) and the edge weights [n][k]."""
+    graph_ids: np.ndarray
+    graph_dists: np.ndarray
+    dims: np.ndarray
+    eigenvalues: np.ndarray
+    bases: np.ndarray
+    edge_weights: np.ndarray
+    negative_fallbacks: int
+
+
+def build_weighted_graph(method: PCAMethod, index, data, *, k: int, candidate_k: Optional[int] = None,
+                         edge_weight: AbstractEdgeWeight = TangentProjectedSourceOnly()) -> WeightedKNNGraph:
+    """``build_weighted_graph(method, index, data; k, candidate_k, edge_weight)``
+    (weighted_knn_graph.jl:432-463) with ``NoSharing``: the kNN graph with k
+    neighbours; every node's geometry fitted on its graph neighbours, or on its
+    candidate_k candidates when candidate_k > k (:455-461, :482-524); then the
+    edge weights of the graph's edges (:194-236).  Each step is one batched
+    GPU call over all nodes."""
+    from .graphs import knn_graph_arrays
+
+    gi, gd = knn_graph_arrays(index, data, int(k))
+    n = gi.shape[0]
+    if candidate_k is None or candidate_k <= k:
+        nbrs = gi.astype(np.int64) + 1
+    else:
+        nbrs = candidate_neighbors(index, data, candidate_k)
+    dims, eig, bases = fit_geometries(method, data, nbrs, centers=np.arange(n) + 1)
+    w, neg = compute_edge_weights(edge_weight, data, gi.astype(np.int64) + 1, dims, bases)
+    return WeightedKNNGraph(gi, gd, dims, eig, bases, w, neg)

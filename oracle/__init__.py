@@ -35,6 +35,7 @@ _SIGS = {
     "orc_topk_route": (_I32, [_P, _I32, _I32, _I32, _P]),
     "orc_ivf_query_f32": (_I32, [_P, _I32, _P, _P, _I32, _P, _P, _P, _I64, _I32, _I32, _I32, _I32,
                                  _P, _P, _I32]),
+    "orc_ivf_route_gemv_f32": (_I32, [_P, _P, _I32, _I32, _P, _I64, _I32, _I32, _P, _I32]),
     "cpu_bruteforce_batch": (_I32, [_P, _I64, _P, _I64, _I32, _I32, _I32, _P, _P, _I32]),
     "orc_kmeanspp": (_I32, [_P, _I64, _I32, _I32, _I64, _P, _P]),
     "orc_kmeans_lloyd": (_I32, [_P, _I64, _I32, _I32, _P, _I32, C.c_double, _I32, _P, _P, _I32]),
@@ -179,6 +180,29 @@ def ivf_query_f32(data, centroids, centroid_norms, list_offsets, list_ids, queri
                                     nq, k, nprobe, metric, centroid_metric, ids.ctypes.data,
                                     d.ctypes.data, threads))
     return ids, d
+
+
+def ivf_route_gemv_f32(centroids, centroid_norms, queries, nprobe, centroid_metric, threads=0):
+    """Probes [nq][min(nprobe, nlist)] of the reference's IVF routing (GEMV-form
+    centroid distances, then partialsortperm)."""
+    centroids, centroid_norms, queries = map(_f32, (centroids, centroid_norms, queries))
+    nlist = centroids.shape[0]
+    np_ = max(1, min(int(nprobe), nlist))
+    out = np.empty((queries.shape[0], np_), np.int32)
+    _check(load().orc_ivf_route_gemv_f32(centroids.ctypes.data, centroid_norms.ctypes.data, nlist,
+                                         centroids.shape[1], queries.ctypes.data, queries.shape[0], np_,
+                                         centroid_metric, out.ctypes.data, threads))
+    return out
+
+
+def centroid_norms_f32(centroids):
+    """||c||^2 of every centroid row as a sequential FP32 sum of squares (the
+    reference's vec(sum(abs2, centroids; dims=1)), src/indices/ivf_flat.jl:82)."""
+    c = _f32(centroids)
+    out = np.zeros(c.shape[0], np.float32)
+    for i in range(c.shape[1]):
+        out = (out + c[:, i] * c[:, i]).astype(np.float32)
+    return out
 
 
 def ivf_scan_f32(data, list_offsets, list_ids, queries, probes, k, metric, threads=0):

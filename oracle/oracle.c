@@ -634,6 +634,48 @@ static int nb_cmp(const void* a, const void* b) {
   return (x->id > y->id) - (x->id < y->id);
 }
 
+/* _centroid_distances (src/indices/ivf_flat.jl:103-131), GEMV form:
+ * ||c||^2 + ||q||^2 - 2 c.q with the caller's centroid norms, clamped at 0,
+ * sqrt for Euclidean; other metrics per pair. */
+static void centroid_dists_gemv(const float* qv, int32_t d, const float* centroids,
+                                const float* centroid_norms, int32_t nlist, int32_t centroid_metric,
+                                float* cd) {
+  float xn = 0.0f;
+  for (int32_t i = 0; i < d; ++i) xn = fmaf(qv[i], qv[i], xn);
+  for (int32_t c = 0; c < nlist; ++c) {
+    const float* cc = centroids + c * (int64_t)d;
+    if (centroid_metric == ORC_COSINE) {
+      cd[c] = orc_dist_f32(cc, qv, d, ORC_COSINE);
+      continue;
+    }
+    float dot = 0.0f;
+    for (int32_t i = 0; i < d; ++i) dot = fmaf(cc[i], qv[i], dot);
+    float sq = (centroid_norms[c] + xn) - 2.0f * dot;
+    if (!(sq > 0.0f)) sq = (sq != sq) ? sq : 0.0f;
+    cd[c] = centroid_metric == ORC_EUCLIDEAN ? sqrtf(sq) : sq;
+  }
+}
+
+int orc_ivf_route_gemv_f32(const float* centroids, const float* centroid_norms, int32_t nlist,
+                           int32_t d, const float* q, int64_t nq, int32_t nprobe,
+                           int32_t centroid_metric, int32_t* probes, int32_t nthreads) {
+  if (d <= 0 || nlist <= 0) return 2;
+  if (nq <= 0) return 0;
+  int32_t np = nprobe < 1 ? 1 : (nprobe > nlist ? nlist : nprobe);
+  int nt = resolve_threads(nthreads);
+#pragma omp parallel num_threads(nt)
+  {
+    float* cd = (float*)malloc(sizeof(float) * (size_t)nlist);
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t qi = 0; qi < nq; ++qi) {
+      centroid_dists_gemv(q + qi * (int64_t)d, d, centroids, centroid_norms, nlist, centroid_metric, cd);
+      orc_topk_route(cd, nlist, nlist, np, probes + qi * (int64_t)np);
+    }
+    free(cd);
+  }
+  return 0;
+}
+
 int orc_ivf_query_f32(const float* data, int32_t d, const float* centroids,
                       const float* centroid_norms, int32_t nlist, const int64_t* list_offsets,
                       const int32_t* list_ids, const float* q, int64_t nq, int32_t k,
@@ -651,21 +693,7 @@ int orc_ivf_query_f32(const float* data, int32_t d, const float* centroids,
 #pragma omp for schedule(dynamic, 4)
     for (int64_t qi = 0; qi < nq; ++qi) {
       const float* qv = q + qi * (int64_t)d;
-      /* _centroid_distances (ivf_flat.jl:103-131), GEMV form */
-      float xn = 0.0f;
-      for (int32_t i = 0; i < d; ++i) xn = fmaf(qv[i], qv[i], xn);
-      for (int32_t c = 0; c < nlist; ++c) {
-        const float* cc = centroids + c * (int64_t)d;
-        if (centroid_metric == ORC_COSINE) {
-          cd[c] = orc_dist_f32(cc, qv, d, ORC_COSINE);
-          continue;
-        }
-        float dot = 0.0f;
-        for (int32_t i = 0; i < d; ++i) dot = fmaf(cc[i], qv[i], dot);
-        float sq = (centroid_norms[c] + xn) - 2.0f * dot;
-        if (!(sq > 0.0f)) sq = (sq != sq) ? sq : 0.0f;
-        cd[c] = centroid_metric == ORC_EUCLIDEAN ? sqrtf(sq) : sq;
-      }
+      centroid_dists_gemv(qv, d, centroids, centroid_norms, nlist, centroid_metric, cd);
       int32_t got = orc_topk_route(cd, nlist, nlist, np, probe);
       int64_t avail = 0;
       for (int32_t p = 0; p < got; ++p)

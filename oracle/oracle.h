@@ -97,6 +97,13 @@ int orc_kmeans_lloyd(const float* X, int64_t n, int32_t d, int32_t k, float* C, 
 int32_t orc_topk_route(const float* dists, int32_t n_dist, int32_t n_children, int32_t k,
                        int32_t* out);
 
+/* The routing step of that query alone: the nprobe lists of every query by
+ * the GEMV-form centroid distances (ivf_flat.jl:103-131) and partialsortperm
+ * (:150).  probes: [nq][min(nprobe, nlist)]. */
+int orc_ivf_route_gemv_f32(const float* centroids, const float* centroid_norms, int32_t nlist,
+                           int32_t d, const float* q, int64_t nq, int32_t nprobe,
+                           int32_t centroid_metric, int32_t* probes, int32_t nthreads);
+
 /* IVF-Flat query (src/indices/ivf_flat.jl:103-168): SqEuclidean / Euclidean
  * centroid distances in GEMV form, partialsortperm(nprobe), scan of the probed
  * lists into a bounded max-heap (strict < admission) and a final sort by
