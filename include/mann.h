@@ -369,9 +369,14 @@ mann_status mann_measure_fp32_peak(double* out_tflops, double* out_ms);
  * MANN_ENOMEM; buffers already held stay valid).
  * MANN_INJECT_LAUNCH: the next `count` checked kernel launches report a CUDA
  * error (the call returns MANN_ECUDA; the work already enqueued completes).
- * count = 0 clears the kind.  Nothing touches the GPU. */
+ * MANN_INJECT_QUEUE: the next `count` batched-graph calls skip publishing
+ * their device work queue (a producer that never delivers); the persistent
+ * kernel's consumers give up after a short bounded wait and the call returns
+ * MANN_ETIMEOUT with the context still usable.
+ * count = 0 clears the kind.  Arming touches no GPU. */
 #define MANN_INJECT_ALLOC 1
 #define MANN_INJECT_LAUNCH 2
+#define MANN_INJECT_QUEUE 3
 mann_status mann_debug_inject(int32_t kind, int32_t count);
 
 /* Exact kNN in the FP32 form for callers that cannot allocate device memory.

@@ -33,6 +33,7 @@ FLAG_TIME_KERNEL = 2
 FLAG_FP64_ERR = 4
 INJECT_ALLOC = 1
 INJECT_LAUNCH = 2
+INJECT_QUEUE = 3
 
 
 class DimensionMismatch(ValueError):

@@ -1,18 +1,21 @@
 // batched.cu -- kNN graphs of many independent point sets of uneven size in
-// one launch of the segmented FP32 tile kernel, replayed from a captured CUDA
-// graph, with the tile height and split count picked by a measuring autotuner.
+// one persistent launch replayed from a captured CUDA graph, with the tile
+// height and split count picked by a measuring autotuner.
 //
 // Replaces a caller's loop of build_knn_graph(BruteForceIndex, cloud; k)
 // (src/graphs/knn_graph.jl:42-81), one call per cloud: every set's graph has
 // the reference's semantics (k+1 neighbours per point, the point itself
 // dropped wherever it appears, (distance, id) order; ids local to the set).
 //
-// Work items are (set, block of BQ query rows, split of the set's points);
-// they are issued largest first so the longest items start early.  A call
-// runs: [memset of the split lists] -> k1_segmented -> [merge of splits] ->
-// finish (drops the point itself) -> local ids.  The launches of one
-// (buffers, sizes, plan) signature are captured once into a CUDA graph and
-// replayed by later calls.
+// Work items are (set, block of BQ query rows, split of the set's points),
+// largest first, in a device work queue.  A call runs: [memset of the split
+// lists] -> publish (writes the queue header: item count, head 0, the call's
+// epoch) -> k1_persistent (resident CTAs take items through an atomic head
+// until the queue is empty; each waits, bounded, for the header of its epoch)
+// -> [merge of splits] -> finish (drops the point itself) -> local ids.  The
+// launches of one (buffers, sizes, plan) signature are captured once into a
+// CUDA graph and replayed by later calls; the queue's status word is read
+// after every call (MANN_ETIMEOUT when the consumers' wait ran out).
 #include <algorithm>
 #include <cstdio>
 #include <map>
@@ -41,11 +44,24 @@ __global__ void localize_ids_kernel(int32_t* __restrict__ ids, int64_t nrows, in
     if (row[j] >= 0) row[j] -= base;
 }
 
+__global__ void publish_queue_kernel(SegQueue* q, int count, unsigned epoch) {
+  q->head = 0;
+  q->count = count;
+  q->status = 0;
+  __threadfence();
+  q->epoch = epoch;
+}
+
 struct Plan {
   int bq = 128, S = 1;
   std::vector<SegItem> items;
   uint64_t hash = 0;
 };
+
+// the consumers' wait for a published queue: about a second at 2 GHz
+constexpr long long QUEUE_WAIT_CYCLES = 1ll << 31;
+// with an injected dropped publish: about 50 us
+constexpr long long QUEUE_WAIT_CYCLES_SHORT = 100000;
 
 constexpr int64_t MIN_SPLIT_POINTS = 8192;
 
@@ -88,6 +104,7 @@ struct Bufs {
   int64_t* offs = nullptr;
   uint64_t* partial = nullptr;
   uint64_t* keys = nullptr;
+  SegQueue* queue = nullptr;
 };
 
 struct Shape {
@@ -99,15 +116,19 @@ struct Shape {
 };
 
 // The launches of one call (no allocation, no synchronisation: capturable).
-mann_status issue(const Shape& sh, const Plan& pl, const Bufs& b, cudaStream_t s) {
+// `publish` = false leaves the queue unpublished (injected dropped publish);
+// the consumers then give up after `wait_cycles`.
+mann_status issue(int num_sms, const Shape& sh, const Plan& pl, const Bufs& b, unsigned epoch, bool publish,
+                  long long wait_cycles, cudaStream_t s) {
   const int nitems = (int)pl.items.size();
-  if (pl.S > 1) {
-    MANN_CUDA_TRY(cudaMemsetAsync(b.partial, 0xFF, sizeof(uint64_t) * sh.N * pl.S * sh.kk, s));
-    MANN_TRY(launch_k1_segmented(sh.data, b.items, nitems, sh.d, sh.metric, pl.bq, sh.kk, pl.S, b.partial, s));
-    MANN_TRY(launch_merge_lists(b.partial, sh.N, pl.S, sh.kk, b.keys, s));
-  } else {
-    MANN_TRY(launch_k1_segmented(sh.data, b.items, nitems, sh.d, sh.metric, pl.bq, sh.kk, 1, b.keys, s));
+  if (pl.S > 1) MANN_CUDA_TRY(cudaMemsetAsync(b.partial, 0xFF, sizeof(uint64_t) * sh.N * pl.S * sh.kk, s));
+  if (publish) {
+    publish_queue_kernel<<<1, 1, 0, s>>>(b.queue, nitems, epoch);
+    MANN_CHECK_LAUNCH();
   }
+  MANN_TRY(launch_k1_persistent(num_sms, sh.data, b.items, b.queue, epoch, wait_cycles, sh.d, sh.metric, pl.bq,
+                                sh.kk, pl.S, pl.S > 1 ? b.partial : b.keys, s));
+  if (pl.S > 1) MANN_TRY(launch_merge_lists(b.partial, sh.N, pl.S, sh.kk, b.keys, s));
   MANN_TRY(launch_finish(b.keys, sh.N, sh.kk, sh.k, sh.include_self ? -1 : 0, nullptr, sh.ids, sh.dists, s));
   localize_ids_kernel<<<(unsigned)ceil_div(sh.N, 256), 256, 0, s>>>(sh.ids, sh.N, sh.k, b.offs, sh.nsets);
   MANN_CHECK_LAUNCH();
@@ -117,6 +138,7 @@ mann_status issue(const Shape& sh, const Plan& pl, const Bufs& b, cudaStream_t s
 struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   uint64_t last_use = 0;
+  unsigned epoch = 0;
 };
 
 struct BatchState {
@@ -127,6 +149,7 @@ struct BatchState {
   cudaStream_t cap = nullptr;
   const void* uploaded_items = nullptr;  // device buffer holding the plan with hash uploaded_hash
   uint64_t uploaded_hash = 0;
+  unsigned epoch = 0;  // last epoch handed to a queue
 };
 
 BatchState& state_of(Context* ctx) {
@@ -145,6 +168,7 @@ mann_status prepare(Context* ctx, cudaStream_t s, const Shape& sh, const int64_t
   MANN_TRY(ctx->scratch_t(SLOT_BATCH_ITEMS, std::max<size_t>(pl.items.size(), 1), &b->items));
   MANN_TRY(ctx->scratch_t(SLOT_BATCH_OFFS, (size_t)sh.nsets + 1, &b->offs));
   MANN_TRY(ctx->scratch_t(SLOT_KEYS, (size_t)sh.N * sh.kk, &b->keys));
+  MANN_TRY(ctx->scratch_t(SLOT_BATCH_QUEUE, 1, &b->queue));
   if (pl.S > 1) MANN_TRY(ctx->scratch_t(SLOT_PARTIAL, (size_t)sh.N * pl.S * sh.kk, &b->partial));
   if (st.uploaded_items != b->items || st.uploaded_hash != pl.hash) {
     MANN_CUDA_TRY(cudaMemcpyAsync(b->items, pl.items.data(), sizeof(SegItem) * pl.items.size(),
@@ -160,9 +184,9 @@ mann_status prepare(Context* ctx, cudaStream_t s, const Shape& sh, const int64_t
 
 std::string graph_key(const Shape& sh, const Plan& pl, const Bufs& b) {
   char buf[512];
-  snprintf(buf, sizeof(buf), "%p|%lld|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%d|%d|%llu|%zu", (const void*)sh.data,
+  snprintf(buf, sizeof(buf), "%p|%lld|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%d|%llu|%zu", (const void*)sh.data,
            (long long)sh.N, sh.nsets, sh.d, sh.metric, sh.k, sh.include_self, (void*)sh.ids, (void*)sh.dists,
-           (void*)b.items, (void*)b.offs, (void*)b.partial, (void*)b.keys, pl.bq, pl.S,
+           (void*)b.items, (void*)b.offs, (void*)b.partial, (void*)b.keys, (void*)b.queue, pl.bq, pl.S,
            (unsigned long long)pl.hash, pl.items.size());
   return buf;
 }
@@ -173,11 +197,13 @@ mann_status run_graph(Context* ctx, cudaStream_t s, const Shape& sh, const Plan&
   auto it = st.graphs.find(key);
   if (it == st.graphs.end()) {
     // captured on the library's own stream (the caller's may be the legacy
-    // default stream, which cannot be captured); replayed on the caller's
+    // default stream, which cannot be captured); replayed on the caller's.
+    // The graph's publish and consumers share its own epoch.
     if (!st.cap) MANN_CUDA_TRY(cudaStreamCreateWithFlags(&st.cap, cudaStreamNonBlocking));
+    const unsigned epoch = ++st.epoch;
     cudaGraph_t g = nullptr;
     MANN_CUDA_TRY(cudaStreamBeginCapture(st.cap, cudaStreamCaptureModeThreadLocal));
-    const mann_status rc = issue(sh, pl, b, st.cap);
+    const mann_status rc = issue(ctx->num_sms, sh, pl, b, epoch, true, QUEUE_WAIT_CYCLES, st.cap);
     const cudaError_t ce = cudaStreamEndCapture(st.cap, &g);
     if (rc != MANN_OK) {
       if (g) cudaGraphDestroy(g);
@@ -195,11 +221,23 @@ mann_status run_graph(Context* ctx, cudaStream_t s, const Shape& sh, const Plan&
       cudaGraphExecDestroy(victim->second.exec);
       st.graphs.erase(victim);
     }
-    it = st.graphs.emplace(key, GraphEntry{exec, 0}).first;
+    it = st.graphs.emplace(key, GraphEntry{exec, 0, epoch}).first;
   }
   it->second.last_use = ++st.clock;
   MANN_CUDA_TRY(cudaGraphLaunch(it->second.exec, s));
-  for (int i = 0; i < (pl.S > 1 ? 4 : 3); ++i) note_launch();  // kernels in the graph
+  for (int i = 0; i < (pl.S > 1 ? 5 : 4); ++i) note_launch();  // kernels in the graph
+  return MANN_OK;
+}
+
+// The queue's status word after the call's kernels: MANN_ETIMEOUT when the
+// consumers' wait for a published queue ran out.
+mann_status check_queue(const Bufs& b, cudaStream_t s) {
+  int h = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(&h, &b.queue->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h != 0)
+    return fail(MANN_ETIMEOUT, "batched graphs: the work queue was not published before the consumers' "
+                               "bounded wait ran out");
   return MANN_OK;
 }
 
@@ -212,7 +250,7 @@ mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_kn
     return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
   const int k = p->k;
   Shape sh{data, offs[nsets], nsets, d, p->metric, k, include_self ? k : k + 1, include_self ? 1 : 0, ids, dists};
-  if (sh.kk > 32) return fail(MANN_EINVAL_ARG, "batched graphs support k <= 31 (32 with include_self)");
+  if (sh.kk > 64) return fail(MANN_EINVAL_ARG, "batched graphs support k <= 63 (64 with include_self)");
   BatchState& st = state_of(ctx);
   std::lock_guard<std::mutex> lk(st.mu);
   char sig[128];
@@ -221,20 +259,25 @@ mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_kn
   Plan pl;
   Bufs b;
   if (tuned == st.tuned.end()) {
-    // measure every candidate once on this call's data (each run writes the full result)
-    static const int cand[][2] = {{128, 1}, {64, 1}, {128, 2}, {128, 4}};
+    // measure every candidate once on this call's data (each run writes the
+    // full result): tile heights (64-row tiles for k+1 > 32) x point splits
+    static const int cand32[][2] = {{128, 1}, {64, 1}, {128, 2}, {64, 2}, {128, 4}};
+    static const int cand64[][2] = {{64, 1}, {32, 1}, {64, 2}, {64, 4}};
+    const int ncand = sh.kk > 32 ? 4 : 5;
     float best = 1e30f;
-    std::pair<int, int> pick{128, 1};
+    std::pair<int, int> pick{sh.kk > 32 ? 64 : 128, 1};
     cudaEvent_t e0, e1;
     MANN_CUDA_TRY(cudaEventCreate(&e0));
     MANN_CUDA_TRY(cudaEventCreate(&e1));
-    for (const auto& c : cand) {
+    for (int ci = 0; ci < ncand; ++ci) {
+      const int* c = sh.kk > 32 ? cand64[ci] : cand32[ci];
       make_plan(offs, nsets, c[0], c[1], &pl);
       MANN_TRY(prepare(ctx, s, sh, offs, pl, &b, st));
       cudaEventRecord(e0, s);
-      MANN_TRY(issue(sh, pl, b, s));
+      MANN_TRY(issue(ctx->num_sms, sh, pl, b, ++st.epoch, true, QUEUE_WAIT_CYCLES, s));
       cudaEventRecord(e1, s);
       MANN_CUDA_TRY(cudaEventSynchronize(e1));
+      MANN_TRY(check_queue(b, s));
       float ms = 0.0f;
       cudaEventElapsedTime(&ms, e0, e1);
       if (ms < best) {
@@ -249,10 +292,16 @@ mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_kn
   make_plan(offs, nsets, tuned->second.first, tuned->second.second, &pl);
   MANN_TRY(prepare(ctx, s, sh, offs, pl, &b, st));
   if (rep) rep->margin_used = pl.bq * 100 + pl.S;  // chosen configuration: tile height * 100 + splits
+  if (injected_dropped_publish()) {
+    // the queue's producer "fails": the consumers find no published queue and
+    // return MANN_ETIMEOUT after a short bounded wait (no kernel is left waiting)
+    MANN_TRY(issue(ctx->num_sms, sh, pl, b, ++st.epoch, false, QUEUE_WAIT_CYCLES_SHORT, s));
+    return check_queue(b, s);
+  }
   ctx->time_begin(s);
   MANN_TRY(run_graph(ctx, s, sh, pl, b, st));
   ctx->time_end(s);
-  return MANN_OK;
+  return check_queue(b, s);
 }
 
 }  // namespace mann

@@ -19,6 +19,8 @@ void clear_error();
 void note_launch();
 // true once per failure requested through mann_debug_inject(MANN_INJECT_LAUNCH, n)
 bool injected_launch_error();
+// true once per dropped queue publish requested through mann_debug_inject(MANN_INJECT_QUEUE, n)
+bool injected_dropped_publish();
 int64_t launch_count();
 
 struct Status {

@@ -14,6 +14,7 @@ std::unique_ptr<Context> g_ctx[64];
 // host-side fault injection (mann_debug_inject): pending failures per kind
 std::atomic<int> g_inject_alloc{0};
 std::atomic<int> g_inject_launch{0};
+std::atomic<int> g_inject_queue{0};
 
 // true once for each pending injected failure of `counter`
 bool take_injected(std::atomic<int>& counter) {
@@ -28,6 +29,7 @@ void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 void note_launch() { ++g_launches; }
 bool injected_launch_error() { return take_injected(g_inject_launch); }
+bool injected_dropped_publish() { return take_injected(g_inject_queue); }
 int64_t launch_count() { return g_launches; }
 const char* last_error_cstr() { return g_last_error.c_str(); }
 
@@ -118,6 +120,8 @@ extern "C" mann_status mann_debug_inject(int32_t kind, int32_t count) {
     mann::g_inject_alloc.store(count);
   } else if (kind == MANN_INJECT_LAUNCH) {
     mann::g_inject_launch.store(count);
+  } else if (kind == MANN_INJECT_QUEUE) {
+    mann::g_inject_queue.store(count);
   } else {
     return mann::fail(MANN_EINVAL_ARG, "unknown injection kind");
   }

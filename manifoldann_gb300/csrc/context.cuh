@@ -71,6 +71,7 @@ enum ScratchSlot : int {
   SLOT_PROBE_D,       // learned probe: squared distances to the centroids
   SLOT_BATCH_ITEMS,   // batched graphs: work items
   SLOT_BATCH_OFFS,    // batched graphs: set offsets
+  SLOT_BATCH_QUEUE,   // batched graphs: work-queue header
   SLOT_COS_B,         // BF16 cosine: unit-normalised points
   SLOT_COS_Q,         // BF16 cosine: unit-normalised queries
   SLOT_COS_NB,        // BF16 cosine: squared norms of the points

@@ -79,8 +79,21 @@ struct SegItem {
   int64_t q0, qend, nb0, nb1;
   int32_t split, pad;
 };
-mann_status launch_k1_segmented(const float* data, const SegItem* items, int nitems, int d, int metric, int bq,
-                                int k, int nsplit, uint64_t* partial, cudaStream_t s);
+// Device work queue of the persistent segmented kernel: `count` items, taken
+// in order through the atomic `head`; `epoch` publishes the queue of one call
+// (consumers wait, bounded, for it); `status` receives MANN_ETIMEOUT when
+// that wait runs out.
+struct SegQueue {
+  unsigned long long head;
+  int count;
+  unsigned epoch;
+  int status;
+  int pad[3];
+};
+// Persistent segmented kernel: resident CTAs consume the items of `q` (k <= 64).
+mann_status launch_k1_persistent(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
+                                 long long wait_cycles, int d, int metric, int bq, int k, int nsplit,
+                                 uint64_t* partial, cudaStream_t s);
 mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_knn_params* p, const float* data,
                                      const int64_t* offs, int nsets, int d, int include_self, int32_t* ids,
                                      float* dists, mann_knn_report* rep);

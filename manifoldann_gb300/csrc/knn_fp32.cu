@@ -329,19 +329,54 @@ __global__ void __launch_bounds__(K1_THREADS, 1)
                                reinterpret_cast<float*>(k1_smem));
 }
 
-// Segmented form: one launch over the work items of many independent point
-// sets stored back to back; item i covers queries [q0, qend) of one set
-// against that set's points [nb0, nb1) (global rows, so the keys carry global
-// ids), writing split slot `split` of each query's lists.
-template <int METRIC, int BQ, bool VEC>
+// Segmented persistent form over a device work queue: the work items of many
+// independent point sets stored back to back -- item i covers queries
+// [q0, qend) of one set against that set's points [nb0, nb1) (global rows,
+// so the keys carry global ids) and writes split slot `split` of each
+// query's lists.  A grid of resident CTAs takes the items (largest first) from the queue
+// by an atomic counter until the queue is exhausted.  Before taking work a
+// CTA waits until the queue of this call is published (q->epoch == epoch,
+// written with the plan ahead of the kernel in stream order); the wait is
+// bounded by `wait_cycles`, after which the CTA records MANN_ETIMEOUT in
+// q->status and returns without touching any list.
+template <int METRIC, int BQ, int KW, bool VEC>
 __global__ void __launch_bounds__(K1_THREADS, 2)
-    k1_segmented(const float* __restrict__ data, const SegItem* __restrict__ items, int d, int k, int nsplit,
-                 uint64_t* __restrict__ partial) {
+    k1_persistent(const float* __restrict__ data, const SegItem* __restrict__ items, SegQueue* q, unsigned epoch,
+                  long long wait_cycles, int d, int k, int nsplit, uint64_t* __restrict__ partial) {
   extern __shared__ float4 k1_smem[];
-  const SegItem it = items[blockIdx.x];
-  k1_body<METRIC, BQ, 1, VEC>(data, it.nb0, it.nb1, data, nullptr, it.q0, it.qend, d, nullptr, nullptr, k,
-                              partial + (int64_t)it.split * k, (int64_t)nsplit * k,
-                              reinterpret_cast<float*>(k1_smem));
+  __shared__ int s_item;
+  __shared__ int s_count;
+  if (threadIdx.x == 0) {
+    volatile SegQueue* vq = q;
+    const long long t0 = clock64();
+    int ok = 1;
+    while (vq->epoch != epoch) {
+      if (clock64() - t0 > wait_cycles) {
+        atomicCAS(&q->status, 0, (int)MANN_ETIMEOUT);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_count = ok ? vq->count : 0;
+  }
+  __syncthreads();
+  const int count = s_count;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const unsigned long long i = atomicAdd(&q->head, 1ull);
+      s_item = i < (unsigned long long)count ? (int)i : -1;
+    }
+    __syncthreads();
+    const int idx = s_item;
+    if (idx < 0) break;
+    const SegItem it = items[idx];
+    k1_body<METRIC, BQ, KW, VEC>(data, it.nb0, it.nb1, data, nullptr, it.q0, it.qend, d, nullptr, nullptr, k,
+                                 partial + (int64_t)it.split * k, (int64_t)nsplit * k,
+                                 reinterpret_cast<float*>(k1_smem));
+    __syncthreads();  // s_item is rewritten only after every thread read it
+  }
 }
 
 // Exact FP32 scan for a handful of query rows (nq <= 32, e.g. the rows the
@@ -592,37 +627,48 @@ mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const
 
 }  // namespace
 
-template <int METRIC, int BQ, bool VEC>
-static mann_status launch_seg_t(const float* data, const SegItem* items, int nitems, int d, int k, int nsplit,
-                                uint64_t* partial, cudaStream_t s) {
+template <int METRIC, int BQ, int KW, bool VEC>
+static mann_status launch_pers_t(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
+                                 long long wait_cycles, int d, int k, int nsplit, uint64_t* partial, cudaStream_t s) {
   constexpr int QSTR = BQ + 4, BSTR = K1_BN + 4;
   const size_t smem = sizeof(float) * (2 * K1_DK * QSTR + 2 * K1_DK * BSTR + BQ * BSTR);
-  auto kern = k1_segmented<METRIC, BQ, VEC>;
+  auto kern = k1_persistent<METRIC, BQ, KW, VEC>;
   MANN_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)nitems, K1_THREADS, smem, s>>>(data, items, d, k, nsplit, partial);
+  int per_sm = 0;
+  MANN_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, K1_THREADS, smem));
+  const int grid = std::max(1, per_sm) * num_sms;  // every CTA resident: the queue needs no co-scheduling
+  kern<<<(unsigned)grid, K1_THREADS, smem, s>>>(data, items, q, epoch, wait_cycles, d, k, nsplit, partial);
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
-mann_status launch_k1_segmented(const float* data, const SegItem* items, int nitems, int d, int metric, int bq,
-                                int k, int nsplit, uint64_t* partial, cudaStream_t s) {
-  if (k < 1 || k > 32) return fail(MANN_EINVAL_ARG, "batched graphs support 1 <= k <= 32 (k+1 with self)");
-  if (nitems <= 0) return MANN_OK;
+mann_status launch_k1_persistent(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
+                                 long long wait_cycles, int d, int metric, int bq, int k, int nsplit,
+                                 uint64_t* partial, cudaStream_t s) {
+  if (k < 1 || k > 64) return fail(MANN_EINVAL_ARG, "batched graphs support 1 <= k <= 64 (k+1 with self)");
   const bool vec = (d % 4) == 0;
-#define SEG_CASE(M, B)                                                                       \
-  return vec ? launch_seg_t<M, B, true>(data, items, nitems, d, k, nsplit, partial, s)       \
-             : launch_seg_t<M, B, false>(data, items, nitems, d, k, nsplit, partial, s)
+#define PERS_CASE(M, B, KW)                                                                                      \
+  return vec ? launch_pers_t<M, B, KW, true>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, s) \
+             : launch_pers_t<M, B, KW, false>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, s)
   if (metric == MANN_METRIC_EUCLIDEAN) {
-    if (bq == 64) SEG_CASE(MANN_METRIC_EUCLIDEAN, 64);
-    if (bq == 32) SEG_CASE(MANN_METRIC_EUCLIDEAN, 32);
-    SEG_CASE(MANN_METRIC_EUCLIDEAN, 128);
+    if (k > 32) {
+      if (bq == 32) PERS_CASE(MANN_METRIC_EUCLIDEAN, 32, 2);
+      PERS_CASE(MANN_METRIC_EUCLIDEAN, 64, 2);
+    }
+    if (bq == 64) PERS_CASE(MANN_METRIC_EUCLIDEAN, 64, 1);
+    if (bq == 32) PERS_CASE(MANN_METRIC_EUCLIDEAN, 32, 1);
+    PERS_CASE(MANN_METRIC_EUCLIDEAN, 128, 1);
   }
   if (metric == MANN_METRIC_SQEUCLIDEAN) {
-    if (bq == 64) SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 64);
-    if (bq == 32) SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 32);
-    SEG_CASE(MANN_METRIC_SQEUCLIDEAN, 128);
+    if (k > 32) {
+      if (bq == 32) PERS_CASE(MANN_METRIC_SQEUCLIDEAN, 32, 2);
+      PERS_CASE(MANN_METRIC_SQEUCLIDEAN, 64, 2);
+    }
+    if (bq == 64) PERS_CASE(MANN_METRIC_SQEUCLIDEAN, 64, 1);
+    if (bq == 32) PERS_CASE(MANN_METRIC_SQEUCLIDEAN, 32, 1);
+    PERS_CASE(MANN_METRIC_SQEUCLIDEAN, 128, 1);
   }
-#undef SEG_CASE
+#undef PERS_CASE
   return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
 }
 

@@ -1,7 +1,8 @@
-"""Batched kNN graphs of many uneven point sets in one launch (replayed from a
-captured CUDA graph): every set's graph equals the oracle's build_knn_graph of
-that set alone (ids and distance bits), at full size it equals the one-set
-GPU graph of each cloud, and graph replays and re-plans give the same bytes."""
+"""Batched kNN graphs of many uneven point sets in one persistent launch over
+a device work queue (replayed from a captured CUDA graph): every set's graph
+equals the oracle's build_knn_graph of that set alone (ids and distance bits,
+k + 1 up to 64), at full size it equals the one-set GPU graph of each cloud,
+and graph replays and re-plans give the same bytes."""
 import numpy as np
 import pytest
 
@@ -14,7 +15,8 @@ def _clouds(count, lo, hi, d, seed):
     return synthetic.manifold_clouds(count, lo, hi, d, seed=seed)
 
 
-@pytest.mark.parametrize("metric,d,k,include_self", [(1, 32, 15, False), (0, 7, 5, True), (1, 12, 31, False)])
+@pytest.mark.parametrize("metric,d,k,include_self", [(1, 32, 15, False), (0, 7, 5, True), (1, 12, 31, False),
+                                                    (1, 32, 40, False), (0, 9, 64, True), (1, 32, 63, False)])
 def test_batched_graphs_equal_oracle_per_set(gpu_lib, orc, metric, d, k, include_self):
     import manifoldann_gb300 as M
 
