@@ -44,9 +44,9 @@ __global__ void localize_ids_kernel(int32_t* __restrict__ ids, int64_t nrows, in
     if (row[j] >= 0) row[j] -= base;
 }
 
-__global__ void publish_queue_kernel(SegQueue* q, int count, unsigned epoch) {
+__global__ void publish_queue_kernel(SegQueue* q, int count, const int* count_dev, unsigned epoch) {
   q->head = 0;
-  q->count = count;
+  q->count = count_dev ? *count_dev : count;
   q->status = 0;
   __threadfence();
   q->epoch = epoch;
@@ -122,10 +122,7 @@ mann_status issue(int num_sms, const Shape& sh, const Plan& pl, const Bufs& b, u
                   long long wait_cycles, cudaStream_t s) {
   const int nitems = (int)pl.items.size();
   if (pl.S > 1) MANN_CUDA_TRY(cudaMemsetAsync(b.partial, 0xFF, sizeof(uint64_t) * sh.N * pl.S * sh.kk, s));
-  if (publish) {
-    publish_queue_kernel<<<1, 1, 0, s>>>(b.queue, nitems, epoch);
-    MANN_CHECK_LAUNCH();
-  }
+  if (publish) MANN_TRY(launch_publish_queue(b.queue, nitems, nullptr, epoch, s));
   MANN_TRY(launch_k1_persistent(num_sms, sh.data, b.items, b.queue, epoch, wait_cycles, sh.d, sh.metric, pl.bq,
                                 sh.kk, pl.S, pl.S > 1 ? b.partial : b.keys, s));
   if (pl.S > 1) MANN_TRY(launch_merge_lists(b.partial, sh.N, pl.S, sh.kk, b.keys, s));
@@ -243,6 +240,12 @@ mann_status check_queue(const Bufs& b, cudaStream_t s) {
 
 }  // namespace
 
+mann_status launch_publish_queue(SegQueue* q, int count, const int* count_dev, unsigned epoch, cudaStream_t s) {
+  publish_queue_kernel<<<1, 1, 0, s>>>(q, count, count_dev, epoch);
+  MANN_CHECK_LAUNCH();
+  return MANN_OK;
+}
+
 mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_knn_params* p, const float* data,
                                      const int64_t* offs, int nsets, int d, int include_self, int32_t* ids,
                                      float* dists, mann_knn_report* rep) {
@@ -250,6 +253,23 @@ mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_kn
     return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
   const int k = p->k;
   Shape sh{data, offs[nsets], nsets, d, p->metric, k, include_self ? k : k + 1, include_self ? 1 : 0, ids, dists};
+  if (p->precision == MANN_PREC_BF16) {
+    // the BF16 tensor-core form: one segmented pass over every set's (block, tile) items
+    int64_t* offs_dev = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_BATCH_OFFS, (size_t)nsets + 1, &offs_dev));
+    MANN_CUDA_TRY(cudaMemcpyAsync(offs_dev, offs, sizeof(int64_t) * (nsets + 1), cudaMemcpyHostToDevice, s));
+    uint64_t* keys = nullptr;
+    ctx->time_begin(s);
+    MANN_TRY(knn_bf16_batched_keys(ctx, s, data, offs, offs_dev, nsets, d, p->metric, sh.kk, p->margin, &keys, rep));
+    ctx->time_end(s);
+    MANN_TRY(launch_finish(keys, sh.N, sh.kk, k, include_self ? -1 : 0, nullptr, ids, dists, s));
+    localize_ids_kernel<<<(unsigned)ceil_div(sh.N, 256), 256, 0, s>>>(ids, sh.N, k, offs_dev, nsets);
+    MANN_CHECK_LAUNCH();
+    BatchState& st = state_of(ctx);
+    std::lock_guard<std::mutex> lk(st.mu);
+    st.uploaded_items = nullptr;  // the offsets buffer was rewritten: the FP32 plan re-uploads
+    return MANN_OK;
+  }
   if (sh.kk > 64) return fail(MANN_EINVAL_ARG, "batched graphs support k <= 63 (64 with include_self)");
   BatchState& st = state_of(ctx);
   std::lock_guard<std::mutex> lk(st.mu);

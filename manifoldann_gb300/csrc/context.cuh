@@ -72,6 +72,10 @@ enum ScratchSlot : int {
   SLOT_BATCH_ITEMS,   // batched graphs: work items
   SLOT_BATCH_OFFS,    // batched graphs: set offsets
   SLOT_BATCH_QUEUE,   // batched graphs: work-queue header
+  SLOT_SEG_ITEMS,     // batched BF16 graphs: (set, block, tile) items
+  SLOT_SEG_RUNS,      // batched BF16 graphs: the items of each block
+  SLOT_SEG_ROWRUN,    // batched BF16 graphs: each row's block
+  SLOT_SEG_QUEUE,     // batched BF16 graphs: fallback work-queue header
   SLOT_COS_B,         // BF16 cosine: unit-normalised points
   SLOT_COS_Q,         // BF16 cosine: unit-normalised queries
   SLOT_COS_NB,        // BF16 cosine: squared norms of the points

@@ -33,6 +33,13 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
                           bool fp64, uint64_t** out_keys, mann_knn_report* rep);
 
+// Self-kNN keys [N][kreq] (global ids, the row itself included) of many point
+// sets stored back to back (set c = rows [offs[c], offs[c+1])), each against
+// its own points, in the BF16 form (offs on the host and on the device).
+mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* data, const int64_t* offs_host,
+                                  const int64_t* offs_dev, int nsets, int d, int metric, int kreq, int margin,
+                                  uint64_t** out_keys, mann_knn_report* rep);
+
 // Orders near-ties of sorted FP32 candidate lists by FP64 distance (when fp64)
 // and truncates them to kreq keys.  counters[0] += rows re-ordered,
 // counters[1] += rows whose boundary tie could not be settled (their query
@@ -91,9 +98,14 @@ struct SegQueue {
   int pad[3];
 };
 // Persistent segmented kernel: resident CTAs consume the items of `q` (k <= 64).
+// `qrows` (optional) maps an item's query index i to the query row qrows[i]
+// (the lists still go to slot i).
 mann_status launch_k1_persistent(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
                                  long long wait_cycles, int d, int metric, int bq, int k, int nsplit,
-                                 uint64_t* partial, cudaStream_t s);
+                                 uint64_t* partial, cudaStream_t s, const int32_t* qrows = nullptr);
+// Publishes a work queue of `count` items (head 0, status 0, then the epoch).
+// count_dev (optional) supplies the count from device memory instead.
+mann_status launch_publish_queue(SegQueue* q, int count, const int* count_dev, unsigned epoch, cudaStream_t s);
 mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_knn_params* p, const float* data,
                                      const int64_t* offs, int nsets, int d, int include_self, int32_t* ids,
                                      float* dists, mann_knn_report* rep);

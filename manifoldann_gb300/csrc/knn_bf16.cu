@@ -39,7 +39,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 #include "ptx.cuh"
@@ -331,10 +333,27 @@ __host__ __device__ __forceinline__ void item_pos(const Walk& w, int64_t i, int&
   t = b * w.band_tiles + (int)(r % tb);
 }
 
+// Work item of a segmented pass (many independent point sets stored back to
+// back, each searched against itself): a 128-row block of one set's rows
+// against a 256-point tile of the same set's points.  Columns at or past
+// `tend` and rows at or past `qend` belong to other sets and are masked.
+// The items of one block are contiguous; `run_first` is the first of them.
+struct TileItem {
+  int64_t q0, qend;   // first row of the block; end of its set's rows
+  int64_t t0, tend;   // first point of the tile; end of its set's points
+  int64_t run_first;  // first item of this block's run
+};
+
+// a block's run of items: first item and count (segmented merge)
+struct RunInfo {
+  int64_t first, len;
+};
+
 struct MainArgs {
   int64_t nq, n;
   int d, dp, nkb;
   Walk w;
+  const TileItem* titems;  // segmented pass (NULL: the banded walk of `w`)
   int smax;           // partial-list slots per query
   int L;              // list capacity (32)
   int depth;          // admission depth = k + margin (<= L)
@@ -347,6 +366,36 @@ struct MainArgs {
   int* err;
   int seedmode;       // keep the SEED_DEPTH smallest 32-column chunk minima instead of points
 };
+
+// What one item means for the kernel's roles: rows [q0, qend), points
+// [c0, cend), and where its block's run starts (segment identity and slot).
+struct ItemView {
+  int64_t q0, qend, c0, cend, run_first;
+  int slot_base;  // band * span (banded walk), 0 (segmented)
+};
+
+__device__ __forceinline__ ItemView view_item(const MainArgs& a, int64_t item, int qrows) {
+  ItemView v;
+  if (a.titems) {
+    const TileItem ti = a.titems[item];
+    v.q0 = ti.q0;
+    v.qend = ti.qend;
+    v.c0 = ti.t0;
+    v.cend = ti.tend;
+    v.run_first = ti.run_first;
+    v.slot_base = 0;
+  } else {
+    int qb, t, band;
+    item_pos(a.w, item, qb, t, band);
+    v.q0 = (int64_t)qb * qrows;
+    v.qend = a.nq;
+    v.c0 = (int64_t)t * BN;
+    v.cend = a.n;
+    v.run_first = run_begin(a.w, band, qb);
+    v.slot_base = band * a.w.span;
+  }
+  return v;
+}
 
 // a * b / c for non-negative operands, without 128-bit division (a software
 // routine of hundreds of instructions) unless the product needs 64 bits
@@ -619,9 +668,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       bool ok = true;
       const uint32_t full0 = PAIR ? ptx::mapa(ptx::smem_u32(&full_bar[0]), 0) : 0u;  // even CTA's full_bar[0]
       for (int64_t st = 0; st < it1 - it0 && ok; ++st) {
-        const int64_t item = walk_item(it0, it1, a.w, st);
-        int qb, t, band;
-        item_pos(a.w, item, qb, t, band);
+        const ItemView v = view_item(a, walk_item(it0, it1, a.w, st), QROWS);
         for (int kb = 0; kb < a.nkb; ++kb, ++it) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
@@ -634,12 +681,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           if (PAIR) {
             if (rank == 0) ptx::mbar_arrive_expect_tx(&full_bar[s], 2 * STAGE_BYTES);
             const uint32_t fb = full0 + (uint32_t)s * 8u;
-            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * BK, qb * QROWS + (int)rank * BM);
-            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * BK, t * BN + (int)rank * Stg<PAIR>::B_ROWS);
+            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * BK, (int)v.q0 + (int)rank * BM);
+            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * BK, (int)v.c0 + (int)rank * Stg<PAIR>::B_ROWS);
           } else {
             ptx::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * BK, qb * BM);
-            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * BK, t * BN);
+            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * BK, (int)v.q0);
+            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * BK, (int)v.c0);
           }
         }
       }
@@ -712,7 +759,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 #pragma unroll
     for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
     int tcount = 0;
-    int cur_qb = -1, cur_band = -1;
+    int64_t cur_run = -1, cur_q0 = 0, cur_qend = 0;
     int seg_slot = 0;
     bool alive = true;
 
@@ -721,10 +768,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     // write the warp's 32 row lists of a finished segment, each sorted across the lanes
     const int64_t row0 = (int64_t)rank * BM;  // this CTA's rows inside a work unit's query block
     const uint32_t tempty0 = PAIR ? ptx::mapa(ptx::smem_u32(&tempty_bar[0]), 0) : 0u;
-    auto flush = [&](int qb_, int slot_) {
+    auto flush = [&](int64_t q0_, int64_t qend_, int slot_) {
       if (a.seedmode) {
-        const int64_t gq = (int64_t)qb_ * QROWS + row0 + row;
-        if (gq < a.nq) {
+        const int64_t gq = q0_ + row0 + row;
+        if (gq < qend_) {
           uint64_t* dst = a.partial + (gq * a.smax + slot_) * LIST;
 #pragma unroll
           for (int i = 0; i < SEED_DEPTH; ++i) dst[i] = top[i];
@@ -738,8 +785,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       for (int r = 0; r < 32; ++r) {
         uint64_t v = lane < CAP ? wl[lane * BM + r] : KEY_NONE;
         v = warp_sort32(v, lane);
-        const int64_t gq = (int64_t)qb_ * QROWS + row0 + quad * 32 + r;
-        if (gq < a.nq && lane < CAP) a.partial[(gq * a.smax + slot_) * LIST + lane] = v;
+        const int64_t gq = q0_ + row0 + quad * 32 + r;
+        if (gq < qend_ && lane < CAP) a.partial[(gq * a.smax + slot_) * LIST + lane] = v;
       }
       __syncwarp();
     };
@@ -748,39 +795,35 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     // current tile's in nbc, the next tile's fetched into nbn one tile ahead
     float nbn[BN / 32], nbc[BN / 32];
     auto fetch_norms = [&](int64_t st_) {
-      const int64_t item_ = walk_item(it0, it1, a.w, st_);
-      int qb_, t_, b_;
-      item_pos(a.w, item_, qb_, t_, b_);
-      const int64_t c0 = (int64_t)t_ * BN;
+      const ItemView v_ = view_item(a, walk_item(it0, it1, a.w, st_), QROWS);
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) {
-        const int64_t col = c0 + lane + 32 * i;
-        nbn[i] = col < a.n ? __ldg(&a.bnorm[col * a.bstride]) : INF;
+        const int64_t col = v_.c0 + lane + 32 * i;
+        nbn[i] = col < v_.cend ? __ldg(&a.bnorm[col * a.bstride]) : INF;
       }
     };
     if (it1 > it0) fetch_norms(0);
     for (int64_t st = 0; st < it1 - it0; ++st, ++tcount) {
-      const int64_t item = walk_item(it0, it1, a.w, st);
-      int qb, t, band;
-      item_pos(a.w, item, qb, t, band);
-      if (qb != cur_qb || band != cur_band) {
-        if (cur_qb >= 0) {
+      const ItemView v = view_item(a, walk_item(it0, it1, a.w, st), QROWS);
+      if (v.run_first != cur_run) {
+        if (cur_run >= 0) {
           // flush the finished segment's lists (every set, even one that saw no candidate)
-          flush(cur_qb, seg_slot);
+          flush(cur_q0, cur_qend, seg_slot);
           for (int e = 0; e < CAP; ++e) mylist[e * BM] = KEY_NONE;
         }
-        cur_qb = qb;
-        cur_band = band;
-        seg_slot = (band * a.w.span + (cta - cta_of(run_begin(a.w, band, qb), a.w.work, a.w.grid))) * NSETS + set;
-        const int64_t gq = (int64_t)qb * QROWS + row0 + row;
-        seed_key = (a.seed != nullptr && gq < a.nq) ? make_key(a.seed[gq], 0u) : KEY_NONE;
+        cur_run = v.run_first;
+        cur_q0 = v.q0;
+        cur_qend = v.qend;
+        seg_slot = (v.slot_base + (cta - cta_of(v.run_first, a.w.work, a.w.grid))) * NSETS + set;
+        const int64_t gq = v.q0 + row0 + row;
+        seed_key = (a.seed != nullptr && gq < v.qend) ? make_key(a.seed[gq], 0u) : KEY_NONE;
         thr_key = seed_key;
         thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
         lslot = 0;
         nfill = 0;
       }
       const int buf = tcount & 1;
-      const int64_t col0 = (int64_t)t * BN;
+      const int64_t col0 = v.c0;
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) nbc[i] = nbn[i];
       if (st + 1 < it1 - it0) fetch_norms(st + 1);
@@ -826,7 +869,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         ptx::tmem_ld_wait();
       }
     }
-    if (alive && cur_qb >= 0) flush(cur_qb, seg_slot);
+    if (alive && cur_run >= 0) flush(cur_q0, cur_qend, seg_slot);
   }
 
   ptx::tc_fence_before();
@@ -848,22 +891,33 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
 // Segment g of a query enumerates its slots band by band: the CTAs of the
 // (band, query block) run in order, each with its nsets lists.
 __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int smax, Walk w, int depth,
-                         int nsets, uint64_t* __restrict__ out) {
+                         int nsets, uint64_t* __restrict__ out, const RunInfo* __restrict__ runs,
+                         const int32_t* __restrict__ row_run) {
   constexpr int L = LIST;
   const int lane = threadIdx.x & 31;
   const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (q >= nq) return;
-  const int qb = (int)(q / w.qrows);
   // slots of this query, at most 64 bands x span x nsets (checked on the host)
   int nseg = 0;
   int band_first_slot[64], band_nslots[64];
-  for (int b = 0; b < w.nbands; ++b) {
-    const int64_t r0 = run_begin(w, b, qb);
-    const int c0 = cta_of(r0, w.work, w.grid);
-    const int c1 = cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
-    band_first_slot[b] = b * w.span * nsets;
-    band_nslots[b] = (c1 - c0 + 1) * nsets;
-    nseg += band_nslots[b];
+  if (runs) {
+    // segmented pass: the row's block run, slots 0 .. (CTAs of the run) x nsets
+    const RunInfo ri = runs[row_run[q]];
+    const int c0 = cta_of(ri.first, w.work, w.grid);
+    const int c1 = cta_of(ri.first + ri.len - 1, w.work, w.grid);
+    band_first_slot[0] = 0;
+    band_nslots[0] = (c1 - c0 + 1) * nsets;
+    nseg = band_nslots[0];
+  } else {
+    const int qb = (int)(q / w.qrows);
+    for (int b = 0; b < w.nbands; ++b) {
+      const int64_t r0 = run_begin(w, b, qb);
+      const int c0 = cta_of(r0, w.work, w.grid);
+      const int c1 = cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
+      band_first_slot[b] = b * w.span * nsets;
+      band_nslots[b] = (c1 - c0 + 1) * nsets;
+      nseg += band_nslots[b];
+    }
   }
   auto slot_of = [&](int g) {
     int b = 0;
@@ -1222,8 +1276,8 @@ __global__ void k2_scatter_fallback(const uint64_t* __restrict__ keys, const int
                                     const int* __restrict__ count, int kk, int L,
                                     uint64_t* __restrict__ cand, int* __restrict__ cand_count,
                                     float* __restrict__ floor_val) {
-  const int i = blockIdx.x;
-  if (i >= *count) return;
+  const int cnt = *count;
+  for (int i = blockIdx.x; i < cnt; i += gridDim.x) {
   const int q = rows[i];
   for (int e = threadIdx.x; e < L; e += blockDim.x) cand[(int64_t)q * L + e] = e < kk ? keys[(int64_t)i * kk + e] : KEY_NONE;
   if (threadIdx.x == 0) {
@@ -1232,6 +1286,47 @@ __global__ void k2_scatter_fallback(const uint64_t* __restrict__ keys, const int
     cand_count[q] = c;
     // the kk-th FP32 distance bounds every point outside the list from below
     floor_val[q] = (c == kk) ? key_dist(keys[(int64_t)i * kk + kk - 1]) : 3.0e38f;
+  }
+  }
+}
+
+// Work items of the segmented fallback: row r = fb_rows[i] against the
+// points of the set holding it; the exact FP32 list goes straight to the
+// row's candidate slots (cand[r][0, LIST)).
+__global__ void fb_items_kernel(const int* __restrict__ fb_rows, const int* __restrict__ fb_count,
+                                const int64_t* __restrict__ offs, int nsets, SegItem* __restrict__ items) {
+  const int cnt = *fb_count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int64_t r = fb_rows[i];
+    int lo = 0, hi = nsets - 1;
+    while (lo < hi) {  // last set whose offset <= r
+      const int mid = (lo + hi + 1) >> 1;
+      if (offs[mid] <= r) lo = mid;
+      else hi = mid - 1;
+    }
+    SegItem it{};
+    it.q0 = r;
+    it.qend = r + 1;
+    it.nb0 = offs[lo];
+    it.nb1 = offs[lo + 1];
+    it.split = 0;
+    items[i] = it;
+  }
+}
+
+// Candidate counts and floors of the fallback rows (their lists are exact
+// FP32 top-LIST lists: the LIST-th distance bounds every other point).
+__global__ void fb_finish_kernel(const int* __restrict__ fb_rows, const int* __restrict__ fb_count,
+                                 const uint64_t* __restrict__ cand, int* __restrict__ cand_count,
+                                 float* __restrict__ floor_val) {
+  const int cnt = *fb_count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const int64_t r = fb_rows[i];
+    const uint64_t* row = cand + r * LIST;
+    int c = 0;
+    while (c < LIST && row[c] != KEY_NONE) ++c;
+    cand_count[r] = c;
+    floor_val[r] = (c == LIST) ? key_dist(row[LIST - 1]) : 3.0e38f;
   }
 }
 
@@ -1607,44 +1702,72 @@ int k2_pair_capacity(Context* ctx) {
 // every query over n points (binfo row p * bstride), as sorted lists [nq][LIST].
 // mapA: the queries' operand (128-row boxes); binfo_map: the points' operand
 // (pass its buffer, rows and row step; the box height follows the form).
+// Segmented pass: the items (in run order), the runs and each row's run
+// (device), the runs on the host (for the slot span) and their count.
+struct SegPass {
+  const TileItem* items = nullptr;
+  int64_t nitems = 0;
+  const RunInfo* runs = nullptr;
+  const int32_t* row_run = nullptr;
+  const RunInfo* runs_host = nullptr;
+  int64_t nruns = 0;
+};
+
 mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA, const void* bxb, int64_t bstride,
                           const RowInfo* qinfo, const RowInfo* binfo, const float* bnorm, int64_t n, int64_t nq,
                           int d, int dp, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
-                          bool timed, uint64_t** lists_out, int seedmode = 0) {
+                          bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr) {
   // two epilogue sets with 16-entry lists when the depth allows it; each set
   // writes its own slot
   const int nsets = depth <= 16 ? 2 : 1;
   // CTA pairs (cta_group::2) when there are at least two 128-row query blocks
-  const int pairs = nq > BM ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx)) : 0;
+  const int pairs = (nq > BM && !seg) ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx)) : 0;
   const bool pair = pairs >= 1;
   const int qrows = pair ? 2 * BM : BM;
   const int64_t qblocks = ceil_div(nq, qrows);
   const int tiles = (int)ceil_div(n, BN);
   Walk w;
-  w.tiles = tiles;
-  w.qblocks = (int)qblocks;
-  w.qrows = qrows;
-  w.work = qblocks * tiles;
-  w.grid = (int)std::min<int64_t>(pair ? pairs : ctx->num_sms, w.work);
-  // bands: a point operand above BAND_MIN_BYTES is walked in bands of about
-  // BAND_BYTES so each band stays in L2 while every query block passes over it
-  const double tile_bytes = (double)BN * dp * 2.0;
-  w.band_tiles = tiles;
-  if (bstride == 1 && (double)n * dp * 2.0 > BAND_MIN_BYTES && ceil_div(nq, BM) >= 8)
-    w.band_tiles = std::max(1, std::min(tiles, (int)(BAND_BYTES / tile_bytes)));
-  w.nbands = (int)ceil_div(tiles, w.band_tiles);
-  if (w.nbands > 64) {  // the merge enumerates at most 64 bands
-    w.band_tiles = (int)ceil_div(tiles, 64);
-    w.nbands = (int)ceil_div(tiles, w.band_tiles);
-  }
-  w.span = 1;
-  for (int b = 0; b < w.nbands; ++b)
-    for (int64_t qb = 0; qb < qblocks; ++qb) {
-      const int64_t r0 = run_begin(w, b, (int)qb);
-      const int c0 = h_cta_of(r0, w.work, w.grid);
-      const int c1 = h_cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
+  if (seg) {
+    // one band over the item list in run order; a run is one block's items
+    w.tiles = 1;
+    w.qblocks = (int)seg->nruns;
+    w.qrows = BM;
+    w.work = seg->nitems;
+    w.grid = (int)std::min<int64_t>(ctx->num_sms, w.work);
+    w.band_tiles = 1;
+    w.nbands = 1;
+    w.span = 1;
+    for (int64_t r = 0; r < seg->nruns; ++r) {
+      const int c0 = h_cta_of(seg->runs_host[r].first, w.work, w.grid);
+      const int c1 = h_cta_of(seg->runs_host[r].first + seg->runs_host[r].len - 1, w.work, w.grid);
       w.span = std::max(w.span, c1 - c0 + 1);
     }
+  } else {
+    w.tiles = tiles;
+    w.qblocks = (int)qblocks;
+    w.qrows = qrows;
+    w.work = qblocks * tiles;
+    w.grid = (int)std::min<int64_t>(pair ? pairs : ctx->num_sms, w.work);
+    // bands: a point operand above BAND_MIN_BYTES is walked in bands of about
+    // BAND_BYTES so each band stays in L2 while every query block passes over it
+    const double tile_bytes = (double)BN * dp * 2.0;
+    w.band_tiles = tiles;
+    if (bstride == 1 && (double)n * dp * 2.0 > BAND_MIN_BYTES && ceil_div(nq, BM) >= 8)
+      w.band_tiles = std::max(1, std::min(tiles, (int)(BAND_BYTES / tile_bytes)));
+    w.nbands = (int)ceil_div(tiles, w.band_tiles);
+    if (w.nbands > 64) {  // the merge enumerates at most 64 bands
+      w.band_tiles = (int)ceil_div(tiles, 64);
+      w.nbands = (int)ceil_div(tiles, w.band_tiles);
+    }
+    w.span = 1;
+    for (int b = 0; b < w.nbands; ++b)
+      for (int64_t qb = 0; qb < qblocks; ++qb) {
+        const int64_t r0 = run_begin(w, b, (int)qb);
+        const int c0 = h_cta_of(r0, w.work, w.grid);
+        const int c1 = h_cta_of(r0 + band_len(w, b) - 1, w.work, w.grid);
+        w.span = std::max(w.span, c1 - c0 + 1);
+      }
+  }
   const int smax = w.nbands * w.span * nsets;
   uint64_t* partial = nullptr;
   MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * smax * LIST, &partial));
@@ -1657,6 +1780,7 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.dp = dp;
   ma.nkb = (int)ceil_div(dp, BK);
   ma.w = w;
+  ma.titems = seg ? seg->items : nullptr;
   ma.smax = smax;
   ma.L = LIST;
   ma.depth = depth;
@@ -1687,7 +1811,8 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
   MANN_TRY(ctx->scratch_t(slot_lists, (size_t)nq * LIST, &lists));
-  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, w, depth, nsets, lists);
+  k2_merge<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(partial, nq, smax, w, depth, nsets, lists,
+                                                     seg ? seg->runs : nullptr, seg ? seg->row_run : nullptr);
   MANN_CHECK_LAUNCH();
   *lists_out = lists;
   return MANN_OK;
@@ -1710,26 +1835,24 @@ struct Bf16Operand {
   float* norms = nullptr;  // contiguous ||x~||^2 (points only)
 };
 
-mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
-                          const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
-                          bool fp64, uint64_t** out_keys, mann_knn_report* rep) {
-  if (nq <= 0) return MANN_OK;
-  const int L = LIST;
-  // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
-  // autotuner's choice for this shape class -- the full list on first sight,
-  // then the depth 99% of rows needed plus one (refreshed after every call).
-  const uint64_t tkey = ((uint64_t)kreq << 56) ^ ((uint64_t)d << 36) ^ ((uint64_t)metric << 32) ^
-                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63);
-  int depth = L;
-  if (margin > 0) {
-    depth = std::min(L, kreq + margin);
-  } else {
-    auto it = ctx->tune.find(tkey);
-    if (it != ctx->tune.end()) depth = (int)it->second;
-  }
-  if (kreq > KREQ_MAX_BF16)
-    return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
-                                     " (k+1 for graphs)");
+// Operands of one BF16 search: unit-normalised rows for cosine, the centre
+// and scale chosen on a row sample, the split decision (read back: the one
+// host synchronisation of the preparation), the converted rows and their
+// bound terms, and the zeroed counters [2] candidates, [4..5] resolve,
+// [8] error word + fallback count (as ints), [16..49] depth histogram.
+struct Bf16Prep {
+  Bf16Operand B, Q;
+  int split = 0, dp = 0, dpe = 0;
+  float* scale = nullptr;
+  BaseMax* bmax = nullptr;
+  float *cos_bn = nullptr, *cos_qn = nullptr;
+  unsigned long long* counters = nullptr;
+  int* err = nullptr;
+  int* fb_count = nullptr;
+};
+
+mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_t n, const float* qs, int64_t nq,
+                         int d, int metric, Bf16Prep* P) {
   const int dp = (d + 7) & ~7;
   const bool self = (qs == base);
   const bool cosine = metric == MANN_METRIC_COSINE;
@@ -1791,10 +1914,6 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
   const int split = h_inexact ? 1 : 0;
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
-  if (margin <= 0) {
-    auto it = ctx->tune.find(tkey ^ ((uint64_t)split << 62));
-    depth = it != ctx->tune.end() ? (int)it->second : L;
-  }
   Bf16Operand B, Q;
   MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dpe, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
@@ -1811,14 +1930,74 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
                                                                   nullptr, nullptr, split, 0);
     MANN_CHECK_LAUNCH();
   }
-
-  // ---- counters: [2] candidates, [4..5] resolve, [8] error word + fallback
-  // count (as ints), [16..49] depth histogram
   unsigned long long* counters = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
-  int* err = reinterpret_cast<int*>(counters + 8);
-  int* fb_count = err + 1;
   MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
+  P->B = B;
+  P->Q = Q;
+  P->split = split;
+  P->dp = dp;
+  P->dpe = dpe;
+  P->scale = scale;
+  P->bmax = bmax;
+  P->cos_bn = cos_bn;
+  P->cos_qn = cos_qn;
+  P->counters = counters;
+  P->err = reinterpret_cast<int*>(counters + 8);
+  P->fb_count = P->err + 1;
+  return MANN_OK;
+}
+
+// The autotuned admission depth (list entries a certificate may need) from
+// the depth histogram of a rerank: the 99.9th percentile + 1, 16 when that
+// is <= 16 (the two-set kernel), the full list when > 0.1 % of rows fell back.
+int tuned_depth(const unsigned long long* hist, int kreq) {
+  const int L = LIST;
+  unsigned long long total = 0, acc = 0;
+  for (int j = 0; j <= L + 1; ++j) total += hist[j];
+  if (hist[L + 1] * 1000 > total) return L;
+  for (int j = 0; j <= L; ++j) {
+    acc += hist[j];
+    if (acc * 1000 >= total * 999) {
+      int want = std::min(L, std::max(kreq + 2, j + 1));
+      if (want <= 16) want = 16;
+      return want;
+    }
+  }
+  return L;
+}
+
+mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
+                          const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep) {
+  if (nq <= 0) return MANN_OK;
+  const int L = LIST;
+  // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
+  // autotuner's choice for this shape class -- the full list on first sight,
+  // then the depth 99.9% of rows needed plus one (refreshed after every call).
+  const uint64_t tkey = ((uint64_t)kreq << 56) ^ ((uint64_t)d << 36) ^ ((uint64_t)metric << 32) ^
+                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63);
+  int depth = L;
+  if (kreq > KREQ_MAX_BF16)
+    return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
+                                     " (k+1 for graphs)");
+  const bool cosine = metric == MANN_METRIC_COSINE;
+  Bf16Prep P;
+  MANN_TRY(bf16_prepare(ctx, s, base, n, qs, nq, d, metric, &P));
+  const int split = P.split, dpe = P.dpe;
+  if (margin > 0) {
+    depth = std::min(L, kreq + margin);
+  } else {
+    auto it = ctx->tune.find(tkey ^ ((uint64_t)split << 62));
+    depth = it != ctx->tune.end() ? (int)it->second : L;
+  }
+  Bf16Operand B = P.B, Q = P.Q;
+  float* scale = P.scale;
+  BaseMax* bmax = P.bmax;
+  float *cos_bn = P.cos_bn, *cos_qn = P.cos_qn;
+  unsigned long long* counters = P.counters;
+  int* err = P.err;
+  int* fb_count = P.fb_count;
 
   CUtensorMap mapA;
   MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM));
@@ -1897,26 +2076,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   const int h_err = reinterpret_cast<const int*>(hc + 8)[0];
   const int h_fb = reinterpret_cast<const int*>(hc + 8)[1];
   if (margin <= 0 && h_err == 0) {
-    // autotune the admission depth from the depths the certificates needed
-    const unsigned long long* hist = hc + 16;
-    unsigned long long total = 0, acc = 0;
-    for (int j = 0; j <= L + 1; ++j) total += hist[j];
-    int want = L;
-    if (hist[L + 1] * 1000 > total) {
-      want = L;  // more than 0.1% fell back at this depth: widen to the full list
-    } else {
-      for (int j = 0; j <= L; ++j) {
-        acc += hist[j];
-        if (acc * 1000 >= total * 999) {
-          // the 99.9th percentile + 1; anything up to 16 runs the 16-entry
-          // two-set kernel, so take all 16 there (fewer exact-scan fallbacks)
-          want = std::min(L, std::max(kreq + 2, j + 1));
-          if (want <= 16) want = 16;
-          break;
-        }
-      }
-    }
-    ctx->tune[tkey ^ ((uint64_t)split << 62)] = (uint64_t)want;
+    // autotune the admission depth (the k-margin) from the depths the certificates needed
+    ctx->tune[tkey ^ ((uint64_t)split << 62)] = (uint64_t)tuned_depth(hc + 16, kreq);
   }
   if (h_err != 0)
     return fail(MANN_ETIMEOUT, "tensor-core kernel: a bounded wait ran out (role " + std::to_string(h_err) + ")");
@@ -1954,6 +2115,194 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
       rep->precision_used = MANN_PREC_BF16;
       rep->margin_used = depth - kreq;
     }
+  }
+  *out_keys = keys;
+  return MANN_OK;
+}
+
+
+// ---------------------------------------------------------------- many point sets (segmented)
+
+namespace {
+
+// Items, runs and row -> run table of one set layout, kept on the host and
+// uploaded once per layout.
+struct SegTables {
+  uint64_t hash = 0;
+  std::vector<TileItem> items;
+  std::vector<RunInfo> runs;
+  std::vector<int32_t> row_run;
+  const void* uploaded = nullptr;  // device items buffer the tables were copied to
+  uint64_t uploaded_hash = 0;
+};
+std::mutex g_seg_mu;
+std::map<Context*, SegTables*> g_seg;
+
+SegTables& seg_tables(Context* ctx) {
+  std::lock_guard<std::mutex> lk(g_seg_mu);
+  SegTables*& t = g_seg[ctx];
+  if (!t) t = new SegTables();
+  return *t;
+}
+
+void build_seg_tables(const int64_t* offs, int nsets, SegTables* T) {
+  uint64_t h = 1469598103934665603ull;
+  for (int c = 0; c <= nsets; ++c) {
+    h ^= (uint64_t)offs[c];
+    h *= 1099511628211ull;
+  }
+  if (T->hash == h && !T->items.empty()) return;
+  T->items.clear();
+  T->runs.clear();
+  T->row_run.assign((size_t)offs[nsets], 0);
+  for (int c = 0; c < nsets; ++c) {
+    const int64_t o = offs[c], nc = offs[c + 1] - offs[c];
+    for (int64_t q = 0; q < nc; q += BM) {
+      const int64_t first = (int64_t)T->items.size();
+      for (int64_t t = 0; t < nc; t += BN) T->items.push_back(TileItem{o + q, o + nc, o + t, o + nc, first});
+      const int32_t r = (int32_t)T->runs.size();
+      T->runs.push_back(RunInfo{first, (int64_t)T->items.size() - first});
+      for (int64_t row = o + q; row < std::min(o + q + BM, o + nc); ++row) T->row_run[(size_t)row] = r;
+    }
+  }
+  T->hash = h;
+}
+
+}  // namespace
+
+// Self-kNN keys of many independent point sets stored back to back (set c is
+// rows [offs[c], offs[c+1])), each searched against its own points only, in
+// the BF16 form: one operand preparation over all rows, one segmented k2_main
+// pass over every (set, 128-row block, 256-point tile) item, the certificate
+// and exact FP32 rerank per row, uncertified rows re-scanned exactly over
+// their own set on the device (work queue published by a kernel, so the host
+// never waits for their count), and the (distance, id) truncation to kreq.
+// Result: keys [N][kreq] with global ids (the row itself included).
+mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* data, const int64_t* offs_host,
+                                  const int64_t* offs_dev, int nsets, int d, int metric, int kreq, int margin,
+                                  uint64_t** out_keys, mann_knn_report* rep) {
+  const int L = LIST;
+  if (kreq > KREQ_MAX_BF16)
+    return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
+                                     " (k+1 for graphs)");
+  if (metric != MANN_METRIC_EUCLIDEAN && metric != MANN_METRIC_SQEUCLIDEAN)
+    return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
+  const int64_t N = offs_host[nsets];
+  SegTables& T = seg_tables(ctx);
+  build_seg_tables(offs_host, nsets, &T);
+  TileItem* d_items = nullptr;
+  RunInfo* d_runs = nullptr;
+  int32_t* d_row_run = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_ITEMS, T.items.size(), &d_items));
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_RUNS, T.runs.size(), &d_runs));
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_ROWRUN, (size_t)N, &d_row_run));
+  if (T.uploaded != d_items || T.uploaded_hash != T.hash) {
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_items, T.items.data(), sizeof(TileItem) * T.items.size(), cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_runs, T.runs.data(), sizeof(RunInfo) * T.runs.size(), cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_row_run, T.row_run.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaStreamSynchronize(s));  // the copies read pageable host memory
+    T.uploaded = d_items;
+    T.uploaded_hash = T.hash;
+  }
+  Bf16Prep P;
+  MANN_TRY(bf16_prepare(ctx, s, data, N, data, N, d, metric, &P));
+  // the admission depth (k-margin): tuned per (layout, k, d, metric, form)
+  const uint64_t tkey = 0x5E6B000000000000ull ^ (T.hash >> 8) ^ ((uint64_t)kreq << 40) ^ ((uint64_t)d << 24) ^
+                        ((uint64_t)metric << 20) ^ ((uint64_t)P.split << 19);
+  int depth = L;
+  if (margin > 0) {
+    depth = std::min(L, kreq + margin);
+  } else {
+    auto it = ctx->tune.find(tkey);
+    if (it != ctx->tune.end()) depth = (int)it->second;
+  }
+  CUtensorMap mapA;
+  MANN_TRY(make_map(&mapA, P.Q.xb, N, P.dpe, BM));
+  SegPass sp;
+  sp.items = d_items;
+  sp.nitems = (int64_t)T.items.size();
+  sp.runs = d_runs;
+  sp.row_run = d_row_run;
+  sp.runs_host = T.runs.data();
+  sp.nruns = (int64_t)T.runs.size();
+  uint64_t* lists = nullptr;
+  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.dpe, depth, nullptr,
+                         P.err, SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, &sp));
+  // ---- certify + rerank (per row; the bounds are global, so valid for every set)
+  uint64_t* cand = nullptr;
+  int* cand_count = nullptr;
+  float* floor_val = nullptr;
+  int* fb_rows = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_CAND, (size_t)N * L, &cand));
+  MANN_TRY(ctx->scratch_t(SLOT_MISC0, (size_t)N, &cand_count));
+  MANN_TRY(ctx->scratch_t(SLOT_MISC1, (size_t)N, &floor_val));
+  MANN_TRY(ctx->scratch_t(SLOT_FALLBACK, (size_t)N, &fb_rows));
+  RerankArgs ra;
+  ra.base = data;
+  ra.qs = data;
+  ra.nq = N;
+  ra.n = N;
+  ra.d = d;
+  ra.L = L;
+  ra.kreq = kreq;
+  ra.metric = metric;
+  ra.scale = P.scale;
+  ra.depth = depth;
+  ra.seed = nullptr;
+  ra.depth_hist = P.counters + 16;
+  ra.qinfo = P.Q.info;
+  ra.bmax = P.bmax;
+  ra.lists = lists;
+  ra.cand = cand;
+  ra.cand_count = cand_count;
+  ra.floor_val = floor_val;
+  ra.fb_rows = fb_rows;
+  ra.fb_count = P.fb_count;
+  ra.cand_total = P.counters + 2;
+  ra.kdim = P.dpe;
+  ra.cos_qn = nullptr;
+  ra.cos_bn = nullptr;
+  ra.eps_c = 0.0f;
+  ra.coop = (d % 4 == 0 && (reinterpret_cast<uintptr_t>(data) & 15) == 0) ? 1 : 0;
+  k2_rerank<<<(unsigned)std::min<int64_t>(ceil_div(N, RR_WARPS), (int64_t)ctx->num_sms * 6), 32 * RR_WARPS, 0,
+              s>>>(ra);
+  MANN_CHECK_LAUNCH();
+  // ---- uncertified rows: exact FP32 scan of their own set, on the device
+  SegItem* fitems = nullptr;
+  SegQueue* fq = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_FALLBACK_KEYS, (size_t)N, &fitems));
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_QUEUE, 1, &fq));
+  const int gfb = ctx->num_sms * 8;
+  fb_items_kernel<<<gfb, 256, 0, s>>>(fb_rows, P.fb_count, offs_dev, nsets, fitems);
+  MANN_CHECK_LAUNCH();
+  static unsigned fb_epoch = 0x40000000u;
+  const unsigned ep = ++fb_epoch;
+  MANN_TRY(launch_publish_queue(fq, 0, P.fb_count, ep, s));
+  MANN_TRY(launch_k1_persistent(ctx->num_sms, data, fitems, fq, ep, 1ll << 31, d, metric, 32, L, 1, cand, s));
+  fb_finish_kernel<<<gfb, 256, 0, s>>>(fb_rows, P.fb_count, cand, cand_count, floor_val);
+  MANN_CHECK_LAUNCH();
+  // ---- truncate to kreq (ties at the k-th distance keep the FP32 (distance, id) order)
+  uint64_t* keys = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)N * kreq, &keys));
+  MANN_TRY(launch_resolve(data, data, d, metric, N, L, kreq, 0, cand, cand_count, floor_val, keys,
+                          P.counters + 4, s));
+  // ---- status, report, and the depth for the next call of this layout
+  unsigned long long hc[64];
+  MANN_CUDA_TRY(cudaMemcpyAsync(hc, P.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  int qstatus = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(&qstatus, &fq->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  const int h_err = reinterpret_cast<const int*>(hc + 8)[0];
+  const int h_fb = reinterpret_cast<const int*>(hc + 8)[1];
+  if (h_err != 0)
+    return fail(MANN_ETIMEOUT, "tensor-core kernel: a bounded wait ran out (role " + std::to_string(h_err) + ")");
+  if (qstatus != 0) return fail(MANN_ETIMEOUT, "batched graphs: the fallback work queue was not published in time");
+  if (margin <= 0) ctx->tune[tkey] = (uint64_t)tuned_depth(hc + 16, kreq);
+  if (rep) {
+    rep->rows_fallback = h_fb;
+    rep->candidates = (int64_t)hc[2];
+    rep->precision_used = MANN_PREC_BF16;
+    rep->margin_used = depth - kreq;
   }
   *out_keys = keys;
   return MANN_OK;

@@ -342,7 +342,8 @@ __global__ void __launch_bounds__(K1_THREADS, 1)
 template <int METRIC, int BQ, int KW, bool VEC>
 __global__ void __launch_bounds__(K1_THREADS, 2)
     k1_persistent(const float* __restrict__ data, const SegItem* __restrict__ items, SegQueue* q, unsigned epoch,
-                  long long wait_cycles, int d, int k, int nsplit, uint64_t* __restrict__ partial) {
+                  long long wait_cycles, int d, int k, int nsplit, uint64_t* __restrict__ partial,
+                  const int32_t* __restrict__ qrows) {
   extern __shared__ float4 k1_smem[];
   __shared__ int s_item;
   __shared__ int s_count;
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(K1_THREADS, 2)
     const int idx = s_item;
     if (idx < 0) break;
     const SegItem it = items[idx];
-    k1_body<METRIC, BQ, KW, VEC>(data, it.nb0, it.nb1, data, nullptr, it.q0, it.qend, d, nullptr, nullptr, k,
+    k1_body<METRIC, BQ, KW, VEC>(data, it.nb0, it.nb1, data, qrows, it.q0, it.qend, d, nullptr, nullptr, k,
                                  partial + (int64_t)it.split * k, (int64_t)nsplit * k,
                                  reinterpret_cast<float*>(k1_smem));
     __syncthreads();  // s_item is rewritten only after every thread read it
@@ -629,7 +630,8 @@ mann_status dispatch_k1(Context* ctx, int k, const float* base, int64_t n, const
 
 template <int METRIC, int BQ, int KW, bool VEC>
 static mann_status launch_pers_t(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
-                                 long long wait_cycles, int d, int k, int nsplit, uint64_t* partial, cudaStream_t s) {
+                                 long long wait_cycles, int d, int k, int nsplit, uint64_t* partial,
+                                 const int32_t* qrows, cudaStream_t s) {
   constexpr int QSTR = BQ + 4, BSTR = K1_BN + 4;
   const size_t smem = sizeof(float) * (2 * K1_DK * QSTR + 2 * K1_DK * BSTR + BQ * BSTR);
   auto kern = k1_persistent<METRIC, BQ, KW, VEC>;
@@ -637,19 +639,21 @@ static mann_status launch_pers_t(int num_sms, const float* data, const SegItem* 
   int per_sm = 0;
   MANN_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, K1_THREADS, smem));
   const int grid = std::max(1, per_sm) * num_sms;  // every CTA resident: the queue needs no co-scheduling
-  kern<<<(unsigned)grid, K1_THREADS, smem, s>>>(data, items, q, epoch, wait_cycles, d, k, nsplit, partial);
+  kern<<<(unsigned)grid, K1_THREADS, smem, s>>>(data, items, q, epoch, wait_cycles, d, k, nsplit, partial, qrows);
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
 
 mann_status launch_k1_persistent(int num_sms, const float* data, const SegItem* items, SegQueue* q, unsigned epoch,
                                  long long wait_cycles, int d, int metric, int bq, int k, int nsplit,
-                                 uint64_t* partial, cudaStream_t s) {
+                                 uint64_t* partial, cudaStream_t s, const int32_t* qrows) {
   if (k < 1 || k > 64) return fail(MANN_EINVAL_ARG, "batched graphs support 1 <= k <= 64 (k+1 with self)");
   const bool vec = (d % 4) == 0;
 #define PERS_CASE(M, B, KW)                                                                                      \
-  return vec ? launch_pers_t<M, B, KW, true>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, s) \
-             : launch_pers_t<M, B, KW, false>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, s)
+  return vec ? launch_pers_t<M, B, KW, true>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, \
+                                             qrows, s)                                                          \
+             : launch_pers_t<M, B, KW, false>(num_sms, data, items, q, epoch, wait_cycles, d, k, nsplit, partial, \
+                                              qrows, s)
   if (metric == MANN_METRIC_EUCLIDEAN) {
     if (k > 32) {
       if (bq == 32) PERS_CASE(MANN_METRIC_EUCLIDEAN, 32, 2);

@@ -73,9 +73,11 @@ def _create_graph_metadata(original_k, directed, node_metadata, n_points):
 
 def knn_graph_arrays(index: BruteForceIndex, data, k: int, *, include_self: bool = False,
                      precision: str = "fp32", fp64_ties: bool = False, margin: int = 0,
-                     report: bool = False):
+                     report: bool = False, fp64_error: bool = False):
     """Self-kNN graph on the GPU: (ids [n, k] 0-based int32, dists [n, k]);
-    ``data`` is the d x n matrix or a DeviceDataset of it."""
+    ``data`` is the d x n matrix or a DeviceDataset of it.  With
+    ``fp64_error`` the report's ``max_abs_err_fp64`` holds the largest
+    |returned distance - FP64 distance| over all returned neighbours."""
     ds = data if isinstance(data, DeviceDataset) else None
     a = None if ds is not None else np.asarray(data)
     n = ds.n if ds is not None else a.shape[1]
@@ -85,7 +87,7 @@ def knn_graph_arrays(index: BruteForceIndex, data, k: int, *, include_self: bool
     ids = np.empty((n, k), np.int32)
     dists = np.empty((n, k), np.float32)
     p = _lib.params(metric_code(index.distance), k, PRECISIONS[precision], margin,
-                    _lib.FLAG_FP64_TIES if fp64_ties else 0)
+                    (_lib.FLAG_FP64_TIES if fp64_ties else 0) | (_lib.FLAG_FP64_ERR if fp64_error else 0))
     rep = _lib.KnnReport()
     if ds is not None:
         _lib.check(_lib.load().mann_knn_graph_dataset(p, ds.handle, int(bool(include_self)), ids.ctypes.data,
@@ -100,9 +102,11 @@ def knn_graph_arrays(index: BruteForceIndex, data, k: int, *, include_self: bool
 
 
 def knn_graph_batched_arrays(clouds, k: int, *, distance=None, include_self: bool = False,
-                             report: bool = False):
+                             report: bool = False, precision: str = "fp32"):
     """Self-kNN graphs of many point sets (each d x n_i) in one library call:
-    (ids [sum n_i, k] 0-based ids local to each set, dists, offsets [nsets+1])."""
+    (ids [sum n_i, k] 0-based ids local to each set, dists, offsets [nsets+1]).
+    ``precision="bf16"``: the tensor-core form (one segmented pass over every
+    set, exact FP32 rerank; the same answer, k + 1 <= 24)."""
     from .distances import default_distance
 
     mats = [np.asarray(c) for c in clouds]
@@ -117,7 +121,7 @@ def knn_graph_batched_arrays(clouds, k: int, *, distance=None, include_self: boo
     N = int(offs[-1])
     ids = np.empty((N, k), np.int32)
     dists = np.empty((N, k), np.float32)
-    p = _lib.params(metric_code(distance or default_distance), k, _lib.PREC_FP32)
+    p = _lib.params(metric_code(distance or default_distance), k, PRECISIONS[precision])
     rep = _lib.KnnReport()
     _lib.check(_lib.load().mann_knn_graph_batched(p, pts.ctypes.data, offs.ctypes.data, len(mats), d,
                                                   int(bool(include_self)), ids.ctypes.data, dists.ctypes.data,

@@ -93,3 +93,43 @@ def test_batched_validation(gpu_lib):
         M.knn_graph_batched_arrays([a, np.zeros((4, 0), np.float32)], 2)
     with pytest.raises(M.ArgumentError):
         M.knn_graph_batched_arrays([a], 2, distance=M.CosineDist())
+
+
+@pytest.mark.parametrize("metric,d,k", [(1, 32, 15), (0, 7, 5), (1, 12, 23), (1, 40, 10)])
+def test_batched_bf16_form_equals_oracle_per_set(gpu_lib, orc, metric, d, k):
+    """The tensor-core form of the batched graphs (one segmented pass over
+    every set's (block, tile) items, exact FP32 rerank, exact re-scan of
+    uncertified rows within their own set) gives each set the oracle's graph."""
+    import manifoldann_gb300 as M
+
+    clouds = _clouds(9, 26, 3000, d, seed=100 + d)
+    clouds.append(np.random.default_rng(d).standard_normal((28, d)).astype(np.float32))  # below the list depth
+    dist = M.SqEuclidean() if metric == 1 else M.Euclidean()
+    ids, dists, offs, rep = M.knn_graph_batched_arrays([c.T for c in clouds], k, distance=dist, report=True,
+                                                       precision="bf16")
+    assert rep["precision_used"] == 1
+    for c, cl in enumerate(clouds):
+        i_o, d_o = orc.knn_graph_f32(cl, k, metric)
+        assert np.array_equal(ids[offs[c]:offs[c + 1]], i_o), c
+        assert np.array_equal(dists[offs[c]:offs[c + 1]].view(np.uint32), d_o.view(np.uint32)), c
+
+
+def test_batched_bf16_form_ties_duplicates_and_full_size(gpu_lib, orc):
+    import manifoldann_gb300 as M
+
+    g = np.stack(np.meshgrid(np.arange(6), np.arange(5), np.arange(4), indexing="ij"), -1).reshape(-1, 3)
+    a = np.concatenate([g, g[:17]]).astype(np.float32)
+    b = (np.arange(40, dtype=np.float32)[:, None] * np.ones((1, 3), np.float32))
+    ids, dists, offs = M.knn_graph_batched_arrays([a.T, b.T], 6, distance=M.SqEuclidean(), precision="bf16")
+    for c, cl in enumerate((a, b)):
+        i_o, d_o = orc.knn_graph_f32(cl, 6, 1)
+        assert np.array_equal(ids[offs[c]:offs[c + 1]], i_o)
+        assert np.array_equal(dists[offs[c]:offs[c + 1]], d_o)
+    clouds = _clouds(64, 2000, 50000, 32, seed=0)
+    i32, d32, o32 = M.knn_graph_batched_arrays([c.T for c in clouds], 15, distance=M.SqEuclidean())
+    for _ in range(2):  # the second call runs the tuned admission depth
+        ib, db, ob, rep = M.knn_graph_batched_arrays([c.T for c in clouds], 15, distance=M.SqEuclidean(),
+                                                     precision="bf16", report=True)
+        assert np.array_equal(ib, i32) and np.array_equal(db.view(np.uint32), d32.view(np.uint32))
+        assert rep["rows_fallback"] <= len(ib) // 100, rep
+
