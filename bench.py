@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched uneven graphs leg")
     ap.add_argument("--no-angular", action="store_true", help="skip the angular (cosine) leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain 64-d FP32 leg")
+    ap.add_argument("--no-fp8", action="store_true", help="skip the FP8-form measurement")
     ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "ivf-profile", "angular", "plain"],
                     default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
@@ -504,6 +505,28 @@ def run_batched_leg(args, stream_ptr=0):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    # the BF16 tensor-core form of the same graphs (one segmented pass, exact rerank)
+    pb = _lib.params(_lib.METRIC_SQEUCLIDEAN, 15, _lib.PREC_BF16)
+    rb = _lib.KnnReport()
+    ids_b = torch.empty_like(ids)
+    d_b = torch.empty_like(d)
+
+    def step_bf16():
+        _lib.check(lib.mann_knn_graph_batched_device(pb, X.data_ptr(), offs.ctypes.data, 64, 32, 0, ids_b.data_ptr(),
+                                                     d_b.data_ptr(), rb, stream_ptr))
+
+    for _ in range(2):
+        step_bf16()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        step_bf16()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    bf16_ms = e0.elapsed_time(e1) / reps
+    bf16_form = {"ms_per_step": bf16_ms, "points_per_s": N / (bf16_ms / 1e3),
+                 "rows_fallback": rb.rows_fallback, "candidates_per_query": rb.candidates / N,
+                 "equals_fp32_form": bool(torch.equal(ids_b, ids) and torch.equal(d_b, d))}
     # the graphs' consumer: a local PCA (intrinsic dimension 2) at every node
     offs_rows = np.repeat(offs[:-1], np.diff(offs)).astype(np.int32)
     glob = ids + torch.from_numpy(offs_rows).cuda()[:, None]
@@ -574,7 +597,7 @@ def run_batched_leg(args, stream_ptr=0):
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": pk["tflops"], "unit": "TFLOP/s",
                          "frac": achieved / pk["tflops"], "peak_source": "measured FP32 FMA rate (" + pk["how"] + ")",
                          "peak_sm_mhz": pk["sm_mhz"], "work": "2*d flops per ordered pair"},
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu, "bf16_form": bf16_form,
             "launches_per_step": r.launches,
             "local_pca": {"ms": pca_ms, "nodes_per_s": N / (pca_ms / 1e3), "neighbours": 15, "intrinsic_dim": 2},
             "edge_weights": {"rule": "CurvatureFreeSymmetric", "ms": wt_ms, "edges_per_s": N * 15 / (wt_ms / 1e3)}}
@@ -635,7 +658,8 @@ def run_angular_leg(args, stream_ptr=0):
     stream = torch.cuda.current_stream()
     out = {"workload": ANG_WORKLOAD}
     res = {}
-    for name, prec, reps in (("bf16", _lib.PREC_BF16, max(3, min(args.steps, 10))), ("fp32", _lib.PREC_FP32, 2)):
+    for name, prec, reps in (("bf16", _lib.PREC_BF16, max(3, min(args.steps, 10))), ("fp8", _lib.PREC_FP8, 3),
+                             ("fp32", _lib.PREC_FP32, 2)):
         p = _lib.params(_lib.METRIC_COSINE, k, prec)
         r = _lib.KnnReport()
 
@@ -655,10 +679,12 @@ def run_angular_leg(args, stream_ptr=0):
         ms = e0.elapsed_time(e1) / reps
         res[name] = (ids.cpu().numpy().copy(), dd.cpu().numpy().copy())
         out[name] = {"ms": ms, "qps": nq / (ms / 1e3), "rows_fallback": r.rows_fallback,
-                     "candidates_per_query": r.candidates / nq if prec == _lib.PREC_BF16 else None}
+                     "candidates_per_query": r.candidates / nq if prec != _lib.PREC_FP32 else None}
     out["bf16_over_fp32"] = out["bf16"]["qps"] / out["fp32"]["qps"]
     out["bf16_equals_fp32_form"] = bool(np.array_equal(res["bf16"][0], res["fp32"][0]) and
                                         np.array_equal(res["bf16"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
+    out["fp8_equals_fp32_form"] = bool(np.array_equal(res["fp8"][0], res["fp32"][0]) and
+                                       np.array_equal(res["fp8"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
     peak_tf, _, _, src = measured_peaks()
     flops = 2.0 * d * n * nq
     ach = flops / (out["bf16"]["ms"] / 1e3) / 1e12
@@ -865,6 +891,29 @@ def run_ours(args):
     e1r, e2r = step(_lib.PREC_BF16, HEAD | _lib.FLAG_FP64_ERR)
     same_again = bool(np.array_equal(bf16_i[0], qi.cpu().numpy()) and np.array_equal(bf16_i[1], gi.cpu().numpy()))
 
+    # ---- the FP8 (e4m3) form on the held-out query batch (its certified window
+    # is wide, so most rows fall back to the exact FP32 scan)
+    fp8 = None
+    if not args.no_fp8:
+        pf = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, _lib.PREC_FP8)
+        rf = _lib.KnnReport()
+        for _ in range(2):
+            _lib.check(lib.mann_knn_device(pf, tb.data_ptr(), N_POINTS, tq.data_ptr(), N_QUERIES, DIM,
+                                           qi.data_ptr(), qd.data_ptr(), rf, sp))
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            _lib.check(lib.mann_knn_device(pf, tb.data_ptr(), N_POINTS, tq.data_ptr(), N_QUERIES, DIM,
+                                           qi.data_ptr(), qd.data_ptr(), rf, sp))
+        e1.record(stream)
+        barrier()
+        fms = e0.elapsed_time(e1) / 2
+        fp8 = {"workload": "the 10,000 held-out queries against the 60,000 points", "ms": fms,
+               "qps": N_QUERIES / (fms / 1e3), "rows_fallback": rf.rows_fallback,
+               "candidates_per_query": rf.candidates / N_QUERIES,
+               "ids_equal_bf16_form": bool(np.array_equal(qi.cpu().numpy(), bf16_i[0]))}
+
     # ---- the plain FP32 form on the same step
     step(_lib.PREC_FP32)
     barrier()
@@ -975,7 +1024,7 @@ def run_ours(args):
             "rows_unresolved_total": unresolved,
             "candidates_per_query": cands / (args.steps * qps_step),
             "e2e": e2e, "roofline": roof, "cpu_baseline": cpu, "clocks": clocks,
-            "gpu_launches": launches, "plain_fp32": plain, "ivf_learned_probe": ivf, "batched_graphs": batched,
+            "fp8_form": fp8, "gpu_launches": launches, "plain_fp32": plain, "ivf_learned_probe": ivf, "batched_graphs": batched,
             "angular_cosine": angular, "fp32_peak": fp32_peak() if (plain or batched) else None,
             "post_timing_s": time.perf_counter() - t0}
     print(json.dumps(line), flush=True)

@@ -43,6 +43,9 @@ typedef int32_t mann_status;
 /* Arithmetic forms of the exact search */
 #define MANN_PREC_FP32 0 /* FP32 difference-form tiles + fused top-k (reference semantics) */
 #define MANN_PREC_BF16 1 /* BF16 tcgen05 tiles, certified top-(k+m), exact FP32 rerank */
+#define MANN_PREC_FP8 2  /* FP8-e4m3 tcgen05 tiles with per-row power-of-two scales, certified
+                            top-(k+m), exact FP32 rerank (never chosen by AUTO: its certified
+                            window is far wider than BF16's on the measured sets) */
 #define MANN_PREC_AUTO 3 /* library picks (BF16 form when d >= 128 and the metric is L2) */
 
 /* Flags */
@@ -75,7 +78,7 @@ typedef struct {
   int64_t launches;          /* kernels this call launched */
   int64_t rows_ties_widened; /* MANN_FLAG_FP64_TIES: rows whose tie at the k-th distance reached
                                 past the candidate list and were re-ordered from their exact
-                                FP32 top-256 */
+                                FP32 top-64 (top-256 when longer) */
   int64_t rows_unresolved;   /* MANN_FLAG_FP64_TIES: rows whose tie cluster is longer than that
                                 (they keep the FP32 (distance, id) order); 0 in every test */
 } mann_knn_report;

@@ -26,6 +26,7 @@ METRIC_COSINE = 2
 
 PREC_FP32 = 0
 PREC_BF16 = 1
+PREC_FP8 = 2
 PREC_AUTO = 3
 
 FLAG_FP64_TIES = 1

@@ -365,7 +365,7 @@ mann_status mann_knn_graph_batched_device(const mann_knn_params* p, const float*
                                     report));
   if (report) {
     report->rows = set_offsets[nsets];
-    report->precision_used = MANN_PREC_FP32;
+    report->precision_used = p->precision == MANN_PREC_BF16 ? MANN_PREC_BF16 : MANN_PREC_FP32;
     report->launches = launch_count() - l0;
     report->kernel_ms = -1;
     if (ctx->timing && ctx->timed) {
@@ -402,7 +402,7 @@ mann_status mann_knn_graph_batched(const mann_knn_params* p, const float* data, 
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
   if (report) {
     report->rows = N;
-    report->precision_used = MANN_PREC_FP32;
+    report->precision_used = p->precision == MANN_PREC_BF16 ? MANN_PREC_BF16 : MANN_PREC_FP32;
     report->launches = launch_count() - l0;
     report->kernel_ms = -1;
   }

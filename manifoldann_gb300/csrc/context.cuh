@@ -76,6 +76,8 @@ enum ScratchSlot : int {
   SLOT_SEG_RUNS,      // batched BF16 graphs: the items of each block
   SLOT_SEG_ROWRUN,    // batched BF16 graphs: each row's block
   SLOT_SEG_QUEUE,     // batched BF16 graphs: fallback work-queue header
+  SLOT_FP8_SCALE_B,   // FP8 form: per-point 1/f
+  SLOT_FP8_SCALE_Q,   // FP8 form: per-query 1/f
   SLOT_COS_B,         // BF16 cosine: unit-normalised points
   SLOT_COS_Q,         // BF16 cosine: unit-normalised queries
   SLOT_COS_NB,        // BF16 cosine: squared norms of the points
@@ -90,11 +92,16 @@ enum ScratchSlot : int {
   SLOT_CSR_ROWS,      // host-pointer union graph: row offsets
   SLOT_FP64_ERR,      // maximum FP64 error of the returned distances
   SLOT_TIES_ROWS,     // FP64 ties: rows whose boundary tie reached past the candidates
+  SLOT_TIES_ROWS2,    // FP64 ties: rows still unsettled after the top-64 widening
+  SLOT_TIES_ROWS3,    // FP64 ties: rows still unsettled after the top-256 widening
   SLOT_TIES_PARTIAL,  // FP64 ties: their wider FP32 lists (per split)
   SLOT_TIES_KEYS,     // FP64 ties: their wider FP32 lists (merged)
   SLOT_TIES_CNT,      // FP64 ties: candidate counts of the wider lists
   SLOT_TIES_FLOOR,    // FP64 ties: floors of the wider lists
   SLOT_TIES_COUNTERS, // FP64 ties: counters of the second resolve
+  SLOT_TIES_TASKS,    // FP64 ties: (row, position, point) tasks
+  SLOT_TIES_VALS,     // FP64 ties: FP64 distances by (row, position)
+  SLOT_TIES_STATE,    // FP64 ties: rows to reorder
   SLOT_COUNT
 };
 

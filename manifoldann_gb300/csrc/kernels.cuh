@@ -29,9 +29,10 @@ mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, in
 
 // BF16 tensor-core form (SqEuclidean / Euclidean): certified candidates,
 // exact FP32 rerank, optional FP64 near-tie order.  Result: keys [nq][kreq].
+// fp8: the same search with E4M3 tiles (per-row power-of-two scales, kind::f8f6f4).
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
-                          bool fp64, uint64_t** out_keys, mann_knn_report* rep);
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, bool fp8 = false);
 
 // Self-kNN keys [N][kreq] (global ids, the row itself included) of many point
 // sets stored back to back (set c = rows [offs[c], offs[c+1])), each against
@@ -43,9 +44,10 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
 // Orders near-ties of sorted FP32 candidate lists by FP64 distance (when fp64)
 // and truncates them to kreq keys.  counters[0] += rows re-ordered,
 // counters[1] += rows whose boundary tie could not be settled (their query
-// rows appended to unres_rows when it is not NULL).  Candidate row i belongs
+// rows appended to unres_rows when it is not NULL), counters[2] is the FP64
+// task count (must start at 0).  Candidate row i belongs
 // to query / output row rows[i] (identity when rows is NULL).
-mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
+mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
                            cudaStream_t s, const int32_t* rows = nullptr, int32_t* unres_rows = nullptr);

@@ -35,6 +35,7 @@
 //   Rs = R_q + max R_p.  A slack of 3 (d+2) u U keeps every point that could
 //   enter the FP32 top-k or tie with its k-th FP32 distance.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <cmath>
@@ -71,8 +72,13 @@ constexpr int SEED_SAMPLE = 2048;                    // points sampled by the se
 constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
-constexpr double BAND_MIN_BYTES = 96.0 * (1 << 20);  // point operands above this are walked in bands
-constexpr double BAND_BYTES = 48.0 * (1 << 20);      // point-operand bytes per band
+// Bands and CTA pairs are built but not selected: on one GB300 the
+// phase-aligned single-band walk beat 48 MB bands (1M x 128: 8.2 vs 11.8 ms;
+// 290k x 256 cosine: 5.5 vs 6.1 ms) and single CTAs beat cta_group::2 pairs
+// (60k x 784 self graph: 4.50 vs 4.75 ms per main pass), CUDA events.
+constexpr double BAND_MIN_BYTES = 1e30;          // point operands above this are walked in bands
+constexpr double BAND_BYTES = 48.0 * (1 << 20);  // point-operand bytes per band
+constexpr bool K2_USE_PAIRS = false;
 
 enum : int { ERR_TIMEOUT_PRODUCER = 1, ERR_TIMEOUT_MMA = 2, ERR_TIMEOUT_EPI = 3 };
 
@@ -286,6 +292,84 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   }
 }
 
+// One warp per row: the FP8 (e4m3) form of scale*(x - mu).  The row gets
+// its own power-of-two factor f = 2^e with max|cv| f <= 448 (e4m3's largest
+// finite value), x8 = e4m3(cv f) (round to nearest, finite), and x~ = x8 / f
+// exactly; `rscale` receives 1/f, the factor that turns the tensor core's
+// sum of x8 products back into x~ units.  Bound terms as convert_rows_kernel.
+__global__ void convert_rows_fp8_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
+                                        const float* __restrict__ mu, const float* __restrict__ scale_ptr,
+                                        uint8_t* __restrict__ x8, float* __restrict__ rscale,
+                                        RowInfo* __restrict__ info, float* __restrict__ norms,
+                                        BaseMax* __restrict__ bmax) {
+  const int lane = threadIdx.x & 31;
+  const float scale = *scale_ptr;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  __shared__ unsigned blk_max[2];
+  if (threadIdx.x < 2) blk_max[threadIdx.x] = 0u;
+  __syncthreads();
+  const bool valid = row < n;
+  const float* xr = x + (valid ? row : 0) * d;
+  uint8_t* br = x8 + (valid ? row : 0) * (int64_t)dp;
+  // the row's largest magnitude
+  float amax = 0.0f;
+  for (int c = lane; valid && c < d; c += 32)
+    amax = fmaxf(amax, fabsf(__fmul_rn(scale, __fsub_rn(__ldg(xr + c), __ldg(mu + c)))));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(FULL, amax, o));
+  float f = 1.0f;
+  if (amax > 0.0f && amax < 3.0e38f) {
+    f = exp2f(floorf(log2f(448.0f / amax)));
+    while (amax * f > 448.0f) f *= 0.5f;
+    while (amax * (2.0f * f) <= 448.0f) f *= 2.0f;
+  }
+  // keep the product of two rows' 1/f factors (and -2) a normal FP32 number
+  f = fminf(fmaxf(f, 0x1p-40f), 0x1p40f);
+  const float inv = 1.0f / f;  // a power of two: exact
+  float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f;
+  for (int c = lane; valid && c < dp; c += 32) {
+    float cv = 0.0f;
+    if (c < d) cv = __fmul_rn(scale, __fsub_rn(__ldg(xr + c), __ldg(mu + c)));
+    const __nv_fp8_storage_t q8 = __nv_cvt_float_to_fp8(cv * f, __NV_SATFINITE, __NV_E4M3);
+    const float bv = __half2float(__half(__nv_cvt_fp8_to_halfraw(q8, __NV_E4M3))) * inv;
+    br[c] = (uint8_t)q8;
+    const float rv = cv - bv;  // exact: bv is cv rounded to fewer bits
+    f_b = __fmaf_rn(bv, bv, f_b);
+    f_r = __fmaf_rn(rv, rv, f_r);
+    f_c = __fmaf_rn(cv, cv, f_c);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    f_b += __shfl_xor_sync(FULL, f_b, o);
+    f_r += __shfl_xor_sync(FULL, f_r, o);
+    f_c += __shfl_xor_sync(FULL, f_c, o);
+  }
+  if (lane == 0 && valid) {
+    const float rel = (float)((dp + 31) / 32 + 2 + 5) * 5.9604644775390625e-08f;  // exact
+    const float onep = __fadd_ru(1.0f, rel);
+    RowInfo ri;
+    ri.nrm = f_b;
+    ri.xn_up = __fsqrt_ru(__fmul_ru(f_b, onep));
+    ri.r_up = __fadd_ru(__fsqrt_ru(__fmul_ru(f_r, onep)),
+                        __fmul_ru(__fmul_ru(1.1920928955078125e-07f, 1.0000002f), __fsqrt_ru(__fmul_ru(f_c, onep))));
+    ri.lo_up = 0.0f;
+    info[row] = ri;
+    rscale[row] = inv;
+    if (norms) norms[row] = ri.nrm;
+    if (bmax) {
+      atomicMax(&blk_max[0], __float_as_uint(ri.xn_up));
+      atomicMax(&blk_max[1], __float_as_uint(ri.r_up));
+    }
+  }
+  if (bmax) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      atomicMax(&bmax->xn_bits, blk_max[0]);
+      atomicMax(&bmax->r_bits, blk_max[1]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- main kernel
 
 // Order of the (query block, point tile) items.  With one band the items
@@ -354,6 +438,8 @@ struct MainArgs {
   int d, dp, nkb;
   Walk w;
   const TileItem* titems;  // segmented pass (NULL: the banded walk of `w`)
+  const float* qscale;     // FP8 form: per query row, 1/f of its e4m3 scaling (NULL otherwise)
+  const float* bscale;     // FP8 form: per point, 1/f (row p * bstride)
   int smax;           // partial-list slots per query
   int L;              // list capacity (32)
   int depth;          // admission depth = k + margin (<= L)
@@ -490,12 +576,19 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 // rescanned for the new largest (independent loads, conflict-free while the
 // lanes run in step; a sorted insert would be a chain of dependent
 // shared-memory loads).
-__device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, uint64_t* __restrict__ mylist,
+template <bool FP8>
+__device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, float csv, float rs,
+                                          uint64_t* __restrict__ mylist,
                                           uint64_t& thr_key, float& thr_est, uint64_t seed_key,
                                           int& lslot, int& nfill, uint32_t col0, int depth) {
+  // est' = ||p~||^2 - 2 q~.p~; in the FP8 form the accumulator holds the sum of
+  // e4m3 products and -2 (1/f_q) (1/f_p) = rs * csv (a power of two) rescales it
   float e[32];
 #pragma unroll
-  for (int j = 0; j < 32; ++j) e[j] = __fmaf_rn(-2.0f, __uint_as_float(v[j]), __shfl_sync(FULL, nbv, j));
+  for (int j = 0; j < 32; ++j) {
+    const float coef = FP8 ? rs * __shfl_sync(FULL, csv, j) : -2.0f;
+    e[j] = __fmaf_rn(coef, __uint_as_float(v[j]), __shfl_sync(FULL, nbv, j));
+  }
   float m4[8];
 #pragma unroll
   for (int j4 = 0; j4 < 8; ++j4)
@@ -545,16 +638,20 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, ui
 // first column, so each comes from a distinct point).  SEED_DEPTH distinct
 // points lie at or below the SEED_DEPTH-th of them, so it bounds the row's
 // SEED_DEPTH-th smallest est' over the sample from above -- all a seed needs.
-__device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, uint64_t (&top)[SEED_DEPTH],
-                                           uint32_t col0) {
+template <bool FP8>
+__device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, float csv, float rs,
+                                           uint64_t (&top)[SEED_DEPTH], uint32_t col0) {
   float m4[8];
 #pragma unroll
   for (int j4 = 0; j4 < 8; ++j4) {
-    float e0 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 0]), __shfl_sync(FULL, nbv, 4 * j4 + 0));
-    float e1 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 1]), __shfl_sync(FULL, nbv, 4 * j4 + 1));
-    float e2 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 2]), __shfl_sync(FULL, nbv, 4 * j4 + 2));
-    float e3 = __fmaf_rn(-2.0f, __uint_as_float(v[4 * j4 + 3]), __shfl_sync(FULL, nbv, 4 * j4 + 3));
-    m4[j4] = fminf(fminf(e0, e1), fminf(e2, e3));
+    float e4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = 4 * j4 + u;
+      const float coef = FP8 ? rs * __shfl_sync(FULL, csv, j) : -2.0f;
+      e4[u] = __fmaf_rn(coef, __uint_as_float(v[j]), __shfl_sync(FULL, nbv, j));
+    }
+    m4[j4] = fminf(fminf(e4[0], e4[1]), fminf(e4[2], e4[3]));
   }
   const float mn = fminf(fminf(fminf(m4[0], m4[1]), fminf(m4[2], m4[3])),
                          fminf(fminf(m4[4], m4[5]), fminf(m4[6], m4[7])));
@@ -604,11 +701,13 @@ static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2)
 // commits arrive on the stage and accumulator barriers of both CTAs, and both
 // CTAs' epilogue warps release an accumulator on the even CTA's barrier.  The
 // work unit (a walk item) is then one pair tile and `a.w.grid` counts pairs.
-template <int CAP, int NSETS, bool PAIR>
+template <int CAP, int NSETS, bool PAIR, bool FP8>
 __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
             MainArgs a) {
   constexpr int NEPI = 4 * NSETS;
+  constexpr int EPS = FP8 ? 128 : BK;  // operand elements per 128-byte stage row
+  constexpr int EPK = EPS / 4;         // elements per MMA (K): 16 BF16 or 32 E4M3
   constexpr int STAGES = Stg<PAIR>::N;
   constexpr int STAGE_BYTES = Stg<PAIR>::BYTES;
   constexpr int QROWS = PAIR ? 2 * BM : BM;  // query rows of one work unit
@@ -681,12 +780,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           if (PAIR) {
             if (rank == 0) ptx::mbar_arrive_expect_tx(&full_bar[s], 2 * STAGE_BYTES);
             const uint32_t fb = full0 + (uint32_t)s * 8u;
-            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * BK, (int)v.q0 + (int)rank * BM);
-            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * BK, (int)v.c0 + (int)rank * Stg<PAIR>::B_ROWS);
+            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * EPS, (int)v.q0 + (int)rank * BM);
+            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * EPS, (int)v.c0 + (int)rank * Stg<PAIR>::B_ROWS);
           } else {
             ptx::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * BK, (int)v.q0);
-            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * BK, (int)v.c0);
+            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * EPS, (int)v.q0);
+            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * EPS, (int)v.c0);
           }
         }
       }
@@ -694,7 +793,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0 && rank == 0) {
-      constexpr uint32_t idesc = ptx::idesc_bf16_f32(QROWS, BN);
+      constexpr uint32_t idesc = FP8 ? ptx::idesc_e4m3_f32(QROWS, BN) : ptx::idesc_bf16_f32(QROWS, BN);
       uint32_t it = 0;
       int tcount = 0;
       bool ok = true;
@@ -716,13 +815,15 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           ptx::tc_fence_after();
           const uint32_t sa = ptx::smem_u32(stage_base + s * STAGE_BYTES);
           const uint32_t sb = sa + A_STAGE_BYTES;
-          const int rem = a.dp - kb * BK;  // valid (zero-padded) columns left
-          const int ksteps = rem >= BK ? BK / 16 : (rem + 15) / 16;
-          for (int kk = 0; kk < ksteps; ++kk) {
+          const int rem = a.dp - kb * EPS;  // valid (zero-padded) columns left
+          const int ksteps = rem >= EPS ? 4 : (rem + EPK - 1) / EPK;
+          for (int kk = 0; kk < ksteps; ++kk) {  // each MMA covers 32 bytes of K
             const uint64_t ad = ptx::sw128_desc(sa + kk * 32);
             const uint64_t bd = ptx::sw128_desc(sb + kk * 32);
             if (PAIR)
               ptx::mma_f16_pair(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            else if (FP8)
+              ptx::mma_f8(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
             else
               ptx::mma_f16(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
           }
@@ -794,12 +895,15 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     // point norms, lane j holding column 32 i + j of the tile in nbc[i]: the
     // current tile's in nbc, the next tile's fetched into nbn one tile ahead
     float nbn[BN / 32], nbc[BN / 32];
+    float csn[FP8 ? BN / 32 : 1], csc[FP8 ? BN / 32 : 1];  // FP8: -2 (1/f) of the columns
+    float rs = 1.0f;                                        // FP8: 1/f of this lane's row
     auto fetch_norms = [&](int64_t st_) {
       const ItemView v_ = view_item(a, walk_item(it0, it1, a.w, st_), QROWS);
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) {
         const int64_t col = v_.c0 + lane + 32 * i;
         nbn[i] = col < v_.cend ? __ldg(&a.bnorm[col * a.bstride]) : INF;
+        if constexpr (FP8) csn[i] = col < v_.cend ? -2.0f * __ldg(&a.bscale[col * a.bstride]) : 0.0f;
       }
     };
     if (it1 > it0) fetch_norms(0);
@@ -817,6 +921,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         seg_slot = (v.slot_base + (cta - cta_of(v.run_first, a.w.work, a.w.grid))) * NSETS + set;
         const int64_t gq = v.q0 + row0 + row;
         seed_key = (a.seed != nullptr && gq < v.qend) ? make_key(a.seed[gq], 0u) : KEY_NONE;
+        if constexpr (FP8) rs = gq < v.qend ? __ldg(&a.qscale[gq]) : 0.0f;
         thr_key = seed_key;
         thr_est = thr_key == KEY_NONE ? INF : key_dist(thr_key);
         lslot = 0;
@@ -826,6 +931,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       const int64_t col0 = v.c0;
 #pragma unroll
       for (int i = 0; i < BN / 32; ++i) nbc[i] = nbn[i];
+      if constexpr (FP8) {
+#pragma unroll
+        for (int i = 0; i < BN / 32; ++i) csc[i] = csn[i];
+      }
       if (st + 1 < it1 - it0) fetch_norms(st + 1);
       const uint32_t tph = (tcount >> 1) & 1;
       if (alive && !ptx::mbar_wait(&tfull_bar[buf], tph, a.err, ERR_TIMEOUT_EPI)) alive = false;
@@ -842,11 +951,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
+        const float cs_a = FP8 ? pick(csc, ch) : 0.0f;
         if (a.seedmode)
-          seed_chunk(va, pick(nbc, ch), top, (uint32_t)(col0 + ch * 32));
+          seed_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, top, (uint32_t)(col0 + ch * 32));
         else
-          epi_chunk(va, pick(nbc, ch), mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                    (uint32_t)(col0 + ch * 32), a.depth);
+          epi_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                         (uint32_t)(col0 + ch * 32), a.depth);
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
@@ -861,11 +971,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             ptx::mbar_arrive(&tempty_bar[buf]);
           }
         }
+        const float cs_b = FP8 ? pick(csc, ch + 1) : 0.0f;
         if (a.seedmode)
-          seed_chunk(vb, pick(nbc, ch + 1), top, (uint32_t)(col0 + (ch + 1) * 32));
+          seed_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, top, (uint32_t)(col0 + (ch + 1) * 32));
         else
-          epi_chunk(vb, pick(nbc, ch + 1), mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                    (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+          epi_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                         (uint32_t)(col0 + (ch + 1) * 32), a.depth);
         ptx::tmem_ld_wait();
       }
     }
@@ -1357,22 +1468,45 @@ __device__ __forceinline__ double fp64_dist_row(const float* __restrict__ x,
   return metric == MANN_METRIC_EUCLIDEAN ? sqrt(s) : s;
 }
 
-// One warp per candidate row i.  cand[i][0..count) sorted by (fp32, id);
-// the row belongs to query (and output row) q = rows[i] (rows == NULL: q = i).
-// Writes the first kreq keys to keys_out[q], ordering near-tie clusters by
-// FP64 when asked.  A row whose boundary tie cluster may reach past its
-// candidates is counted in n_unresolved and, when unres_rows is given, its q
-// is appended there (the caller widens those rows' candidates and resolves
-// them again).
-__global__ void resolve_kernel(const float* __restrict__ base, const float* __restrict__ qs,
-                               int d, int metric, int64_t nq, int L, int kreq, int fp64,
-                               const uint64_t* __restrict__ cand, const int* __restrict__ cand_count,
-                               const float* __restrict__ floor_val, uint64_t* __restrict__ keys_out,
-                               unsigned long long* __restrict__ n_fp64_rows,
-                               unsigned long long* __restrict__ n_unresolved,
-                               const int32_t* __restrict__ rows, int32_t* __restrict__ unres_rows) {
+// Clusters of adjacent candidates whose FP32 distances lie within the FP32
+// rounding bound of each other: cl[p] = first position of p's cluster.
+__device__ __forceinline__ void tie_clusters(const uint64_t* key, int cm, int d, int metric, int* cl) {
+  const double eps = (double)(d + 2) * 5.9604644775390625e-08 * 1.01 + 1.2e-7;
+  int start = 0;
+  cl[0] = 0;
+  for (int p = 1; p < cm; ++p) {
+    const double a = (double)key_dist(key[p - 1]);
+    const double b = (double)key_dist(key[p]);
+    // FP32 cosine distances carry an absolute error of order (d+4)u
+    const bool link = metric == MANN_METRIC_COSINE ? (b - a) <= 2.0 * eps + 4.8e-7
+                                                   : (b - a) <= eps * (fabs(a) + fabs(b));
+    if (!link) start = p;
+    cl[p] = start;
+  }
+}
+
+struct TieTask {  // one FP64 distance to compute: candidate row i, position p, point id
+  int64_t i;
+  int32_t p, id;
+};
+
+// Pass 1 of the FP64 near-tie order (one warp per candidate row i; the row
+// belongs to query / output row q = rows[i], or i).  cand[i][0..count) is
+// sorted by (fp32, id).  Writes the first kreq keys to keys_out[q] in FP32
+// order; when `fp64` and the cluster holding position kreq-1 is a real tie,
+// the row is marked (state[i] = 1) and every member of the clusters up to
+// that one becomes a task of the compacted list (task_count[0] entries), so
+// pass 2 runs 32 FP64 sums per warp.  A row whose boundary cluster may reach
+// past its candidates is counted in n_unresolved and, with unres_rows, listed.
+__global__ void resolve_mark_kernel(int d, int metric, int64_t nq, int L, int kreq, int fp64,
+                                    const uint64_t* __restrict__ cand, const int* __restrict__ cand_count,
+                                    const float* __restrict__ floor_val, uint64_t* __restrict__ keys_out,
+                                    unsigned long long* __restrict__ n_fp64_rows,
+                                    unsigned long long* __restrict__ n_unresolved,
+                                    unsigned long long* __restrict__ task_count, TieTask* __restrict__ tasks,
+                                    int8_t* __restrict__ state, const int32_t* __restrict__ rows,
+                                    int32_t* __restrict__ unres_rows) {
   __shared__ uint64_t s_key[4][256];
-  __shared__ double s_val[4][256];
   __shared__ int s_cl[4][256];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * 4 + w;
@@ -1381,35 +1515,21 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
   const uint64_t* cq = cand + i * L;
   const int c = min(cand_count[i], L);
   uint64_t* out = keys_out + q * kreq;
-  if (!fp64 || c <= 1) {
-    for (int e = lane; e < kreq; e += 32) out[e] = e < c ? cq[e] : KEY_NONE;
-    return;
-  }
+  for (int e = lane; e < kreq; e += 32) out[e] = e < c ? cq[e] : KEY_NONE;
+  if (state && lane == 0) state[i] = 0;
+  if (!fp64 || c <= 1) return;
   const int cm = min(c, 256);
   for (int e = lane; e < cm; e += 32) s_key[w][e] = cq[e];
   __syncwarp();
-  const double eps = (double)(d + 2) * 5.9604644775390625e-08 * 1.01 + 1.2e-7;
-  if (lane == 0) {
-    // clusters of adjacent positions whose FP32 distances are within the rounding bound
-    int start = 0;
-    s_cl[w][0] = 0;
-    for (int p = 1; p < cm; ++p) {
-      const double a = (double)key_dist(s_key[w][p - 1]);
-      const double b = (double)key_dist(s_key[w][p]);
-      // FP32 cosine distances carry an absolute error of order (d+4)u
-      const bool link = metric == MANN_METRIC_COSINE ? (b - a) <= 2.0 * eps + 4.8e-7
-                                                     : (b - a) <= eps * (fabs(a) + fabs(b));
-      if (!link) start = p;
-      s_cl[w][p] = start;
-    }
-  }
+  if (lane == 0) tie_clusters(s_key[w], cm, d, metric, s_cl[w]);
   __syncwarp();
   // the cluster holding position kreq-1 must end inside the candidate list
-  int end = kreq - 1;
-  if (end >= cm) end = cm - 1;
-  while (end + 1 < cm && s_cl[w][end + 1] == s_cl[w][kreq - 1 < cm ? kreq - 1 : cm - 1]) ++end;
+  const int kl = kreq - 1 < cm ? kreq - 1 : cm - 1;
+  int end = kl;
+  while (end + 1 < cm && s_cl[w][end + 1] == s_cl[w][kl]) ++end;
   bool resolvable = true;
   if (end == cm - 1) {
+    const double eps = (double)(d + 2) * 5.9604644775390625e-08 * 1.01 + 1.2e-7;
     const double lastv = (double)key_dist(s_key[w][cm - 1]);
     const double fl = (double)floor_val[i];
     const bool clear = metric == MANN_METRIC_COSINE ? lastv + 2.0 * eps + 4.8e-7 < fl
@@ -1418,43 +1538,98 @@ __global__ void resolve_kernel(const float* __restrict__ base, const float* __re
   }
   bool any_tie = false;
   for (int p = 1; p <= end; ++p)
-    if (s_cl[w][p] != p) { any_tie = true; break; }
+    if (s_cl[w][p] != p) {
+      any_tie = true;
+      break;
+    }
   if (!resolvable) {
     if (lane == 0) {
       const unsigned long long slot = atomicAdd(n_unresolved, 1ull);
       if (unres_rows) unres_rows[slot] = (int32_t)q;
     }
-  } else if (any_tie) {
-    const float* qrow = qs + q * d;
-    for (int p = lane; p <= end; p += 32) {
-      const bool member = (s_cl[w][p] != p) || (p + 1 <= end && s_cl[w][p + 1] == p);
-      s_val[w][p] = member ? fp64_dist_row(qrow, base + (int64_t)key_id(s_key[w][p]) * d, d, metric) : 0.0;
+    return;
+  }
+  if (!any_tie) return;
+  // members: positions <= end inside a cluster of two or more
+  unsigned long long base_slot = 0;
+  for (int p0 = 0; p0 <= end; p0 += 32) {
+    const int p = p0 + lane;
+    const bool member = p <= end && ((s_cl[w][p] != p) || (p + 1 <= end && s_cl[w][p + 1] == p));
+    const unsigned m = __ballot_sync(FULL, member);
+    if (lane == 0) base_slot = atomicAdd(task_count, (unsigned long long)__popc(m));
+    base_slot = __shfl_sync(FULL, base_slot, 0);
+    if (member) {
+      const unsigned long long slot = base_slot + __popc(m & ((1u << lane) - 1u));
+      tasks[slot] = TieTask{i, p, key_id(s_key[w][p])};
     }
-    __syncwarp();
-    if (lane == 0) {
-      atomicAdd(n_fp64_rows, 1ull);
-      // insertion sort inside each cluster by (fp64 distance, id)
-      int p = 0;
-      while (p <= end) {
-        int e = p;
-        while (e + 1 <= end && s_cl[w][e + 1] == p) ++e;
-        for (int i = p + 1; i <= e; ++i) {
-          const uint64_t kk = s_key[w][i];
-          const double vv = s_val[w][i];
-          int j = i - 1;
-          while (j >= p && (s_val[w][j] > vv || (s_val[w][j] == vv && key_id(s_key[w][j]) > key_id(kk)))) {
-            s_key[w][j + 1] = s_key[w][j];
-            s_val[w][j + 1] = s_val[w][j];
-            --j;
-          }
-          s_key[w][j + 1] = kk;
-          s_val[w][j + 1] = vv;
+  }
+  if (lane == 0) {
+    state[i] = 1;
+    atomicAdd(n_fp64_rows, 1ull);
+  }
+}
+
+// Pass 2: the FP64 distance of every task (one thread each), the sequential
+// sum of the FP64 oracle; vals[i][p].
+__global__ void resolve_fp64_kernel(const float* __restrict__ base, const float* __restrict__ qs, int d, int metric,
+                                    int L, const unsigned long long* __restrict__ task_count,
+                                    const TieTask* __restrict__ tasks, const int32_t* __restrict__ rows,
+                                    double* __restrict__ vals) {
+  const unsigned long long cnt = *task_count;
+  for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < cnt;
+       t += (unsigned long long)gridDim.x * blockDim.x) {
+    const TieTask tk = tasks[t];
+    const int64_t q = rows ? (int64_t)rows[tk.i] : tk.i;
+    vals[tk.i * L + tk.p] = fp64_dist_row(qs + q * d, base + (int64_t)tk.id * d, d, metric);
+  }
+}
+
+// Pass 3 (one warp per marked row): insertion sort of each cluster up to the
+// boundary one by (FP64 distance, id); the first kreq keys go out.
+__global__ void resolve_sort_kernel(int d, int metric, int64_t nq, int L, int kreq,
+                                    const uint64_t* __restrict__ cand, const int* __restrict__ cand_count,
+                                    const int8_t* __restrict__ state, const double* __restrict__ vals,
+                                    uint64_t* __restrict__ keys_out, const int32_t* __restrict__ rows) {
+  __shared__ uint64_t s_key[4][256];
+  __shared__ double s_val[4][256];
+  __shared__ int s_cl[4][256];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * 4 + w;
+  if (i >= nq || state[i] == 0) return;
+  const int64_t q = rows ? (int64_t)rows[i] : i;
+  const uint64_t* cq = cand + i * L;
+  const int cm = min(min(cand_count[i], L), 256);
+  for (int e = lane; e < cm; e += 32) {
+    s_key[w][e] = cq[e];
+    s_val[w][e] = vals[i * L + e];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    tie_clusters(s_key[w], cm, d, metric, s_cl[w]);
+    const int kl = kreq - 1 < cm ? kreq - 1 : cm - 1;
+    int end = kl;
+    while (end + 1 < cm && s_cl[w][end + 1] == s_cl[w][kl]) ++end;
+    int p = 0;
+    while (p <= end) {
+      int e = p;
+      while (e + 1 <= end && s_cl[w][e + 1] == p) ++e;
+      for (int a = p + 1; a <= e; ++a) {
+        const uint64_t kk = s_key[w][a];
+        const double vv = s_val[w][a];
+        int j = a - 1;
+        while (j >= p && (s_val[w][j] > vv || (s_val[w][j] == vv && key_id(s_key[w][j]) > key_id(kk)))) {
+          s_key[w][j + 1] = s_key[w][j];
+          s_val[w][j + 1] = s_val[w][j];
+          --j;
         }
-        p = e + 1;
+        s_key[w][j + 1] = kk;
+        s_val[w][j + 1] = vv;
       }
+      p = e + 1;
     }
   }
   __syncwarp();
+  uint64_t* out = keys_out + q * kreq;
   for (int e = lane; e < kreq; e += 32) out[e] = e < cm ? s_key[w][e] : KEY_NONE;
 }
 
@@ -1497,15 +1672,31 @@ mann_status fp64_max_error(Context* ctx, cudaStream_t s, const float* base, cons
   return MANN_OK;
 }
 
-mann_status launch_resolve(const float* base, const float* qs, int d, int metric, int64_t nq, int L,
+mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
                            cudaStream_t s, const int32_t* rows, int32_t* unres_rows) {
   if (nq <= 0) return MANN_OK;
-  resolve_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(base, qs, d, metric, nq, L, kreq, fp64,
-                                                            cand, cand_count, floor_val, keys_out,
-                                                            counters, counters + 1, rows, unres_rows);
+  TieTask* tasks = nullptr;
+  double* vals = nullptr;
+  int8_t* state = nullptr;
+  if (fp64) {
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_TASKS, (size_t)nq * L, &tasks));
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_VALS, (size_t)nq * L, &vals));
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_STATE, (size_t)nq, &state));
+  }
+  const unsigned grid = (unsigned)ceil_div(nq, 4);
+  resolve_mark_kernel<<<grid, 128, 0, s>>>(d, metric, nq, L, kreq, fp64, cand, cand_count, floor_val, keys_out,
+                                           counters, counters + 1, counters + 2, tasks, state, rows, unres_rows);
   MANN_CHECK_LAUNCH();
+  if (fp64) {
+    resolve_fp64_kernel<<<(unsigned)ctx->num_sms * 8, 256, 0, s>>>(base, qs, d, metric, L, counters + 2, tasks,
+                                                                   rows, vals);
+    MANN_CHECK_LAUNCH();
+    resolve_sort_kernel<<<grid, 128, 0, s>>>(d, metric, nq, L, kreq, cand, cand_count, state, vals, keys_out,
+                                             rows);
+    MANN_CHECK_LAUNCH();
+  }
   return MANN_OK;
 }
 
@@ -1527,39 +1718,47 @@ __global__ void fp32_lists_to_cand_kernel(const uint64_t* __restrict__ keys, int
 }  // namespace
 
 // Rows whose boundary tie cluster reached past their candidates (listed in
-// unres_rows, h_unres of them): the exact FP32 top-min(n, KMAX_FUSED) of each
-// such row, then the FP64 near-tie order again, written over those rows of
-// keys_out.  Rows still unsettled (a tie cluster longer than that list) are
-// returned in *still_unresolved; they keep the FP32 (distance, id) order.
+// unres_rows, h_unres of them): their exact FP32 top-64, then the FP64
+// near-tie order again, written over those rows of keys_out; rows whose
+// cluster is longer still get their exact top-min(n, KMAX_FUSED).  Rows left
+// unsettled after that (a tie cluster longer than the list) are returned in
+// *still_unresolved; they keep the FP32 (distance, id) order.
 mann_status widen_unresolved(Context* ctx, cudaStream_t s, const float* base, const float* qs,
                              int64_t n, int d, int metric, int kreq, const float* qn,
                              const float* bn, const int32_t* unres_rows, int64_t h_unres,
                              uint64_t* keys_out, int64_t* still_unresolved) {
   *still_unresolved = 0;
-  if (h_unres <= 0) return MANN_OK;
-  const int kk = (int)std::min<int64_t>(n, KMAX_FUSED);
-  if (kk <= kreq) {  // every point is already a candidate: nothing lies beyond the list
-    return MANN_OK;
+  const int32_t* rows = unres_rows;
+  for (int stage = 0; stage < 2 && h_unres > 0; ++stage) {
+    const int kk = (int)std::min<int64_t>(n, stage == 0 ? 64 : KMAX_FUSED);
+    if (kk <= kreq || (stage == 1 && kk <= 64)) {  // every point is already a candidate
+      *still_unresolved = 0;
+      return MANN_OK;
+    }
+    uint64_t* fkeys = nullptr;
+    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_unres, d, metric, kk, rows, qn, bn, &fkeys,
+                           SLOT_TIES_PARTIAL, SLOT_TIES_KEYS));
+    int* cand_count = nullptr;
+    float* floor_val = nullptr;
+    unsigned long long* counters = nullptr;
+    int32_t* next_rows = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_CNT, (size_t)h_unres, &cand_count));
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_FLOOR, (size_t)h_unres, &floor_val));
+    MANN_TRY(ctx->scratch_t(SLOT_TIES_COUNTERS, 4, &counters));
+    MANN_TRY(ctx->scratch_t(stage == 0 ? SLOT_TIES_ROWS2 : SLOT_TIES_ROWS3, (size_t)h_unres, &next_rows));
+    MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
+    fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(h_unres, 128), 128, 0, s>>>(fkeys, h_unres, kk, cand_count,
+                                                                              floor_val);
+    MANN_CHECK_LAUNCH();
+    MANN_TRY(launch_resolve(ctx, base, qs, d, metric, h_unres, kk, kreq, 1, fkeys, cand_count, floor_val, keys_out,
+                            counters, s, rows, next_rows));
+    unsigned long long h[2] = {0, 0};
+    MANN_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s));
+    MANN_CUDA_TRY(cudaStreamSynchronize(s));
+    h_unres = (int64_t)h[1];
+    rows = next_rows;
+    *still_unresolved = h_unres;
   }
-  uint64_t* fkeys = nullptr;
-  MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_unres, d, metric, kk, unres_rows, qn, bn, &fkeys,
-                         SLOT_TIES_PARTIAL, SLOT_TIES_KEYS));
-  int* cand_count = nullptr;
-  float* floor_val = nullptr;
-  unsigned long long* counters = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_TIES_CNT, (size_t)h_unres, &cand_count));
-  MANN_TRY(ctx->scratch_t(SLOT_TIES_FLOOR, (size_t)h_unres, &floor_val));
-  MANN_TRY(ctx->scratch_t(SLOT_TIES_COUNTERS, 4, &counters));
-  MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
-  fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(h_unres, 128), 128, 0, s>>>(fkeys, h_unres, kk, cand_count,
-                                                                            floor_val);
-  MANN_CHECK_LAUNCH();
-  MANN_TRY(launch_resolve(base, qs, d, metric, h_unres, kk, kreq, 1, fkeys, cand_count, floor_val, keys_out,
-                          counters, s, unres_rows, nullptr));
-  unsigned long long h[2] = {0, 0};
-  MANN_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s));
-  MANN_CUDA_TRY(cudaStreamSynchronize(s));
-  *still_unresolved = (int64_t)h[1];
   return MANN_OK;
 }
 
@@ -1581,7 +1780,7 @@ mann_status fp32_then_resolve(Context* ctx, cudaStream_t s, const float* base, c
   fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(fkeys, nq, kk, cand_count,
                                                                        floor_val);
   MANN_CHECK_LAUNCH();
-  MANN_TRY(launch_resolve(base, qs, d, metric, nq, kk, kreq, 1, fkeys, cand_count, floor_val, keys,
+  MANN_TRY(launch_resolve(ctx, base, qs, d, metric, nq, kk, kreq, 1, fkeys, cand_count, floor_val, keys,
                           counters + 4, s, nullptr, unres));
   unsigned long long h[2] = {0, 0};
   MANN_CUDA_TRY(cudaMemcpyAsync(h, counters + 4, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -1620,16 +1819,19 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// rows of dp BF16 values; row r of the map is row r * row_step of the buffer
+// rows of dp BF16 values (E4M3 bytes with fp8); row r of the map is row
+// r * row_step of the buffer; boxes of 128 bytes x box_rows
 mann_status make_map(CUtensorMap* m, const void* ptr, int64_t rows, int dp, int box_rows,
-                     int64_t row_step = 1) {
+                     int64_t row_step = 1, bool fp8 = false) {
   EncodeTiledFn enc = encode_fn();
   if (!enc) return fail(MANN_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  const int es_bytes = fp8 ? 1 : 2;
   cuuint64_t dims[2] = {(cuuint64_t)dp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)dp * 2 * (cuuint64_t)row_step};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)dp * es_bytes * (cuuint64_t)row_step};
+  cuuint32_t box[2] = {(cuuint32_t)(128 / es_bytes), (cuuint32_t)box_rows};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box,
+  CUresult r = enc(m, fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                   const_cast<void*>(ptr), dims, strides, box,
                    es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(MANN_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -1645,10 +1847,10 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
 }
 
 // Launch of one k2_main instance: `units` CTAs, or `units` clusters of two CTAs (PAIR).
-template <int CAP, int NSETS, bool PAIR>
+template <int CAP, int NSETS, bool PAIR, bool FP8 = false>
 mann_status launch_k2(const CUtensorMap& mapA, const CUtensorMap& mapB, const MainArgs& ma, int units, size_t smem,
                       cudaStream_t s) {
-  auto fn = k2_main<CAP, NSETS, PAIR>;
+  auto fn = k2_main<CAP, NSETS, PAIR, FP8>;
   MANN_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(PAIR ? 2 * units : units));
@@ -1676,7 +1878,7 @@ int k2_pair_capacity(Context* ctx) {
   auto it = ctx->tune.find(key);
   if (it != ctx->tune.end()) return (int)it->second;
   int n = 0;
-  auto fn = k2_main<CAP, NSETS, true>;
+  auto fn = k2_main<CAP, NSETS, true, false>;
   const size_t smem = k2_smem_bytes<true>(CAP, NSETS);
   if (smem <= ctx->smem_optin &&
       cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess) {
@@ -1716,12 +1918,16 @@ struct SegPass {
 mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA, const void* bxb, int64_t bstride,
                           const RowInfo* qinfo, const RowInfo* binfo, const float* bnorm, int64_t n, int64_t nq,
                           int d, int dp, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
-                          bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr) {
+                          bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr,
+                          const float* qscale = nullptr, const float* bscale = nullptr) {
+  const bool fp8 = qscale != nullptr;
   // two epilogue sets with 16-entry lists when the depth allows it; each set
   // writes its own slot
   const int nsets = depth <= 16 ? 2 : 1;
   // CTA pairs (cta_group::2) when there are at least two 128-row query blocks
-  const int pairs = (nq > BM && !seg) ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx)) : 0;
+  const int pairs = (K2_USE_PAIRS && nq > BM && !seg && !fp8)
+                        ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx))
+                        : 0;
   const bool pair = pairs >= 1;
   const int qrows = pair ? 2 * BM : BM;
   const int64_t qblocks = ceil_div(nq, qrows);
@@ -1772,15 +1978,17 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   uint64_t* partial = nullptr;
   MANN_TRY(ctx->scratch_t(slot_partial, (size_t)nq * smax * LIST, &partial));
   CUtensorMap mapB;
-  MANN_TRY(make_map(&mapB, bxb, n, dp, pair ? Stg<true>::B_ROWS : Stg<false>::B_ROWS, bstride));
+  MANN_TRY(make_map(&mapB, bxb, n, dp, pair ? Stg<true>::B_ROWS : Stg<false>::B_ROWS, bstride, fp8));
   MainArgs ma;
   ma.nq = nq;
   ma.n = n;
   ma.d = d;
   ma.dp = dp;
-  ma.nkb = (int)ceil_div(dp, BK);
+  ma.nkb = (int)ceil_div(dp, fp8 ? 128 : BK);
   ma.w = w;
   ma.titems = seg ? seg->items : nullptr;
+  ma.qscale = qscale;
+  ma.bscale = bscale;
   ma.smax = smax;
   ma.L = LIST;
   ma.depth = depth;
@@ -1801,6 +2009,11 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
       MANN_TRY((launch_k2<16, 2, true>(mapA, mapB, ma, w.grid, smem, s)));
     else
       MANN_TRY((launch_k2<32, 1, true>(mapA, mapB, ma, w.grid, smem, s)));
+  } else if (fp8) {
+    if (nsets == 2)
+      MANN_TRY((launch_k2<16, 2, false, true>(mapA, mapB, ma, w.grid, smem, s)));
+    else
+      MANN_TRY((launch_k2<32, 1, false, true>(mapA, mapB, ma, w.grid, smem, s)));
   } else {
     if (nsets == 2)
       MANN_TRY((launch_k2<16, 2, false>(mapA, mapB, ma, w.grid, smem, s)));
@@ -1830,9 +2043,10 @@ __global__ void seed_from_lists_kernel(const uint64_t* __restrict__ lists, int64
 
 // Prepared BF16 operand of one matrix (points or queries).
 struct Bf16Operand {
-  __nv_bfloat16* xb = nullptr;
+  __nv_bfloat16* xb = nullptr;  // BF16 rows, or E4M3 bytes in the FP8 form
   RowInfo* info = nullptr;
-  float* norms = nullptr;  // contiguous ||x~||^2 (points only)
+  float* norms = nullptr;   // contiguous ||x~||^2 (points only)
+  float* rscale = nullptr;  // FP8 form: 1/f per row
 };
 
 // Operands of one BF16 search: unit-normalised rows for cosine, the centre
@@ -1852,8 +2066,9 @@ struct Bf16Prep {
 };
 
 mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_t n, const float* qs, int64_t nq,
-                         int d, int metric, Bf16Prep* P) {
-  const int dp = (d + 7) & ~7;
+                         int d, int metric, Bf16Prep* P, bool fp8 = false) {
+  // operand rows: 16-byte multiples (8 BF16 or 16 E4M3 values)
+  const int dp = fp8 ? (d + 15) & ~15 : (d + 7) & ~7;
   const bool self = (qs == base);
   const bool cosine = metric == MANN_METRIC_COSINE;
 
@@ -1912,9 +2127,31 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   int h_inexact = 0;
   MANN_CUDA_TRY(cudaMemcpyAsync(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost, s));
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
-  const int split = h_inexact ? 1 : 0;
+  const int split = (h_inexact && !fp8) ? 1 : 0;  // the FP8 form has no split
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
   Bf16Operand B, Q;
+  if (fp8) {
+    // E4M3 rows with per-row power-of-two scales (dp bytes per row)
+    MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp / 2 + 1, &B.xb));
+    MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
+    MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
+    MANN_TRY(ctx->scratch_t(SLOT_FP8_SCALE_B, (size_t)n, &B.rscale));
+    convert_rows_fp8_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, mu, scale,
+                                                                    reinterpret_cast<uint8_t*>(B.xb), B.rscale,
+                                                                    B.info, B.norms, bmax);
+    MANN_CHECK_LAUNCH();
+    if (self) {
+      Q = B;
+    } else {
+      MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dp / 2 + 1, &Q.xb));
+      MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
+      MANN_TRY(ctx->scratch_t(SLOT_FP8_SCALE_Q, (size_t)nq, &Q.rscale));
+      convert_rows_fp8_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, mu, scale,
+                                                                       reinterpret_cast<uint8_t*>(Q.xb), Q.rscale,
+                                                                       Q.info, nullptr, nullptr);
+      MANN_CHECK_LAUNCH();
+    }
+  } else {
   MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dpe, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
   MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
@@ -1929,6 +2166,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
     convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, mu, scale, Q.xb, Q.info,
                                                                   nullptr, nullptr, split, 0);
     MANN_CHECK_LAUNCH();
+  }
   }
   unsigned long long* counters = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
@@ -1969,21 +2207,21 @@ int tuned_depth(const unsigned long long* hist, int kreq) {
 
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
-                          bool fp64, uint64_t** out_keys, mann_knn_report* rep) {
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, bool fp8) {
   if (nq <= 0) return MANN_OK;
   const int L = LIST;
   // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
   // autotuner's choice for this shape class -- the full list on first sight,
   // then the depth 99.9% of rows needed plus one (refreshed after every call).
   const uint64_t tkey = ((uint64_t)kreq << 56) ^ ((uint64_t)d << 36) ^ ((uint64_t)metric << 32) ^
-                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63);
+                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63) ^ ((uint64_t)fp8 << 61);
   int depth = L;
   if (kreq > KREQ_MAX_BF16)
     return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
                                      " (k+1 for graphs)");
   const bool cosine = metric == MANN_METRIC_COSINE;
   Bf16Prep P;
-  MANN_TRY(bf16_prepare(ctx, s, base, n, qs, nq, d, metric, &P));
+  MANN_TRY(bf16_prepare(ctx, s, base, n, qs, nq, d, metric, &P, fp8));
   const int split = P.split, dpe = P.dpe;
   if (margin > 0) {
     depth = std::min(L, kreq + margin);
@@ -2000,7 +2238,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   int* fb_count = P.fb_count;
 
   CUtensorMap mapA;
-  MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM));
+  MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM, 1, fp8));
 
   // ---- seed pass: over an evenly spaced sample of SEED_SAMPLE points, the
   // SEED_DEPTH-th smallest 32-column chunk minimum of each query (an upper
@@ -2013,7 +2251,8 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     const int64_t bstride = n / SEED_SAMPLE;
     uint64_t* slists = nullptr;
     MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, bstride, Q.info, B.info, B.norms, SEED_SAMPLE, nq, d, dpe,
-                           SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1));
+                           SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1,
+                           nullptr, Q.rscale, B.rscale));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
     seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, SEED_DEPTH - 1, seed);
     MANN_CHECK_LAUNCH();
@@ -2022,7 +2261,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   // ---- main pass over every point
   uint64_t* lists = nullptr;
   MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, 1, Q.info, B.info, B.norms, n, nq, d, dpe, depth, seed, err,
-                         SLOT_PARTIAL, SLOT_KEYS, true, &lists));
+                         SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, nullptr, Q.rscale, B.rscale));
 
   // ---- certify + rerank
   uint64_t* cand = nullptr;
@@ -2096,7 +2335,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   int32_t* unres = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)nq * kreq, &keys));
   if (fp64) MANN_TRY(ctx->scratch_t(SLOT_TIES_ROWS, (size_t)nq, &unres));
-  MANN_TRY(launch_resolve(base, qs, d, metric, nq, L, kreq, fp64 ? 1 : 0, cand, cand_count, floor_val,
+  MANN_TRY(launch_resolve(ctx, base, qs, d, metric, nq, L, kreq, fp64 ? 1 : 0, cand, cand_count, floor_val,
                           keys, counters + 4, s, nullptr, unres));
   if (rep || fp64) {
     unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
@@ -2112,7 +2351,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
       rep->rows_fp64_ties = (int64_t)h[4];
       rep->rows_ties_widened = fp64 ? (int64_t)h[5] : 0;
       rep->rows_unresolved = left;
-      rep->precision_used = MANN_PREC_BF16;
+      rep->precision_used = fp8 ? MANN_PREC_FP8 : MANN_PREC_BF16;
       rep->margin_used = depth - kreq;
     }
   }
@@ -2284,7 +2523,7 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   // ---- truncate to kreq (ties at the k-th distance keep the FP32 (distance, id) order)
   uint64_t* keys = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)N * kreq, &keys));
-  MANN_TRY(launch_resolve(data, data, d, metric, N, L, kreq, 0, cand, cand_count, floor_val, keys,
+  MANN_TRY(launch_resolve(ctx, data, data, d, metric, N, L, kreq, 0, cand, cand_count, floor_val, keys,
                           P.counters + 4, s));
   // ---- status, report, and the depth for the next call of this layout
   unsigned long long hc[64];

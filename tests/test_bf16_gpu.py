@@ -232,3 +232,38 @@ def test_report_max_fp64_error(gpu_lib, metric, precision):
     assert got <= 1e-4 * max(1.0, float(np.abs(d).max()))
     _, _, rep0 = gpu_knn(base, q, 12, metric, precision=precision, report=True)
     assert rep0["max_abs_err_fp64"] == -1.0
+
+
+# ---- the FP8 (e4m3) form: per-row power-of-two scales, the same certificate
+# and exact FP32 rerank; its window is wide, so many rows fall back to the
+# exact FP32 scan -- the answer is the FP32 oracle's either way
+
+@pytest.mark.parametrize("kind,n,nq,d,k,metric", [("mix", 6000, 300, 256, 10, M_SQ), ("iid", 5000, 200, 128, 10, M_SQ),
+                                                 ("iid", 3000, 150, 40, 7, M_EUC), ("ang", 9000, 200, 256, 20, M_COS),
+                                                 ("mix", 40000, 300, 784, 10, M_SQ)])
+def test_fp8_form_equals_oracle(gpu_lib, orc, kind, n, nq, d, k, metric):
+    from manifoldann_gb300 import synthetic
+
+    if kind == "mix":
+        base, q = synthetic.quantized_mixture(n, d, seed=11), synthetic.quantized_mixture(nq, d, seed=12)
+    elif kind == "ang":
+        base, q = _angular(n, d, 11), _angular(nq, d, 12)
+    else:
+        base, q = synthetic.iid_normal(n, d, seed=11), synthetic.iid_normal(nq, d, seed=12)
+    ids, dd, rep = gpu_knn(base, q, k, metric, precision="fp8", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, k, metric)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dd, d_o)
+    assert rep["precision_used"] == 2
+    ids64, _ = gpu_knn(base, q, k, metric, precision="fp8", fp64_ties=True)
+    assert np.array_equal(ids64, orc.knn_f64(base, q, k, metric)[0])
+
+
+def test_fp8_form_graph(gpu_lib, orc):
+    from manifoldann_gb300 import synthetic
+
+    data = synthetic.quantized_mixture(5000, 128, seed=13)
+    g, gd = gpu_graph(data, 12, M_SQ, precision="fp8")
+    g_o, gd_o = orc.knn_graph_f32(data, 12, M_SQ)
+    assert np.array_equal(g, g_o) and same_bits(gd, gd_o)
+
