@@ -41,12 +41,14 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
                                   const int64_t* offs_dev, int nsets, int d, int metric, int kreq, int margin,
                                   uint64_t** out_keys, mann_knn_report* rep);
 
-// Orders near-ties of sorted FP32 candidate lists by FP64 distance (when fp64)
-// and truncates them to kreq keys.  counters[0] += rows re-ordered,
-// counters[1] += rows whose boundary tie could not be settled (their query
-// rows appended to unres_rows when it is not NULL), counters[2] is the FP64
-// task count (must start at 0).  Candidate row i belongs
-// to query / output row rows[i] (identity when rows is NULL).
+// Orders near-ties of sorted FP32 candidate lists as the FP64 oracle does
+// (when fp64) and truncates them to kreq keys.  counters[0] += rows with a
+// tie, counters[1] += rows whose boundary tie could not be settled (their
+// query rows appended to unres_rows when it is not NULL), counters[2] is
+// scratch of the call (Euclidean / SqEuclidean: += rows that needed FP64
+// sequential sums; cosine: the FP64 task cursor, reset by the call).
+// Candidate row i belongs to query / output row rows[i] (identity when rows
+// is NULL).
 mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int d, int metric, int64_t nq, int L,
                            int kreq, int fp64, const uint64_t* cand, const int* cand_count,
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,

@@ -1633,6 +1633,249 @@ __global__ void resolve_sort_kernel(int d, int metric, int64_t nq, int L, int kr
   for (int e = lane; e < kreq; e += 32) out[e] = e < cm ? s_key[w][e] : KEY_NONE;
 }
 
+// ---- (Sq)Euclidean near-tie order without bulk FP64 arithmetic
+//
+// FP64 runs at a small fraction of the FP32 rate on this GPU, so the members
+// of a tie cluster are ordered by a double-float value instead: V ~ S, the
+// exact sum over c of (q_c - p_c)^2, with a rigorous bound |V - S| <= E.
+// Where two neighbours of a cluster (sorted by V) are separated by more than
+// E_a + E_b + R_a + R_b, with R the error bound of the FP64 sequential sum
+// (and of its square root), their FP64 values order the same way; only the
+// rare groups that stay inside that window get the FP64 sequential sums.
+//
+// hp_sqdist: one warp per distance, lane l takes dimensions l, l + 32, ...
+//   t = th + tl exactly (TwoSum of q_c and -p_c), th^2 = p + e exactly
+//   (TwoProd), cc = fl(e + 2 th tl) (tl^2 <= u^2 th^2 is dropped);
+//   (sh, r) = Fast2Sum(sh, p) exactly, sl += fl(r + cc); then a butterfly of
+//   the lanes' (sh, sl) pairs in the same form.  With u = 2^-24 and n the
+//   dimensions per lane, |sl| stays below u S (n + 9) and the roundings sum to
+//   at most u^2 S (4 + (n + 3.01)(n + 1)(1.001) + 10 (n + 8.1)); E doubles the
+//   leading terms, adds the double rounding of sh + sl and, for gradual
+//   underflow, 4 d 2^-149 per distance.
+__device__ __forceinline__ void hp_sqdist(const float* __restrict__ qr, const float* __restrict__ pr, int d,
+                                          int lane, double& V, double& E) {
+  float sh = 0.0f, sl = 0.0f;
+  for (int c = lane; c < d; c += 32) {
+    const float a = __ldg(qr + c), b = __ldg(pr + c);
+    const float th = __fsub_rn(a, b);
+    const float bb = __fsub_rn(th, a);
+    const float tl = __fadd_rn(__fsub_rn(a, __fsub_rn(th, bb)), __fsub_rn(-b, bb));
+    const float p = __fmul_rn(th, th);
+    const float e = __fmaf_rn(th, th, -p);
+    const float cc = __fmaf_rn(__fmul_rn(2.0f, th), tl, e);
+    const float hi = fmaxf(sh, p), lo = fminf(sh, p);
+    const float s2 = __fadd_rn(hi, lo);
+    const float r = __fsub_rn(lo, __fsub_rn(s2, hi));
+    sh = s2;
+    sl = __fadd_rn(sl, __fadd_rn(r, cc));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(FULL, sh, o), ol = __shfl_xor_sync(FULL, sl, o);
+    const float hi = fmaxf(sh, oh), lo = fminf(sh, oh);
+    const float s2 = __fadd_rn(hi, lo);
+    const float r = __fsub_rn(lo, __fsub_rn(s2, hi));
+    sh = s2;
+    sl = __fadd_rn(__fadd_rn(sl, ol), r);
+  }
+  V = (double)sh + (double)sl;
+  const double n = (double)((d + 31) / 32);
+  const double u2 = 3.5527136788005009e-15;  // 2^-48
+  E = u2 * V * (8.0 + 1.01 * (n + 4.0) * (n + 1.0) + 11.0 * (n + 9.0)) + 2.3e-16 * V + (double)d * 2.9e-44;
+  if (!(V < 1e30) || !(sh == sh)) E = __longlong_as_double(0x7FF0000000000000ll);  // +inf: FP64 decides
+}
+
+// error bound of the oracle's FP64 sequential FMA sum (t = q - p in FP64, s =
+// fma(t, t, s)) around S, plus four ulps for square-root collisions
+__device__ __forceinline__ double fp64_seq_bound(double V, int d) {
+  return V * ((double)(d + 3) * 1.1102230246251565e-16 * 1.01 + 8.9e-16) + 1e-300;
+}
+
+// Conservative FP32 link of adjacent sorted candidates: never false where the
+// FP64 test (b - a) <= eps (|a| + |b|) holds.
+__device__ __forceinline__ bool link_l2(float a, float b, float eps_up) {
+  return __fsub_rd(b, a) <= __fmul_ru(eps_up, __fadd_ru(fabsf(a), fabsf(b)));
+}
+
+__device__ __forceinline__ bool hp_less(double va, uint64_t ka, double vb, uint64_t kb) {
+  const unsigned long long ba = (unsigned long long)__double_as_longlong(va);
+  const unsigned long long bb = (unsigned long long)__double_as_longlong(vb);
+  return ba < bb || (ba == bb && key_id(ka) < key_id(kb));
+}
+
+// insertion sort of positions [p, e] by (value bits, id); values >= 0
+__device__ void sort_range(uint64_t* K, double* Vv, double* Ee, int p, int e) {
+  for (int a = p + 1; a <= e; ++a) {
+    const uint64_t kk = K[a];
+    const double vv = Vv[a], ee = Ee[a];
+    int j = a - 1;
+    while (j >= p && hp_less(vv, kk, Vv[j], K[j])) {
+      K[j + 1] = K[j];
+      Vv[j + 1] = Vv[j];
+      Ee[j + 1] = Ee[j];
+      --j;
+    }
+    K[j + 1] = kk;
+    Vv[j + 1] = vv;
+    Ee[j + 1] = ee;
+  }
+}
+
+// One warp per candidate row i (query / output row q = rows[i], or i), for
+// Euclidean and SqEuclidean with the FP64 near-tie order.  cand[i][0..count)
+// is sorted by (fp32, id).  The row's clusters (adjacent candidates whose FP32
+// distances lie within the FP32 rounding bound of each other) up to the one
+// holding position kreq-1 are ordered as the FP64 oracle orders them, and the
+// first kreq keys are written to keys_out[q].  When that cluster runs to the
+// end of the candidate list and the FP32 floor test cannot clear it, the row
+// is still settled when the double-float bound of its kreq-th member lies
+// below the floor; otherwise it keeps the FP32 order, is counted in
+// n_unresolved and (with unres_rows) listed for a wider list.
+// counters: [0] rows with a tie, [1] unresolved rows, [2] rows that needed
+// FP64 sequential sums.
+__global__ void __launch_bounds__(128) resolve_l2_kernel(const float* __restrict__ base,
+                                                         const float* __restrict__ qs, int d, int metric,
+                                                         int64_t nq, int L, int kreq, float eps_up, double eps,
+                                                         const uint64_t* __restrict__ cand,
+                                                         const int* __restrict__ cand_count,
+                                                         const float* __restrict__ floor_val,
+                                                         uint64_t* __restrict__ keys_out,
+                                                         unsigned long long* __restrict__ counters,
+                                                         const int32_t* __restrict__ rows,
+                                                         int32_t* __restrict__ unres_rows) {
+  __shared__ uint64_t s_key[4][256];
+  __shared__ double s_v[4][256];
+  __shared__ double s_e[4][256];
+  __shared__ short s_cl[4][256];
+  __shared__ short s_g[4][256];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * 4 + w;
+  if (i >= nq) return;
+  const int64_t q = rows ? (int64_t)rows[i] : i;
+  const uint64_t* cq = cand + i * L;
+  const int c = min(cand_count[i], L);
+  uint64_t* out = keys_out + q * kreq;
+  for (int e = lane; e < kreq; e += 32) out[e] = e < c ? cq[e] : KEY_NONE;
+  if (c <= 1) return;
+  const int cm = min(c, 256);
+  uint64_t* K = s_key[w];
+  double* Vv = s_v[w];
+  double* Ee = s_e[w];
+  short* cl = s_cl[w];
+  short* gr = s_g[w];
+  for (int e = lane; e < cm; e += 32) K[e] = cq[e];
+  __syncwarp();
+  // cluster starts by ballot: cl[p] = the last start at or before p
+  int carry = 0;
+  for (int b = 0; b < cm; b += 32) {
+    const int p = b + lane;
+    bool start = true;
+    if (p > 0 && p < cm) start = !link_l2(key_dist(K[p - 1]), key_dist(K[p]), eps_up);
+    const unsigned sm = __ballot_sync(FULL, p < cm && start);
+    const unsigned mine = sm & (0xFFFFFFFFu >> (31 - lane));
+    if (p < cm) cl[p] = (short)(mine ? b + 31 - __clz(mine) : carry);
+    if (sm) carry = b + 31 - __clz(sm);
+  }
+  __syncwarp();
+  const int kl = kreq - 1 < cm ? kreq - 1 : cm - 1;
+  int end = cm - 1;
+  bool any_tie = false;
+  for (int b = 0; b < cm; b += 32) {
+    const int p = b + lane;
+    const unsigned nx = __ballot_sync(FULL, p < cm && p > kl && cl[p] == p);
+    if (nx) {
+      end = b + __ffs(nx) - 2;
+      break;
+    }
+  }
+  for (int b = 0; b <= end; b += 32) {
+    const int p = b + lane;
+    if (__any_sync(FULL, p >= 1 && p <= end && cl[p] != p)) any_tie = true;
+  }
+  bool clear = true;
+  double fl_exact = 0.0;  // lower bound of every non-candidate's exact S
+  if (end == cm - 1) {
+    const double lastv = (double)key_dist(K[cm - 1]);
+    const double fl = (double)floor_val[i];
+    clear = lastv * (1.0 + eps) < fl * (1.0 - eps) || fl >= 3.0e38;
+    const double f1 = fl * (1.0 - eps);
+    fl_exact = f1 <= 0.0 ? 0.0 : (metric == MANN_METRIC_EUCLIDEAN ? f1 * f1 * (1.0 - 1e-15) : f1);
+  }
+  if (clear && !any_tie) return;
+  // double-float values of the cluster members (every position when the
+  // boundary cluster has to be settled against the floor)
+  const float* qr = qs + q * d;
+  for (int p = 0; p <= end; ++p) {
+    const bool need = !clear || cl[p] != p || (p + 1 <= end && cl[p + 1] == p);
+    if (!need) continue;  // warp-uniform
+    double V, E;
+    hp_sqdist(qr, base + (int64_t)key_id(K[p]) * d, d, lane, V, E);
+    if (lane == 0) {
+      Vv[p] = V;
+      Ee[p] = E;
+    }
+  }
+  __syncwarp();
+  int flag64 = 0, settled = 1;
+  if (lane == 0) {
+    int p = 0;
+    while (p <= end) {
+      int e = p;
+      while (e + 1 <= end && cl[e + 1] == p) ++e;
+      gr[p] = (short)p;
+      if (e > p) {
+        sort_range(K, Vv, Ee, p, e);
+        for (int a = p + 1; a <= e; ++a) {
+          const double thr = Ee[a - 1] + Ee[a] + fp64_seq_bound(Vv[a - 1], d) + fp64_seq_bound(Vv[a], d);
+          const bool lk = !(Vv[a] - Vv[a - 1] > thr);
+          gr[a] = lk ? gr[a - 1] : (short)a;
+          flag64 |= lk ? 1 : 0;
+        }
+      }
+      p = e + 1;
+    }
+    if (!clear) {
+      // every member of the group holding position kl lies at or below ub
+      int ge = kl;
+      while (ge + 1 <= end && gr[ge + 1] == gr[kl]) ++ge;
+      double ub = 0.0;
+      for (int a = 0; a <= ge; ++a) ub = fmax(ub, Vv[a] + Ee[a]);
+      const double m = ((double)d + 8.0) * 4.4408920985006262e-16;  // FP64 sums and roundings
+      settled = ub * (1.0 + m) < fl_exact * (1.0 - m) ? 1 : 0;
+    }
+  }
+  settled = __shfl_sync(FULL, settled, 0);
+  if (!settled) {
+    if (lane == 0) {
+      const unsigned long long slot = atomicAdd(&counters[1], 1ull);
+      if (unres_rows) unres_rows[slot] = (int32_t)q;
+    }
+    return;
+  }
+  flag64 = __shfl_sync(FULL, flag64, 0);
+  if (flag64) {
+    // groups still inside the window: the oracle's FP64 values and ids decide
+    for (int p = lane; p <= end; p += 32) {
+      const bool in_group = gr[p] != p || (p + 1 <= end && gr[p + 1] == p);
+      if (in_group) Vv[p] = fp64_dist_row(qr, base + (int64_t)key_id(K[p]) * d, d, metric);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      int p = 0;
+      while (p <= end) {
+        int e = p;
+        while (e + 1 <= end && gr[e + 1] == p) ++e;
+        if (e > p) sort_range(K, Vv, Ee, p, e);
+        p = e + 1;
+      }
+      atomicAdd(&counters[2], 1ull);
+    }
+  }
+  if (lane == 0 && any_tie) atomicAdd(&counters[0], 1ull);
+  __syncwarp();
+  for (int e = lane; e < kreq; e += 32) out[e] = e < cm ? K[e] : KEY_NONE;
+}
+
 }  // namespace
 
 namespace {
@@ -1677,6 +1920,16 @@ mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int
                            const float* floor_val, uint64_t* keys_out, unsigned long long* counters,
                            cudaStream_t s, const int32_t* rows, int32_t* unres_rows) {
   if (nq <= 0) return MANN_OK;
+  if (fp64 && metric != MANN_METRIC_COSINE) {
+    // (Sq)Euclidean: one pass, double-float order with FP64 only where it must decide
+    const double eps = (double)(d + 2) * 5.9604644775390625e-08 * 1.01 + 1.2e-7;
+    const float eps_up = std::nextafter((float)eps, 1.0f);
+    resolve_l2_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(base, qs, d, metric, nq, L, kreq, eps_up, eps,
+                                                                cand, cand_count, floor_val, keys_out, counters,
+                                                                rows, unres_rows);
+    MANN_CHECK_LAUNCH();
+    return MANN_OK;
+  }
   TieTask* tasks = nullptr;
   double* vals = nullptr;
   int8_t* state = nullptr;
@@ -1684,6 +1937,8 @@ mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int
     MANN_TRY(ctx->scratch_t(SLOT_TIES_TASKS, (size_t)nq * L, &tasks));
     MANN_TRY(ctx->scratch_t(SLOT_TIES_VALS, (size_t)nq * L, &vals));
     MANN_TRY(ctx->scratch_t(SLOT_TIES_STATE, (size_t)nq, &state));
+    // the task cursor starts at zero on every call (callers may share counters)
+    MANN_CUDA_TRY(cudaMemsetAsync(counters + 2, 0, sizeof(unsigned long long), s));
   }
   const unsigned grid = (unsigned)ceil_div(nq, 4);
   resolve_mark_kernel<<<grid, 128, 0, s>>>(d, metric, nq, L, kreq, fp64, cand, cand_count, floor_val, keys_out,
@@ -1735,9 +1990,6 @@ mann_status widen_unresolved(Context* ctx, cudaStream_t s, const float* base, co
       *still_unresolved = 0;
       return MANN_OK;
     }
-    uint64_t* fkeys = nullptr;
-    MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, h_unres, d, metric, kk, rows, qn, bn, &fkeys,
-                           SLOT_TIES_PARTIAL, SLOT_TIES_KEYS));
     int* cand_count = nullptr;
     float* floor_val = nullptr;
     unsigned long long* counters = nullptr;
@@ -1747,11 +1999,20 @@ mann_status widen_unresolved(Context* ctx, cudaStream_t s, const float* base, co
     MANN_TRY(ctx->scratch_t(SLOT_TIES_COUNTERS, 4, &counters));
     MANN_TRY(ctx->scratch_t(stage == 0 ? SLOT_TIES_ROWS2 : SLOT_TIES_ROWS3, (size_t)h_unres, &next_rows));
     MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), s));
-    fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(h_unres, 128), 128, 0, s>>>(fkeys, h_unres, kk, cand_count,
-                                                                              floor_val);
-    MANN_CHECK_LAUNCH();
-    MANN_TRY(launch_resolve(ctx, base, qs, d, metric, h_unres, kk, kreq, 1, fkeys, cand_count, floor_val, keys_out,
-                            counters, s, rows, next_rows));
+    // batches of at most 32 rows take the few-row scan (one point per thread
+    // across the GPU) when the list fits it; a wider list scans all rows at once
+    const int64_t chunk = kk <= 64 ? 32 : h_unres;
+    for (int64_t r0 = 0; r0 < h_unres; r0 += chunk) {
+      const int64_t nr = std::min<int64_t>(chunk, h_unres - r0);
+      uint64_t* fkeys = nullptr;
+      MANN_TRY(knn_fp32_keys(ctx, s, base, n, qs, nr, d, metric, kk, rows + r0, qn, bn, &fkeys,
+                             SLOT_TIES_PARTIAL, SLOT_TIES_KEYS));
+      fp32_lists_to_cand_kernel<<<(unsigned)ceil_div(nr, 128), 128, 0, s>>>(fkeys, nr, kk, cand_count + r0,
+                                                                           floor_val + r0);
+      MANN_CHECK_LAUNCH();
+      MANN_TRY(launch_resolve(ctx, base, qs, d, metric, nr, kk, kreq, 1, fkeys, cand_count + r0, floor_val + r0,
+                              keys_out, counters, s, rows + r0, next_rows));
+    }
     unsigned long long h[2] = {0, 0};
     MANN_CUDA_TRY(cudaMemcpyAsync(h, counters, sizeof(h), cudaMemcpyDeviceToHost, s));
     MANN_CUDA_TRY(cudaStreamSynchronize(s));
