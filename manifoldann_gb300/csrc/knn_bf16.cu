@@ -67,6 +67,7 @@ struct Stg {
   static constexpr int N = PAIR ? 6 : 4;
 };
 
+constexpr int AUG = 24;                              // norm-fold columns read after a BF16 row's main part
 constexpr int LIST = 32;                             // candidates kept per query row
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
@@ -199,8 +200,11 @@ __global__ void choose_scale_kernel(const double* __restrict__ score, float* __r
 // Split form (split = 1): x~ = hi + lo with hi = bf16(cv), lo = bf16(cv - hi),
 // written as three dp-wide segments -- [hi | hi | lo] for query rows (role 0),
 // [hi | lo | hi] for point rows (role 1) -- so one MMA over 3dp columns gives
-// hi.hi + hi.lo + lo.hi = q~.p~ - lo_q.lo_p.
-__global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp,
+// hi.hi + hi.lo + lo.hi = q~.p~ - lo_q.lo_p.  The row (width = augx + 16
+// columns) then holds zeros up to augx and the first 16 columns of the
+// norm-fold block, [P0 P1 P2 1 1 1 0 0 | 1 1 1 P0 P1 P2 0 0], with P0 + P1 +
+// P2 = -||x~||^2 / 2 exactly; its last 8 columns are zeros past the row.
+__global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int d, int dp, int augx, int width,
                                     const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
                                     float* __restrict__ norms, BaseMax* __restrict__ bmax, int split,
@@ -213,7 +217,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   __syncthreads();
   const bool valid = row < n;
   const float* xr = x + (valid ? row : 0) * d;
-  __nv_bfloat16* br = xb + (valid ? row : 0) * (int64_t)(split ? 3 * dp : dp);
+  __nv_bfloat16* br = xb + (valid ? row : 0) * (int64_t)width;
   // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
   // certificate adds to its bound (norm_rel_err)
@@ -261,6 +265,25 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     f_r += __shfl_xor_sync(FULL, f_r, o);
     f_c += __shfl_xor_sync(FULL, f_c, o);
     f_l += __shfl_xor_sync(FULL, f_l, o);
+  }
+  if (valid) {
+    // the butterfly leaves the same f_b in every lane (x + y == y + x); split
+    // -f_b / 2 into three BF16 pieces: each remainder is exact (Sterbenz) and
+    // the third holds at most 8 significant bits
+    const float hn = -0.5f * f_b;
+    const __nv_bfloat16 p0 = __float2bfloat16_rn(hn);
+    const float r1 = __fsub_rn(hn, __bfloat162float(p0));
+    const __nv_bfloat16 p1 = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 p2 = __float2bfloat16_rn(__fsub_rn(r1, __bfloat162float(p1)));
+    const __nv_bfloat16 one = __float2bfloat16_rn(1.0f), zero = __float2bfloat16_rn(0.0f);
+    for (int c = (split ? 3 * dp : dp) + lane; c < width; c += 32) {
+      const int a = c - augx;  // < 0: zero padding of the main columns
+      const int k = a < 8 ? a : a - 11;  // piece index in the first / second group
+      __nv_bfloat16 val = zero;
+      if ((a >= 0 && a < 3) || (a >= 11 && a < 14)) val = k == 0 ? p0 : (k == 1 ? p1 : p2);
+      else if ((a >= 3 && a < 6) || (a >= 8 && a < 11)) val = one;
+      br[c] = val;
+    }
   }
   if (lane == 0 && valid) {
     // FP32 with directed rounding (FP64 is slow on this part): each bound is
@@ -435,7 +458,8 @@ struct RunInfo {
 
 struct MainArgs {
   int64_t nq, n;
-  int d, dp, nkb;
+  int d, dp, nkb;     // dp: main operand columns (zero-padded); nkb: K-stages per tile
+  int augx;           // norm-folded form: first fold column (within the last stage); 0 = none
   Walk w;
   const TileItem* titems;  // segmented pass (NULL: the banded walk of `w`)
   const float* qscale;     // FP8 form: per query row, 1/f of its e4m3 scaling (NULL otherwise)
@@ -669,6 +693,97 @@ __device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, f
   }
 }
 
+// Norm-folded epilogue (BF16 form).  Every operand row carries, after its
+// main columns, a 24-column block [P0 P1 P2 1 1 1 0 0 | 1 1 1 P0 P1 P2 0 0 |
+// 0 ...] with P0 + P1 + P2 = -||x~||^2 / 2 exactly (three BF16 pieces of an
+// FP32 value); one extra K-step reads the query block at its first column and
+// the point block eight columns later, so it adds -(||q~||^2 + ||p~||^2) / 2 and the accumulator
+// holds acc = q~.p~ - (||q~||^2 + ||p~||^2) / 2.  The estimate is then
+// est = -2 acc = ||q~ - p~||^2 (an exact scaling): the chunk's smallest est is
+// -2 max(acc), one FMNMX per value and no per-column norm.  Columns j >=
+// nvalid lie past the tile's last point (or in another point set).
+__device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t* __restrict__ mylist,
+                                               uint64_t& thr_key, float& thr_est, uint64_t seed_key, int& lslot,
+                                               int& nfill, uint32_t col0, int depth) {
+  if (nvalid < 32) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if (j >= nvalid) v[j] = 0xFF800000u;  // -inf: est = +inf
+  }
+  float m4[8];
+#pragma unroll
+  for (int j4 = 0; j4 < 8; ++j4)
+    m4[j4] = fmaxf(fmaxf(__uint_as_float(v[4 * j4 + 0]), __uint_as_float(v[4 * j4 + 1])),
+                   fmaxf(__uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3])));
+  const float mx = fmaxf(fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3])),
+                         fmaxf(fmaxf(m4[4], m4[5]), fmaxf(m4[6], m4[7])));
+  const float mn = -2.0f * mx;
+  if (!__any_sync(FULL, mn < thr_est)) return;
+  if (mn < thr_est) {
+    unsigned mask = 0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) mask |= (-2.0f * __uint_as_float(v[j]) < thr_est ? 1u : 0u) << j;
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      uint32_t bits = v[0];
+#pragma unroll
+      for (int u = 1; u < 32; ++u) bits = j == u ? v[u] : bits;
+      const uint64_t c = make_key(-2.0f * __uint_as_float(bits), col0 + (uint32_t)j);
+      if (c < thr_key) {
+        if (nfill < depth) {
+          mylist[nfill * BM] = c;
+          if (++nfill < depth) continue;
+        } else {
+          mylist[lslot * BM] = c;
+        }
+        uint64_t m = 0;
+        int ms = 0;
+#pragma unroll 8
+        for (int e2 = 0; e2 < depth; ++e2) {
+          const uint64_t v2 = mylist[e2 * BM];
+          if (v2 > m) {
+            m = v2;
+            ms = e2;
+          }
+        }
+        lslot = ms;
+        thr_key = m == KEY_NONE ? seed_key : m;
+        thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
+      }
+    }
+  }
+}
+
+// Seed-pass form of epi_chunk_fold (the chunk minimum of est = -2 max(acc)).
+__device__ __forceinline__ void seed_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t (&top)[SEED_DEPTH],
+                                                uint32_t col0) {
+  if (nvalid < 32) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j)
+      if (j >= nvalid) v[j] = 0xFF800000u;
+  }
+  float m4[8];
+#pragma unroll
+  for (int j4 = 0; j4 < 8; ++j4)
+    m4[j4] = fmaxf(fmaxf(__uint_as_float(v[4 * j4 + 0]), __uint_as_float(v[4 * j4 + 1])),
+                   fmaxf(__uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3])));
+  const float mx = fmaxf(fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3])),
+                         fmaxf(fmaxf(m4[4], m4[5]), fmaxf(m4[6], m4[7])));
+  uint64_t c = make_key(-2.0f * mx, col0);
+  if (c < top[SEED_DEPTH - 1]) {
+    top[SEED_DEPTH - 1] = c;
+#pragma unroll
+    for (int i = SEED_DEPTH - 1; i > 0; --i) {
+      const uint64_t lo = top[i - 1], hi = top[i];
+      if (hi < lo) {
+        top[i - 1] = hi;
+        top[i] = lo;
+      }
+    }
+  }
+}
+
 // Shared-memory footprint of k2_main<CAP, NSETS>.
 template <bool PAIR>
 __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
@@ -777,15 +892,16 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           }
           uint8_t* sa = stage_base + s * STAGE_BYTES;
           uint8_t* sb = sa + A_STAGE_BYTES;
+          const int xa = kb * EPS, xb = kb * EPS;
           if (PAIR) {
             if (rank == 0) ptx::mbar_arrive_expect_tx(&full_bar[s], 2 * STAGE_BYTES);
             const uint32_t fb = full0 + (uint32_t)s * 8u;
-            ptx::tma_load_2d_pair(sa, &mapA, fb, kb * EPS, (int)v.q0 + (int)rank * BM);
-            ptx::tma_load_2d_pair(sb, &mapB, fb, kb * EPS, (int)v.c0 + (int)rank * Stg<PAIR>::B_ROWS);
+            ptx::tma_load_2d_pair(sa, &mapA, fb, xa, (int)v.q0 + (int)rank * BM);
+            ptx::tma_load_2d_pair(sb, &mapB, fb, xb, (int)v.c0 + (int)rank * Stg<PAIR>::B_ROWS);
           } else {
             ptx::mbar_arrive_expect_tx(&full_bar[s], STAGE_BYTES);
-            ptx::tma_load_2d(sa, &mapA, &full_bar[s], kb * EPS, (int)v.q0);
-            ptx::tma_load_2d(sb, &mapB, &full_bar[s], kb * EPS, (int)v.c0);
+            ptx::tma_load_2d(sa, &mapA, &full_bar[s], xa, (int)v.q0);
+            ptx::tma_load_2d(sb, &mapB, &full_bar[s], xb, (int)v.c0);
           }
         }
       }
@@ -815,8 +931,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           ptx::tc_fence_after();
           const uint32_t sa = ptx::smem_u32(stage_base + s * STAGE_BYTES);
           const uint32_t sb = sa + A_STAGE_BYTES;
-          const int rem = a.dp - kb * EPS;  // valid (zero-padded) columns left
-          const int ksteps = rem >= EPS ? 4 : (rem + EPK - 1) / EPK;
+          const int rem = a.dp - kb * EPS;  // main (zero-padded) columns left
+          const int ksteps = rem >= EPS ? 4 : (rem > 0 ? (rem + EPK - 1) / EPK : 0);
           for (int kk = 0; kk < ksteps; ++kk) {  // each MMA covers 32 bytes of K
             const uint64_t ad = ptx::sw128_desc(sa + kk * 32);
             const uint64_t bd = ptx::sw128_desc(sb + kk * 32);
@@ -826,6 +942,18 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
               ptx::mma_f8(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
             else
               ptx::mma_f16(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+          }
+          if (!FP8 && a.augx > 0 && kb == a.augx / EPS) {
+            // the norm-fold K-step: the query block at its first column, the
+            // point block eight columns (16 bytes) later -- inside the same
+            // 128-byte swizzled row (fold columns start at 0, 16 or 32 of the stage)
+            const int ka = (a.augx % EPS) / 16;
+            const uint64_t ad = ptx::sw128_desc(sa + ka * 32);
+            const uint64_t bd = ptx::sw128_desc(sb + ka * 32 + 16);
+            if (PAIR)
+              ptx::mma_f16_pair(dcol, ad, bd, idesc, 1u);
+            else
+              ptx::mma_f16(dcol, ad, bd, idesc, 1u);
           }
           // frees the stage (in both CTAs of a pair) when these MMAs finish
           if (PAIR)
@@ -897,13 +1025,16 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     float nbn[BN / 32], nbc[BN / 32];
     float csn[FP8 ? BN / 32 : 1], csc[FP8 ? BN / 32 : 1];  // FP8: -2 (1/f) of the columns
     float rs = 1.0f;                                        // FP8: 1/f of this lane's row
+    // (the BF16 form folds the norms into the MMA and needs none of these)
     auto fetch_norms = [&](int64_t st_) {
-      const ItemView v_ = view_item(a, walk_item(it0, it1, a.w, st_), QROWS);
+      if constexpr (FP8) {
+        const ItemView v_ = view_item(a, walk_item(it0, it1, a.w, st_), QROWS);
 #pragma unroll
-      for (int i = 0; i < BN / 32; ++i) {
-        const int64_t col = v_.c0 + lane + 32 * i;
-        nbn[i] = col < v_.cend ? __ldg(&a.bnorm[col * a.bstride]) : INF;
-        if constexpr (FP8) csn[i] = col < v_.cend ? -2.0f * __ldg(&a.bscale[col * a.bstride]) : 0.0f;
+        for (int i = 0; i < BN / 32; ++i) {
+          const int64_t col = v_.c0 + lane + 32 * i;
+          nbn[i] = col < v_.cend ? __ldg(&a.bnorm[col * a.bstride]) : INF;
+          csn[i] = col < v_.cend ? -2.0f * __ldg(&a.bscale[col * a.bstride]) : 0.0f;
+        }
       }
     };
     if (it1 > it0) fetch_norms(0);
@@ -929,11 +1060,12 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       }
       const int buf = tcount & 1;
       const int64_t col0 = v.c0;
-#pragma unroll
-      for (int i = 0; i < BN / 32; ++i) nbc[i] = nbn[i];
       if constexpr (FP8) {
 #pragma unroll
-        for (int i = 0; i < BN / 32; ++i) csc[i] = csn[i];
+        for (int i = 0; i < BN / 32; ++i) {
+          nbc[i] = nbn[i];
+          csc[i] = csn[i];
+        }
       }
       if (st + 1 < it1 - it0) fetch_norms(st + 1);
       const uint32_t tph = (tcount >> 1) & 1;
@@ -951,12 +1083,21 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
         ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
         ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
-        const float cs_a = FP8 ? pick(csc, ch) : 0.0f;
-        if (a.seedmode)
-          seed_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, top, (uint32_t)(col0 + ch * 32));
-        else
-          epi_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                         (uint32_t)(col0 + ch * 32), a.depth);
+        if constexpr (FP8) {
+          const float cs_a = pick(csc, ch);
+          if (a.seedmode)
+            seed_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, top, (uint32_t)(col0 + ch * 32));
+          else
+            epi_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                           (uint32_t)(col0 + ch * 32), a.depth);
+        } else {
+          const int nva = (int)min((int64_t)32, v.cend - (col0 + ch * 32));
+          if (a.seedmode)
+            seed_chunk_fold(va, nva, top, (uint32_t)(col0 + ch * 32));
+          else
+            epi_chunk_fold(va, nva, mylist, thr_key, thr_est, seed_key, lslot, nfill, (uint32_t)(col0 + ch * 32),
+                           a.depth);
+        }
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
           ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
@@ -971,12 +1112,21 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             ptx::mbar_arrive(&tempty_bar[buf]);
           }
         }
-        const float cs_b = FP8 ? pick(csc, ch + 1) : 0.0f;
-        if (a.seedmode)
-          seed_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, top, (uint32_t)(col0 + (ch + 1) * 32));
-        else
-          epi_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                         (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+        if constexpr (FP8) {
+          const float cs_b = pick(csc, ch + 1);
+          if (a.seedmode)
+            seed_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, top, (uint32_t)(col0 + (ch + 1) * 32));
+          else
+            epi_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                           (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+        } else {
+          const int nvb = (int)min((int64_t)32, v.cend - (col0 + (ch + 1) * 32));
+          if (a.seedmode)
+            seed_chunk_fold(vb, nvb, top, (uint32_t)(col0 + (ch + 1) * 32));
+          else
+            epi_chunk_fold(vb, nvb, mylist, thr_key, thr_est, seed_key, lslot, nfill,
+                           (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+        }
         ptx::tmem_ld_wait();
       }
     }
@@ -1090,7 +1240,8 @@ struct RerankArgs {
   const float* cos_qn;  // [nq] squared norms of the original queries (FP32 form order)
   const float* cos_bn;  // [n]  squared norms of the original points
   float eps_c;          // |FP32 cosine - ||q^ - p^||^2 / 2| bound (rounded up)
-  int kdim;             // columns of the tensor-core dot (dp, or 3 dp in the split form)
+  int kdim;             // columns of the tensor-core dot (dp, or 3 dp in the split form; + the fold step)
+  int full_est;         // list keys hold est (norm-folded BF16 form), not est' = est - ||q~||^2
   int coop;             // d % 4 == 0 and 16-byte aligned rows: warp-cooperative row loads
 };
 
@@ -1152,7 +1303,8 @@ __device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int l
   // round down, and est' + ||q~||^2 is rounded down where it is compared with
   // T, so the candidate set only grows and the certificate stays rigorous.
   const bool cosine = a.metric == MANN_METRIC_COSINE;
-  const float qn = a.qinfo[q].nrm;  // list keys hold est' = est - ||q~||^2
+  // list keys hold est' = est - ||q~||^2, or est itself in the norm-folded form
+  const float qn = a.full_est ? 0.0f : a.qinfo[q].nrm;
   float T = 0.0f, d_floor = 0.0f;
   int cert_i = 0, all_in_i = 0;
   if (lane == 0) {
@@ -2178,7 +2330,7 @@ struct SegPass {
 
 mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA, const void* bxb, int64_t bstride,
                           const RowInfo* qinfo, const RowInfo* binfo, const float* bnorm, int64_t n, int64_t nq,
-                          int d, int dp, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
+                          int d, int dp, int mainw, int augx, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
                           bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr,
                           const float* qscale = nullptr, const float* bscale = nullptr) {
   const bool fp8 = qscale != nullptr;
@@ -2244,8 +2396,9 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.nq = nq;
   ma.n = n;
   ma.d = d;
-  ma.dp = dp;
-  ma.nkb = (int)ceil_div(dp, fp8 ? 128 : BK);
+  ma.dp = mainw;
+  ma.nkb = (int)(augx > 0 ? ceil_div(augx + AUG, BK) : ceil_div(mainw, fp8 ? 128 : BK));
+  ma.augx = augx;
   ma.w = w;
   ma.titems = seg ? seg->items : nullptr;
   ma.qscale = qscale;
@@ -2318,6 +2471,9 @@ struct Bf16Operand {
 struct Bf16Prep {
   Bf16Operand B, Q;
   int split = 0, dp = 0, dpe = 0;
+  int width = 0;  // operand row length: mainw + AUG (BF16), dp (FP8)
+  int mainw = 0;  // main columns: dpe zero-padded to a multiple of 16 (BF16), dp (FP8)
+  int augx = 0;   // first augmented column (BF16: mainw), 0 without the norm fold
   float* scale = nullptr;
   BaseMax* bmax = nullptr;
   float *cos_bn = nullptr, *cos_qn = nullptr;
@@ -2392,7 +2548,10 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
   Bf16Operand B, Q;
   if (fp8) {
-    // E4M3 rows with per-row power-of-two scales (dp bytes per row)
+    // E4M3 rows with per-row power-of-two scales (dp bytes per row), no norm fold
+    P->width = dp;
+    P->mainw = dp;
+    P->augx = 0;
     MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dp / 2 + 1, &B.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
     MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
@@ -2413,21 +2572,32 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
       MANN_CHECK_LAUNCH();
     }
   } else {
-  MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * dpe, &B.xb));
+  // rows: [main (dpe) | zeros up to augx | the first 16 norm-fold columns];
+  // the fold's last 8 columns (zeros) lie past the row, where TMA fills zeros.
+  // augx is mainw (dpe rounded up to 16) when the fold's 24 columns fit in
+  // that stage, else the next stage.  Rows are 32-byte multiples (rows that
+  // straddle 32-byte sectors slowed k2_main 1.6x).
+  const int mainw = (dpe + 15) & ~15;
+  const int augx = (mainw % BK) + AUG <= BK ? mainw : (mainw + BK - 1) / BK * BK;  // fold inside one stage
+  const int width = augx + 16;
+  MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * width, &B.xb));
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
   MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
-  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, mu, scale, B.xb, B.info,
-                                                              B.norms, bmax, split, 1);
+  convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, augx, width, mu, scale, B.xb,
+                                                              B.info, B.norms, bmax, split, 1);
   MANN_CHECK_LAUNCH();
   if (self && !split) {
     Q = B;
   } else {
-    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * dpe, &Q.xb));
+    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * width, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
-    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, mu, scale, Q.xb, Q.info,
-                                                                  nullptr, nullptr, split, 0);
+    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, augx, width, mu, scale, Q.xb,
+                                                                  Q.info, nullptr, nullptr, split, 0);
     MANN_CHECK_LAUNCH();
   }
+  P->width = width;
+  P->mainw = mainw;
+  P->augx = augx;
   }
   unsigned long long* counters = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
@@ -2499,7 +2669,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   int* fb_count = P.fb_count;
 
   CUtensorMap mapA;
-  MANN_TRY(make_map(&mapA, Q.xb, nq, dpe, BM, 1, fp8));
+  MANN_TRY(make_map(&mapA, Q.xb, nq, P.width, BM, 1, fp8));
 
   // ---- seed pass: over an evenly spaced sample of SEED_SAMPLE points, the
   // SEED_DEPTH-th smallest 32-column chunk minimum of each query (an upper
@@ -2511,7 +2681,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (n >= 16 * SEED_SAMPLE) {
     const int64_t bstride = n / SEED_SAMPLE;
     uint64_t* slists = nullptr;
-    MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, bstride, Q.info, B.info, B.norms, SEED_SAMPLE, nq, d, dpe,
+    MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, bstride, Q.info, B.info, B.norms, SEED_SAMPLE, nq, d, P.width, P.mainw, P.augx,
                            SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1,
                            nullptr, Q.rscale, B.rscale));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
@@ -2521,7 +2691,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
 
   // ---- main pass over every point
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, 1, Q.info, B.info, B.norms, n, nq, d, dpe, depth, seed, err,
+  MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, 1, Q.info, B.info, B.norms, n, nq, d, P.width, P.mainw, P.augx, depth, seed, err,
                          SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, nullptr, Q.rscale, B.rscale));
 
   // ---- certify + rerank
@@ -2555,7 +2725,9 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   ra.fb_rows = fb_rows;
   ra.fb_count = fb_count;
   ra.cand_total = counters + 2;
-  ra.kdim = dpe;
+  // the norm fold adds one 16-term K-step to the accumulation
+  ra.kdim = P.augx > 0 ? P.mainw + 16 : dpe;
+  ra.full_est = P.augx > 0 ? 1 : 0;
   ra.cos_qn = cos_qn;
   ra.cos_bn = cos_bn;
   {
@@ -2717,7 +2889,7 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
     if (it != ctx->tune.end()) depth = (int)it->second;
   }
   CUtensorMap mapA;
-  MANN_TRY(make_map(&mapA, P.Q.xb, N, P.dpe, BM));
+  MANN_TRY(make_map(&mapA, P.Q.xb, N, P.width, BM));
   SegPass sp;
   sp.items = d_items;
   sp.nitems = (int64_t)T.items.size();
@@ -2726,7 +2898,7 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   sp.runs_host = T.runs.data();
   sp.nruns = (int64_t)T.runs.size();
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.dpe, depth, nullptr,
+  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.width, P.mainw, P.augx, depth, nullptr,
                          P.err, SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, &sp));
   // ---- certify + rerank (per row; the bounds are global, so valid for every set)
   uint64_t* cand = nullptr;
@@ -2759,7 +2931,8 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   ra.fb_rows = fb_rows;
   ra.fb_count = P.fb_count;
   ra.cand_total = P.counters + 2;
-  ra.kdim = P.dpe;
+  ra.kdim = P.augx > 0 ? P.mainw + 16 : P.dpe;
+  ra.full_est = P.augx > 0 ? 1 : 0;
   ra.cos_qn = nullptr;
   ra.cos_bn = nullptr;
   ra.eps_c = 0.0f;

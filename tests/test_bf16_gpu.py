@@ -267,3 +267,31 @@ def test_fp8_form_graph(gpu_lib, orc):
     g_o, gd_o = orc.knn_graph_f32(data, 12, M_SQ)
     assert np.array_equal(g, g_o) and same_bits(gd, gd_o)
 
+
+
+def test_fp64_tie_order_at_the_bit_level(gpu_lib, orc):
+    """Squared distances from the origin that FP32 cannot tell apart (all round
+    to 1 + 2^-22) but FP64 can: gaps of 2^-30 and 2^-32 (ordered by the
+    double-float values alone), 2^-46 (inside their error window: FP64
+    sequential sums decide) and an exact tie (ids decide).  Lower ids sit on
+    the larger distances, so FP32 (distance, id) order differs from the
+    oracle's at every position of the cluster."""
+    d = 8
+    pts = np.zeros((5, d), np.float32)
+    pts[0, 0] = np.float32(1.0 + 2.0 ** -23)                    # 1 + 2^-22 + 2^-46
+    pts[1, :3] = [1.0, 2.0 ** -11, 2.0 ** -15]                  # 1 + 2^-22 + 2^-30
+    pts[2, :4] = [1.0, 2.0 ** -11, 0.0, 2.0 ** -16]             # 1 + 2^-22 + 2^-32
+    pts[3, :5] = [1.0, 2.0 ** -11, 0.0, 0.0, 2.0 ** -23]        # 1 + 2^-22 + 2^-46 (ties id 0)
+    pts[4, :2] = [1.0, 2.0 ** -11]                              # 1 + 2^-22
+    rng = np.random.default_rng(21)
+    inner = (rng.standard_normal((4, d)) * 0.2).astype(np.float32)
+    far = (rng.standard_normal((3000, d)) * 0.3 + 3.0).astype(np.float32)
+    base = np.concatenate([pts, far, inner])
+    q = np.zeros((4, d), np.float32)
+    for metric in (M_SQ, M_EUC):
+        ids_o, _ = orc.knn_f64(base, q, 9, metric)
+        assert list(ids_o[0, 4:9]) == [4, 0, 3, 2, 1]
+        for precision in ("fp32", "bf16"):
+            ids64, _, rep = gpu_knn(base, q, 9, metric, precision=precision, fp64_ties=True, report=True)
+            assert np.array_equal(ids64, ids_o), (precision, metric, ids64[0], ids_o[0])
+            assert rep["rows_unresolved"] == 0, rep
