@@ -76,6 +76,9 @@ enum ScratchSlot : int {
   SLOT_SEG_RUNS,      // batched BF16 graphs: the items of each block
   SLOT_SEG_ROWRUN,    // batched BF16 graphs: each row's block
   SLOT_SEG_QUEUE,     // batched BF16 graphs: fallback work-queue header
+  SLOT_SEG_SITEMS,    // batched BF16 graphs: seed-pass items
+  SLOT_SEG_SRUNS,     // batched BF16 graphs: seed-pass items of each block
+  SLOT_SEG_SROWRUN,   // batched BF16 graphs: seed pass, each row's block
   SLOT_FP8_SCALE_B,   // FP8 form: per-point 1/f
   SLOT_FP8_SCALE_Q,   // FP8 form: per-query 1/f
   SLOT_COS_B,         // BF16 cosine: unit-normalised points

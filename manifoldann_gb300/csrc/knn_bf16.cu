@@ -72,6 +72,7 @@ constexpr int LIST = 32;                             // candidates kept per quer
 constexpr int SEED_SAMPLE = 2048;                    // points sampled by the seed pass
 constexpr int SEED_DEPTH = 5;                        // the seed is the 5th smallest (chunk minimum)
 constexpr int KREQ_MAX_BF16 = 24;                    // largest k (k+1 for graphs) of this form
+constexpr int SEG_SEED_STRIDE = 32;                  // many point sets: the seed pass samples every 32nd point
 constexpr uint32_t TMEM_COLS = 2 * BN;               // double-buffered accumulator
 // Bands and CTA pairs are built but not selected: on one GB300 the
 // phase-aligned single-band walk beat 48 MB bands (1M x 128: 8.2 vs 11.8 ms;
@@ -2804,7 +2805,13 @@ struct SegTables {
   std::vector<TileItem> items;
   std::vector<RunInfo> runs;
   std::vector<int32_t> row_run;
+  // seed pass: each block against its own set's every SEG_SEED_STRIDE-th point
+  // (rows of a strided map over the same operand)
+  std::vector<TileItem> sitems;
+  std::vector<RunInfo> sruns;
+  std::vector<int32_t> srow_run;
   const void* uploaded = nullptr;  // device items buffer the tables were copied to
+  const void* suploaded = nullptr;  // device seed-items buffer
   uint64_t uploaded_hash = 0;
 };
 std::mutex g_seg_mu;
@@ -2827,14 +2834,26 @@ void build_seg_tables(const int64_t* offs, int nsets, SegTables* T) {
   T->items.clear();
   T->runs.clear();
   T->row_run.assign((size_t)offs[nsets], 0);
+  T->sitems.clear();
+  T->sruns.clear();
+  T->srow_run.assign((size_t)offs[nsets], 0);
   for (int c = 0; c < nsets; ++c) {
     const int64_t o = offs[c], nc = offs[c + 1] - offs[c];
+    // the set's sampled points: map rows i with i * stride in [o, o + nc)
+    const int64_t s0 = (o + SEG_SEED_STRIDE - 1) / SEG_SEED_STRIDE;
+    const int64_t s1 = (o + nc + SEG_SEED_STRIDE - 1) / SEG_SEED_STRIDE;
     for (int64_t q = 0; q < nc; q += BM) {
       const int64_t first = (int64_t)T->items.size();
       for (int64_t t = 0; t < nc; t += BN) T->items.push_back(TileItem{o + q, o + nc, o + t, o + nc, first});
       const int32_t r = (int32_t)T->runs.size();
       T->runs.push_back(RunInfo{first, (int64_t)T->items.size() - first});
       for (int64_t row = o + q; row < std::min(o + q + BM, o + nc); ++row) T->row_run[(size_t)row] = r;
+      const int64_t sfirst = (int64_t)T->sitems.size();
+      for (int64_t t = s0; t < s1; t += BN) T->sitems.push_back(TileItem{o + q, o + nc, t, s1, sfirst});
+      if (s1 == s0) T->sitems.push_back(TileItem{o + q, o + nc, s0, s0, sfirst});  // no sample: an empty item
+      const int32_t sr = (int32_t)T->sruns.size();
+      T->sruns.push_back(RunInfo{sfirst, (int64_t)T->sitems.size() - sfirst});
+      for (int64_t row = o + q; row < std::min(o + q + BM, o + nc); ++row) T->srow_run[(size_t)row] = sr;
     }
   }
   T->hash = h;
@@ -2868,12 +2887,23 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   MANN_TRY(ctx->scratch_t(SLOT_SEG_ITEMS, T.items.size(), &d_items));
   MANN_TRY(ctx->scratch_t(SLOT_SEG_RUNS, T.runs.size(), &d_runs));
   MANN_TRY(ctx->scratch_t(SLOT_SEG_ROWRUN, (size_t)N, &d_row_run));
-  if (T.uploaded != d_items || T.uploaded_hash != T.hash) {
+  TileItem* d_sitems = nullptr;
+  RunInfo* d_sruns = nullptr;
+  int32_t* d_srow_run = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_SITEMS, T.sitems.size(), &d_sitems));
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_SRUNS, T.sruns.size(), &d_sruns));
+  MANN_TRY(ctx->scratch_t(SLOT_SEG_SROWRUN, (size_t)N, &d_srow_run));
+  if (T.uploaded != d_items || T.suploaded != d_sitems || T.uploaded_hash != T.hash) {
     MANN_CUDA_TRY(cudaMemcpyAsync(d_items, T.items.data(), sizeof(TileItem) * T.items.size(), cudaMemcpyHostToDevice, s));
     MANN_CUDA_TRY(cudaMemcpyAsync(d_runs, T.runs.data(), sizeof(RunInfo) * T.runs.size(), cudaMemcpyHostToDevice, s));
     MANN_CUDA_TRY(cudaMemcpyAsync(d_row_run, T.row_run.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_sitems, T.sitems.data(), sizeof(TileItem) * T.sitems.size(),
+                                  cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_sruns, T.sruns.data(), sizeof(RunInfo) * T.sruns.size(), cudaMemcpyHostToDevice, s));
+    MANN_CUDA_TRY(cudaMemcpyAsync(d_srow_run, T.srow_run.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, s));
     MANN_CUDA_TRY(cudaStreamSynchronize(s));  // the copies read pageable host memory
     T.uploaded = d_items;
+    T.suploaded = d_sitems;
     T.uploaded_hash = T.hash;
   }
   Bf16Prep P;
@@ -2897,8 +2927,28 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   sp.row_run = d_row_run;
   sp.runs_host = T.runs.data();
   sp.nruns = (int64_t)T.runs.size();
+  // ---- seed pass: each row's SEED_DEPTH-th smallest chunk minimum over
+  // every SEG_SEED_STRIDE-th point of its own set bounds its estimates from
+  // above (a set with no sampled point gets no seed), so the main pass admits
+  // ~3x fewer candidates
+  SegPass ssp;
+  ssp.items = d_sitems;
+  ssp.nitems = (int64_t)T.sitems.size();
+  ssp.runs = d_sruns;
+  ssp.row_run = d_srow_run;
+  ssp.runs_host = T.sruns.data();
+  ssp.nruns = (int64_t)T.sruns.size();
+  uint64_t* slists = nullptr;
+  const int64_t nsample = (N + SEG_SEED_STRIDE - 1) / SEG_SEED_STRIDE;
+  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, SEG_SEED_STRIDE, P.Q.info, P.B.info, P.B.norms, nsample, N, d, P.width,
+                         P.mainw, P.augx, SEED_DEPTH, nullptr, P.err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists,
+                         1, &ssp));
+  float* seed = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)N, &seed));
+  seed_from_lists_kernel<<<(unsigned)ceil_div(N, 256), 256, 0, s>>>(slists, N, SEED_DEPTH - 1, seed);
+  MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
-  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.width, P.mainw, P.augx, depth, nullptr,
+  MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.width, P.mainw, P.augx, depth, seed,
                          P.err, SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, &sp));
   // ---- certify + rerank (per row; the bounds are global, so valid for every set)
   uint64_t* cand = nullptr;
@@ -2920,7 +2970,7 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   ra.metric = metric;
   ra.scale = P.scale;
   ra.depth = depth;
-  ra.seed = nullptr;
+  ra.seed = seed;
   ra.depth_hist = P.counters + 16;
   ra.qinfo = P.Q.info;
   ra.bmax = P.bmax;
