@@ -103,19 +103,17 @@ struct BaseMax {
 // Column means over an evenly spaced sample of rows.  Any centre keeps the
 // distances unchanged; a good one shrinks the BF16 values and their rounding.
 // Block (32 columns x 32 row groups): FP32 partial sums per thread, FP64 across groups.
-// Unit-normalised copy of every row (cosine): |x|^2 as the FP32 form's
-// sequential sum (kept for the rerank), x^ = x / sqrt(|x|^2); a zero row stays zero.
-__global__ void normalize_rows_kernel(const float* __restrict__ x, int64_t n, int d, float* __restrict__ xh,
-                                      float* __restrict__ sqn) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float* r = x + i * (int64_t)d;
-  float s = 0.0f;
-  for (int c = 0; c < d; ++c) s = __fmaf_rn(r[c], r[c], s);
-  sqn[i] = s;
-  const float nr = __fsqrt_rn(s);
-  float* o = xh + i * (int64_t)d;
-  for (int c = 0; c < d; ++c) o[c] = nr > 0.0f ? __fdiv_rn(r[c], nr) : 0.0f;
+// Unit-normalised copy of every row (cosine): x^ = x / sqrt(|x|^2) with
+// |x|^2 the FP32 form's sequential sum (row_sqnorm_kernel, kept for the
+// rerank); a zero row stays zero.  One warp per row, coalesced.
+__global__ void scale_rows_kernel(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ sqn,
+                                  float* __restrict__ xh) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n) return;
+  const float nr = __fsqrt_rn(sqn[row]);
+  const float* r = x + row * (int64_t)d;
+  float* o = xh + row * (int64_t)d;
+  for (int c = threadIdx.x & 31; c < d; c += 32) o[c] = nr > 0.0f ? __fdiv_rn(__ldg(r + c), nr) : 0.0f;
 }
 
 __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
@@ -2499,7 +2497,8 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
     float *xb = nullptr, *xq = nullptr;
     MANN_TRY(ctx->scratch_t(SLOT_COS_B, (size_t)n * d, &xb));
     MANN_TRY(ctx->scratch_t(SLOT_COS_NB, (size_t)n, &cos_bn));
-    normalize_rows_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, s>>>(base, n, d, xb, cos_bn);
+    MANN_TRY(launch_row_sqnorm(base, n, d, cos_bn, s));
+    scale_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, cos_bn, xb);
     MANN_CHECK_LAUNCH();
     mbase = xb;
     if (self) {
@@ -2508,7 +2507,8 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
     } else {
       MANN_TRY(ctx->scratch_t(SLOT_COS_Q, (size_t)nq * d, &xq));
       MANN_TRY(ctx->scratch_t(SLOT_COS_NQ, (size_t)nq, &cos_qn));
-      normalize_rows_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, s>>>(qs, nq, d, xq, cos_qn);
+      MANN_TRY(launch_row_sqnorm(qs, nq, d, cos_qn, s));
+      scale_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, cos_qn, xq);
       MANN_CHECK_LAUNCH();
       mqs = xq;
     }

@@ -27,14 +27,27 @@ constexpr unsigned FULL = 0xFFFFFFFFu;
 using wl::list_get;
 using wl::list_insert;
 
-__global__ void row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
-                                  float* __restrict__ out) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float* r = x + i * (int64_t)d;
+// Squared row norms as the FP32 form's sequential sum (dimension order, one
+// fmaf per term).  One warp per 32 rows: 32 x 32 tiles come in through
+// shared memory with coalesced loads (a row's 32 columns per load
+// instruction), then lane l adds row l's squares in order.
+__global__ void __launch_bounds__(256) row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
+                                                         float* __restrict__ out) {
+  __shared__ float tile[8][32][33];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r0 = ((int64_t)blockIdx.x * 8 + w) * 32;
+  if (r0 >= n) return;
+  const int nr = (int)min((int64_t)32, n - r0);
   float s = 0.0f;
-  for (int j = 0; j < d; ++j) s = __fmaf_rn(r[j], r[j], s);
-  out[i] = s;
+  for (int c0 = 0; c0 < d; c0 += 32) {
+    const int cw = min(32, d - c0);
+    for (int i = 0; i < nr; ++i) tile[w][i][lane] = lane < cw ? __ldg(&x[(r0 + i) * d + c0 + lane]) : 0.0f;
+    __syncwarp();
+    if (lane < nr)
+      for (int c = 0; c < cw; ++c) s = __fmaf_rn(tile[w][lane][c], tile[w][lane][c], s);
+    __syncwarp();
+  }
+  if (lane < nr) out[r0 + lane] = s;
 }
 
 // Thread-tile row/column maps.  TQ rows per thread: 8 -> {ty*4+i, 64+ty*4+i},
@@ -687,7 +700,7 @@ mann_status launch_merge_lists(const uint64_t* partial, int64_t nq, int nsplit, 
 
 mann_status launch_row_sqnorm(const float* x, int64_t n, int d, float* out, cudaStream_t s) {
   if (n <= 0) return MANN_OK;
-  row_sqnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, d, out);
+  row_sqnorm_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(x, n, d, out);  // 8 warps x 32 rows
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }
