@@ -586,6 +586,94 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
   return v;
 }
 
+// A row's list: the `depth` smallest keys seen, unsorted in shared memory
+// (entry e at list[e * BM]).  While it fills (nfill < depth) a key takes the
+// next slot and the threshold stays the row's seed key.  Once full, the
+// threshold is the largest entry (slot lslot); the entries form LGROUPS
+// groups of 8 whose maxima (and slots) stay in registers, so a new key that
+// replaces the largest entry costs a rescan of its group (8 independent
+// loads) and a 4-way compare instead of a rescan of all `depth` entries
+// (GROUPED: the many-set pass, where rows admit many candidates; measured
+// slower on the seeded single-set passes, so those keep the plain rescan).
+constexpr int LGROUPS = 4;             // LIST / 8
+constexpr int GROUPED_MIN_DEPTH = 24;  // single-set passes use the groups from this list depth
+
+__device__ __forceinline__ void list_group_max(const uint64_t* __restrict__ list, int g, int depth, uint64_t& m,
+                                               int& ms) {
+  m = 0;
+  ms = 8 * g;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int e = 8 * g + i;
+    const uint64_t v = e < depth ? list[e * BM] : 0ull;
+    if (v > m) {
+      m = v;
+      ms = e;
+    }
+  }
+}
+
+template <bool GROUPED>
+__device__ __forceinline__ void list_admit(uint64_t* __restrict__ list, uint64_t c, uint64_t& thr_key,
+                                           float& thr_est, int& lslot, int& nfill, int depth,
+                                           uint64_t (&gmax)[LGROUPS], int (&gidx)[LGROUPS]) {
+  if (!(c < thr_key)) return;
+  if (!GROUPED) {
+    // plain form: the new key replaces the largest entry and all `depth`
+    // entries are rescanned (independent loads; cheapest where admissions are
+    // rare, e.g. rows with an admission seed)
+    if (nfill < depth) {
+      list[nfill * BM] = c;  // an empty slot: the threshold stays the seed until the list is full
+      if (++nfill < depth) return;
+    } else {
+      list[lslot * BM] = c;  // the largest entry drops out
+    }
+    uint64_t m = 0;
+    int ms = 0;
+#pragma unroll 8
+    for (int e2 = 0; e2 < depth; ++e2) {
+      const uint64_t v2 = list[e2 * BM];
+      if (v2 > m) {
+        m = v2;
+        ms = e2;
+      }
+    }
+    lslot = ms;
+    thr_key = m;
+    thr_est = key_dist(thr_key);
+    return;
+  }
+  if (nfill < depth) {
+    list[nfill * BM] = c;  // an empty slot: the threshold stays the seed until the list is full
+    if (++nfill < depth) return;
+#pragma unroll
+    for (int g = 0; g < LGROUPS; ++g) list_group_max(list, g, depth, gmax[g], gidx[g]);
+  } else {
+    list[lslot * BM] = c;  // the largest entry drops out
+    const int g = lslot >> 3;
+    uint64_t m;
+    int ms;
+    list_group_max(list, g, depth, m, ms);
+#pragma unroll
+    for (int gg = 0; gg < LGROUPS; ++gg)
+      if (gg == g) {
+        gmax[gg] = m;
+        gidx[gg] = ms;
+      }
+  }
+  uint64_t m = gmax[0];
+  int ms = gidx[0];
+#pragma unroll
+  for (int g = 1; g < LGROUPS; ++g)
+    if (gmax[g] > m) {
+      m = gmax[g];
+      ms = gidx[g];
+    }
+  lslot = ms;
+  thr_key = m;
+  thr_est = key_dist(thr_key);
+}
+
 // One 32-column chunk of the epilogue.  Lane r owns row r of the warp's 32
 // rows: v holds the row's 32 accumulators of the chunk; lane j's nbv is the
 // norm of the chunk's point j (read by shuffle).  The row's list lives in
@@ -599,11 +687,12 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 // rescanned for the new largest (independent loads, conflict-free while the
 // lanes run in step; a sorted insert would be a chain of dependent
 // shared-memory loads).
-template <bool FP8>
+template <bool FP8, bool GROUPED>
 __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, float csv, float rs,
                                           uint64_t* __restrict__ mylist,
-                                          uint64_t& thr_key, float& thr_est, uint64_t seed_key,
-                                          int& lslot, int& nfill, uint32_t col0, int depth) {
+                                          uint64_t& thr_key, float& thr_est, int& lslot, int& nfill,
+                                          uint32_t col0, int depth, uint64_t (&gmax)[LGROUPS],
+                                          int (&gidx)[LGROUPS]) {
   // est' = ||p~||^2 - 2 q~.p~; in the FP8 form the accumulator holds the sum of
   // e4m3 products and -2 (1/f_q) (1/f_p) = rs * csv (a power of two) rescales it
   float e[32];
@@ -630,28 +719,7 @@ __device__ __forceinline__ void epi_chunk(const uint32_t (&v)[32], float nbv, fl
 #pragma unroll
       for (int u = 1; u < 32; ++u) val = j == u ? e[u] : val;
       const uint64_t c = make_key(val, col0 + (uint32_t)j);
-      if (c < thr_key) {
-        if (nfill < depth) {
-          // an empty slot: the threshold stays the seed until the list is full
-          mylist[nfill * BM] = c;
-          if (++nfill < depth) continue;
-        } else {
-          mylist[lslot * BM] = c;  // the largest entry drops out
-        }
-        uint64_t m = 0;
-        int ms = 0;
-#pragma unroll 8
-        for (int e2 = 0; e2 < depth; ++e2) {
-          const uint64_t v2 = mylist[e2 * BM];
-          if (v2 > m) {
-            m = v2;
-            ms = e2;
-          }
-        }
-        lslot = ms;
-        thr_key = m == KEY_NONE ? seed_key : m;
-        thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
-      }
+      list_admit<GROUPED>(mylist, c, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
     }
   }
 }
@@ -701,9 +769,11 @@ __device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, f
 // est = -2 acc = ||q~ - p~||^2 (an exact scaling): the chunk's smallest est is
 // -2 max(acc), one FMNMX per value and no per-column norm.  Columns j >=
 // nvalid lie past the tile's last point (or in another point set).
+template <bool GROUPED>
 __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t* __restrict__ mylist,
-                                               uint64_t& thr_key, float& thr_est, uint64_t seed_key, int& lslot,
-                                               int& nfill, uint32_t col0, int depth) {
+                                               uint64_t& thr_key, float& thr_est, int& lslot, int& nfill,
+                                               uint32_t col0, int depth, uint64_t (&gmax)[LGROUPS],
+                                               int (&gidx)[LGROUPS]) {
   if (nvalid < 32) {
 #pragma unroll
     for (int j = 0; j < 32; ++j)
@@ -729,27 +799,7 @@ __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, ui
 #pragma unroll
       for (int u = 1; u < 32; ++u) bits = j == u ? v[u] : bits;
       const uint64_t c = make_key(-2.0f * __uint_as_float(bits), col0 + (uint32_t)j);
-      if (c < thr_key) {
-        if (nfill < depth) {
-          mylist[nfill * BM] = c;
-          if (++nfill < depth) continue;
-        } else {
-          mylist[lslot * BM] = c;
-        }
-        uint64_t m = 0;
-        int ms = 0;
-#pragma unroll 8
-        for (int e2 = 0; e2 < depth; ++e2) {
-          const uint64_t v2 = mylist[e2 * BM];
-          if (v2 > m) {
-            m = v2;
-            ms = e2;
-          }
-        }
-        lslot = ms;
-        thr_key = m == KEY_NONE ? seed_key : m;
-        thr_est = thr_key == KEY_NONE ? __int_as_float(0x7F800000) : key_dist(thr_key);
-      }
+      list_admit<GROUPED>(mylist, c, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
     }
   }
 }
@@ -815,7 +865,7 @@ static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2)
 // commits arrive on the stage and accumulator barriers of both CTAs, and both
 // CTAs' epilogue warps release an accumulator on the even CTA's barrier.  The
 // work unit (a walk item) is then one pair tile and `a.w.grid` counts pairs.
-template <int CAP, int NSETS, bool PAIR, bool FP8>
+template <int CAP, int NSETS, bool PAIR, bool FP8, bool GROUPED = false>
 __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
             MainArgs a) {
@@ -983,6 +1033,13 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
     int lslot = 0, nfill = 0;
+    uint64_t gmax[LGROUPS];  // the list's group maxima and their slots (list_admit)
+    int gidx[LGROUPS];
+#pragma unroll
+    for (int g = 0; g < LGROUPS; ++g) {
+      gmax[g] = 0;
+      gidx[g] = 8 * g;
+    }
     uint64_t top[SEED_DEPTH];
 #pragma unroll
     for (int i = 0; i < SEED_DEPTH; ++i) top[i] = KEY_NONE;
@@ -1087,15 +1144,15 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           if (a.seedmode)
             seed_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, top, (uint32_t)(col0 + ch * 32));
           else
-            epi_chunk<FP8>(va, pick(nbc, ch), cs_a, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                           (uint32_t)(col0 + ch * 32), a.depth);
+            epi_chunk<FP8, GROUPED>(va, pick(nbc, ch), cs_a, rs, mylist, thr_key, thr_est, lslot, nfill,
+                           (uint32_t)(col0 + ch * 32), a.depth, gmax, gidx);
         } else {
           const int nva = (int)min((int64_t)32, v.cend - (col0 + ch * 32));
           if (a.seedmode)
             seed_chunk_fold(va, nva, top, (uint32_t)(col0 + ch * 32));
           else
-            epi_chunk_fold(va, nva, mylist, thr_key, thr_est, seed_key, lslot, nfill, (uint32_t)(col0 + ch * 32),
-                           a.depth);
+            epi_chunk_fold<GROUPED>(va, nva, mylist, thr_key, thr_est, lslot, nfill, (uint32_t)(col0 + ch * 32),
+                           a.depth, gmax, gidx);
         }
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
@@ -1116,15 +1173,15 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
           if (a.seedmode)
             seed_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, top, (uint32_t)(col0 + (ch + 1) * 32));
           else
-            epi_chunk<FP8>(vb, pick(nbc, ch + 1), cs_b, rs, mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                           (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+            epi_chunk<FP8, GROUPED>(vb, pick(nbc, ch + 1), cs_b, rs, mylist, thr_key, thr_est, lslot, nfill,
+                           (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx);
         } else {
           const int nvb = (int)min((int64_t)32, v.cend - (col0 + (ch + 1) * 32));
           if (a.seedmode)
             seed_chunk_fold(vb, nvb, top, (uint32_t)(col0 + (ch + 1) * 32));
           else
-            epi_chunk_fold(vb, nvb, mylist, thr_key, thr_est, seed_key, lslot, nfill,
-                           (uint32_t)(col0 + (ch + 1) * 32), a.depth);
+            epi_chunk_fold<GROUPED>(vb, nvb, mylist, thr_key, thr_est, lslot, nfill,
+                           (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx);
         }
         ptx::tmem_ld_wait();
       }
@@ -2259,10 +2316,10 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
 }
 
 // Launch of one k2_main instance: `units` CTAs, or `units` clusters of two CTAs (PAIR).
-template <int CAP, int NSETS, bool PAIR, bool FP8 = false>
+template <int CAP, int NSETS, bool PAIR, bool FP8 = false, bool GROUPED = false>
 mann_status launch_k2(const CUtensorMap& mapA, const CUtensorMap& mapB, const MainArgs& ma, int units, size_t smem,
                       cudaStream_t s) {
-  auto fn = k2_main<CAP, NSETS, PAIR, FP8>;
+  auto fn = k2_main<CAP, NSETS, PAIR, FP8, GROUPED>;
   MANN_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(PAIR ? 2 * units : units));
@@ -2427,6 +2484,13 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
       MANN_TRY((launch_k2<16, 2, false, true>(mapA, mapB, ma, w.grid, smem, s)));
     else
       MANN_TRY((launch_k2<32, 1, false, true>(mapA, mapB, ma, w.grid, smem, s)));
+  } else if (!seedmode && (seg || depth >= GROUPED_MIN_DEPTH)) {
+    // grouped list maxima where rows admit many candidates: the many-set pass
+    // (short per-set scans) and deep lists
+    if (nsets == 2)
+      MANN_TRY((launch_k2<16, 2, false, false, true>(mapA, mapB, ma, w.grid, smem, s)));
+    else
+      MANN_TRY((launch_k2<32, 1, false, false, true>(mapA, mapB, ma, w.grid, smem, s)));
   } else {
     if (nsets == 2)
       MANN_TRY((launch_k2<16, 2, false>(mapA, mapB, ma, w.grid, smem, s)));
