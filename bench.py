@@ -68,7 +68,8 @@ def parse():
     ap.add_argument("--no-angular", action="store_true", help="skip the angular (cosine) leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain 64-d FP32 leg")
     ap.add_argument("--no-fp8", action="store_true", help="skip the FP8-form measurement")
-    ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "ivf-profile", "angular", "plain"],
+    ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "batched-profile", "ivf-profile", "angular",
+                                       "plain"],
                     default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
                          "launches per step), for ncu captures")
@@ -603,6 +604,34 @@ def run_batched_leg(args, stream_ptr=0):
             "edge_weights": {"rule": "CurvatureFreeSymmetric", "ms": wt_ms, "edges_per_s": N * 15 / (wt_ms / 1e3)}}
 
 
+def run_batched_profile_case(args):
+    """Case for ncu: the BF16 form of the batched graphs only, on 16 manifold
+    clouds (2,000-20,000 points, d = 32, k = 15; ~99k points): per call a
+    segmented seed pass and a segmented main pass (k2_main), warmup + steps
+    calls."""
+    import torch
+
+    from manifoldann_gb300 import _lib, synthetic
+
+    lib = _lib.load()
+    clouds = synthetic.manifold_clouds(16, 2000, 20000, 32, seed=2)
+    X = torch.from_numpy(np.ascontiguousarray(np.concatenate(clouds))).cuda()
+    offs = np.zeros(len(clouds) + 1, np.int64)
+    offs[1:] = np.cumsum([len(c) for c in clouds])
+    n = int(offs[-1])
+    ids = torch.empty((n, 15), dtype=torch.int32, device="cuda")
+    dd = torch.empty((n, 15), dtype=torch.float32, device="cuda")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = _lib.params(_lib.METRIC_SQEUCLIDEAN, 15, _lib.PREC_BF16)
+    for _ in range(args.warmup + args.steps):
+        _lib.check(lib.mann_knn_graph_batched_device(p, X.data_ptr(), offs.ctypes.data, len(clouds), 32, 0,
+                                                     ids.data_ptr(), dd.data_ptr(), None, sp))
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "batched-profile", "points": n, "calls": args.warmup + args.steps,
+                      "k2_main_launches": 2 * (args.warmup + args.steps)}), flush=True)
+    return 0
+
+
 def run_ivf_profile_case(args):
     """Case for ncu: IVF searches only (learned routing with an untrained
     network of the same shape -- same kernels and sizes -- then centroid
@@ -1053,6 +1082,8 @@ def main():
         print(json.dumps({"case": "plain", "plain_fp32": run_plain_leg(
             args, C.c_void_p(torch.cuda.current_stream().cuda_stream))}), flush=True)
         return 0
+    if args.case == "batched-profile":
+        return run_batched_profile_case(args)
     if args.case == "batched":
         import torch
 
