@@ -1346,11 +1346,17 @@ __device__ __forceinline__ float fp32_cos_row(const float* __restrict__ x, const
   return v;
 }
 
-// One query row (one warp): certify, then rerank the candidates.  The row's
-// certificate depth goes to the warp's histogram hist_w and its candidate
-// count to cand_sum (lane 0), flushed to global memory once per warp.
-__device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int lane, int* hist_w,
-                                           unsigned long long& cand_sum) {
+// Certificate of one query row (lane 0 computes it, the warp shares it): the
+// threshold T (every point of the exact top-k has est <= T), the floor of
+// non-candidates' exact distances, and whether the row is certified; the
+// row's certificate depth goes to the warp's histogram and an uncertified row
+// is queued for the FP32 form.
+struct RowCert {
+  float T, d_floor, qn;
+  bool certified, all_in;
+};
+
+__device__ __forceinline__ RowCert rerank_certify(const RerankArgs& a, int64_t q, int lane, int* hist_w) {
   const uint64_t* lst = a.lists + q * a.L;
   const uint64_t ek_key = lst[a.kreq - 1];
   const uint64_t last_key = lst[a.depth - 1];
@@ -1429,111 +1435,20 @@ __device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int l
       a.fb_rows[slot] = (int)q;
       a.cand_count[q] = -1;
     }
-    return;
+    return RowCert{T, d_floor, qn, false, all_in};
   }
   if (all_in) d_floor = 3.0e38f;
-  const float* qrow = a.qs + q * a.d;
-  // candidates: entries with est <= T (the list is sorted by est)
-  uint64_t key[2] = {KEY_NONE, KEY_NONE};
-  int ncand = 0;
-  if (a.coop && a.L == 32) {
-    // The warp streams its candidates' rows through shared memory in chunks
-    // of RR_CH dimensions (cp.async, 16 bytes a lane, two chunks in flight);
-    // lane i then adds candidate i's chunk to its sequential FP32 sum, in the
-    // same order as the one-lane-per-row form.
-    __shared__ __align__(16) float rr_rows[RR_WARPS][2][32 * RR_STR];
-    __shared__ __align__(16) float rr_q[RR_WARPS][2][RR_CH];
-    __shared__ int rr_id[RR_WARPS][32];
-    const int w = threadIdx.x >> 5;
-    const uint64_t k0 = lst[lane];
-    const bool isc = k0 != KEY_NONE && __fadd_rd(key_dist(k0), qn) <= T;
-    const unsigned cm = __ballot_sync(FULL, isc);
-    const int nc = __popc(cm);
-    if (isc) rr_id[w][__popc(cm & ((1u << lane) - 1u))] = key_id(k0);
-    __syncwarp();
-    const int nch = (a.d + RR_CH - 1) / RR_CH;
-    auto issue = [&](int chunk, int b) {
-      const int c0 = chunk * RR_CH;
-      const int cw = min(RR_CH, a.d - c0);
-      const int c4 = lane & 15;
-      if (c4 * 4 < cw) {
-        for (int r = lane >> 4; r < nc; r += 2)
-          ptx::cp_async16(&rr_rows[w][b][r * RR_STR + c4 * 4], a.base + (int64_t)rr_id[w][r] * a.d + c0 + c4 * 4);
-        if (lane < 16) ptx::cp_async16(&rr_q[w][b][c4 * 4], qrow + c0 + c4 * 4);
-      }
-      ptx::cp_async_commit();
-    };
-    float acc = 0.0f;
-    issue(0, 0);
-    for (int chunk = 0; chunk < nch; ++chunk) {
-      const int b = chunk & 1;
-      if (chunk + 1 < nch) {
-        issue(chunk + 1, b ^ 1);
-        ptx::cp_async_wait<1>();
-      } else {
-        ptx::cp_async_wait<0>();
-      }
-      __syncwarp();
-      if (lane < nc) {
-        // float4 reads: a quarter-warp's rows start 272 bytes apart, so its
-        // 16-byte reads fall in distinct banks; the query chunk is a broadcast
-        const float4* row = reinterpret_cast<const float4*>(&rr_rows[w][b][lane * RR_STR]);
-        const float4* qq = reinterpret_cast<const float4*>(rr_q[w][b]);
-        const int cw4 = min(RR_CH, a.d - chunk * RR_CH) >> 2;  // d % 4 == 0 here
-        if (cosine) {
-#pragma unroll 4
-          for (int c = 0; c < cw4; ++c) {
-            const float4 x = qq[c], y = row[c];
-            acc = __fmaf_rn(x.x, y.x, acc);
-            acc = __fmaf_rn(x.y, y.y, acc);
-            acc = __fmaf_rn(x.z, y.z, acc);
-            acc = __fmaf_rn(x.w, y.w, acc);
-          }
-        } else {
-#pragma unroll 4
-          for (int c = 0; c < cw4; ++c) {
-            const float4 x = qq[c], y = row[c];
-            float t = __fsub_rn(x.x, y.x);
-            acc = __fmaf_rn(t, t, acc);
-            t = __fsub_rn(x.y, y.y);
-            acc = __fmaf_rn(t, t, acc);
-            t = __fsub_rn(x.z, y.z);
-            acc = __fmaf_rn(t, t, acc);
-            t = __fsub_rn(x.w, y.w);
-            acc = __fmaf_rn(t, t, acc);
-          }
-        }
-      }
-      __syncwarp();  // the buffer is refilled two chunks on
-    }
-    if (lane < nc) {
-      const int id = rr_id[w][lane];
-      float dist;
-      if (cosine) {
-        const float den = __fmul_rn(__fsqrt_rn(a.cos_qn[q]), __fsqrt_rn(a.cos_bn[id]));
-        dist = __fsub_rn(1.0f, __fdiv_rn(acc, den));
-        if (dist < 0.0f) dist = 0.0f;
-      } else {
-        dist = a.metric == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc) : acc;
-      }
-      key[0] = make_key(dist, (uint32_t)id);
-    }
-  } else {
-#pragma unroll
-    for (int s = 0; s < 2; ++s) {
-      const int e = s * 32 + lane;
-      if (e < a.L) {
-        const uint64_t k = lst[e];
-        if (k != KEY_NONE && __fadd_rd(key_dist(k), qn) <= T) {
-          const int id = key_id(k);
-          const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
-                                    : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
-          key[s] = make_key(dist, (uint32_t)id);
-        }
-      }
-    }
-  }
-  ncand = __popc(__ballot_sync(FULL, key[0] != KEY_NONE)) + __popc(__ballot_sync(FULL, key[1] != KEY_NONE));
+  return RowCert{T, d_floor, qn, true, all_in};
+}
+
+// The row's candidates, one key per lane in key[] (KEY_NONE elsewhere), go to
+// its candidate table sorted by (distance, id), with its count and floor.
+__device__ __forceinline__ void rerank_finish(const RerankArgs& a, int64_t q, int lane, const uint64_t (&key)[2],
+                                              const RowCert& cr, unsigned long long& cand_sum) {
+  const bool cosine = a.metric == MANN_METRIC_COSINE;
+  const bool all_in = cr.all_in;
+  const float d_floor = cr.d_floor;
+  const int ncand = __popc(__ballot_sync(FULL, key[0] != KEY_NONE)) + __popc(__ballot_sync(FULL, key[1] != KEY_NONE));
   if (cosine && !all_in) {
     // a zero-norm point has a NaN cosine and no bound from the unit-norm
     // pass: a row that needs such points (fewer than k finite candidates)
@@ -1574,6 +1489,175 @@ __device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int l
   }
 }
 
+
+// Exact FP32 distances of the candidates (list entries with est <= T) of one
+// or two certified rows, one lane per candidate: row 0's candidates take lanes
+// [0, nc0) and row 1's the next ones (the caller keeps the total <= 32).  The
+// warp streams the candidates' rows through shared memory in chunks of RR_CH
+// dimensions (cp.async, 16 bytes a lane, two chunks in flight), with each
+// row's query chunk beside them; lane i then adds candidate i's chunk to its
+// sequential FP32 sum, in the same order as the one-lane-per-row form.
+// Two rows per warp fill the lanes that one row's ~11 candidates leave idle.
+// Returns this lane's key (KEY_NONE past the candidates).
+__device__ __forceinline__ uint64_t rerank_coop(const RerankArgs& a, int ng, const int64_t (&qv)[2],
+                                                const RowCert (&cr)[2], int lane, int& nc0) {
+  __shared__ __align__(16) float rr_rows[RR_WARPS][2][32 * RR_STR];
+  __shared__ __align__(16) float rr_q[RR_WARPS][2][2][RR_CH];
+  __shared__ int rr_id[RR_WARPS][32];
+  const bool cosine = a.metric == MANN_METRIC_COSINE;
+  const int w = threadIdx.x >> 5;
+  int nc = 0;
+  nc0 = 0;
+  for (int g = 0; g < ng; ++g) {
+    const uint64_t k0 = a.lists[qv[g] * a.L + lane];
+    const bool isc = k0 != KEY_NONE && __fadd_rd(key_dist(k0), cr[g].qn) <= cr[g].T;
+    const unsigned cm = __ballot_sync(FULL, isc);
+    if (isc) rr_id[w][nc + __popc(cm & ((1u << lane) - 1u))] = key_id(k0);
+    if (g == 0) nc0 = __popc(cm);
+    nc += __popc(cm);
+  }
+  __syncwarp();
+  const int gl = lane < nc0 ? 0 : 1;  // this lane's row
+  const float* qrow0 = a.qs + qv[0] * a.d;
+  const float* qrow1 = a.qs + qv[ng > 1 ? 1 : 0] * a.d;
+  const int nch = (a.d + RR_CH - 1) / RR_CH;
+  auto issue = [&](int chunk, int b) {
+    const int c0 = chunk * RR_CH;
+    const int cw = min(RR_CH, a.d - c0);
+    const int c4 = lane & 15;
+    if (c4 * 4 < cw) {
+      for (int r = lane >> 4; r < nc; r += 2)
+        ptx::cp_async16(&rr_rows[w][b][r * RR_STR + c4 * 4], a.base + (int64_t)rr_id[w][r] * a.d + c0 + c4 * 4);
+      if (lane < 16)
+        ptx::cp_async16(&rr_q[w][b][0][c4 * 4], qrow0 + c0 + c4 * 4);
+      else if (ng > 1)
+        ptx::cp_async16(&rr_q[w][b][1][c4 * 4], qrow1 + c0 + c4 * 4);
+    }
+    ptx::cp_async_commit();
+  };
+  float acc = 0.0f;
+  issue(0, 0);
+  for (int chunk = 0; chunk < nch; ++chunk) {
+    const int b = chunk & 1;
+    if (chunk + 1 < nch) {
+      issue(chunk + 1, b ^ 1);
+      ptx::cp_async_wait<1>();
+    } else {
+      ptx::cp_async_wait<0>();
+    }
+    __syncwarp();
+    if (lane < nc) {
+      // float4 reads: a quarter-warp's rows start 272 bytes apart, so its
+      // 16-byte reads fall in distinct banks; a row's query chunk is a broadcast
+      const float4* row = reinterpret_cast<const float4*>(&rr_rows[w][b][lane * RR_STR]);
+      const float4* qq = reinterpret_cast<const float4*>(rr_q[w][b][gl]);
+      const int cw4 = min(RR_CH, a.d - chunk * RR_CH) >> 2;  // d % 4 == 0 here
+      if (cosine) {
+#pragma unroll 4
+        for (int c = 0; c < cw4; ++c) {
+          const float4 x = qq[c], y = row[c];
+          acc = __fmaf_rn(x.x, y.x, acc);
+          acc = __fmaf_rn(x.y, y.y, acc);
+          acc = __fmaf_rn(x.z, y.z, acc);
+          acc = __fmaf_rn(x.w, y.w, acc);
+        }
+      } else {
+#pragma unroll 4
+        for (int c = 0; c < cw4; ++c) {
+          const float4 x = qq[c], y = row[c];
+          float t = __fsub_rn(x.x, y.x);
+          acc = __fmaf_rn(t, t, acc);
+          t = __fsub_rn(x.y, y.y);
+          acc = __fmaf_rn(t, t, acc);
+          t = __fsub_rn(x.z, y.z);
+          acc = __fmaf_rn(t, t, acc);
+          t = __fsub_rn(x.w, y.w);
+          acc = __fmaf_rn(t, t, acc);
+        }
+      }
+    }
+    __syncwarp();  // the buffer is refilled two chunks on
+  }
+  if (lane >= nc) return KEY_NONE;
+  const int id = rr_id[w][lane];
+  float dist;
+  if (cosine) {
+    const float den = __fmul_rn(__fsqrt_rn(a.cos_qn[qv[gl]]), __fsqrt_rn(a.cos_bn[id]));
+    dist = __fsub_rn(1.0f, __fdiv_rn(acc, den));
+    if (dist < 0.0f) dist = 0.0f;
+  } else {
+    dist = a.metric == MANN_METRIC_EUCLIDEAN ? __fsqrt_rn(acc) : acc;
+  }
+  return make_key(dist, (uint32_t)id);
+}
+
+// One query row (one warp): certify, then rerank the candidates.  The row's
+// certificate depth goes to the warp's histogram hist_w and its candidate
+// count to cand_sum (lane 0), flushed to global memory once per warp.
+__device__ __forceinline__ void rerank_row(const RerankArgs& a, int64_t q, int lane, int* hist_w,
+                                           unsigned long long& cand_sum) {
+  const RowCert cr = rerank_certify(a, q, lane, hist_w);
+  if (!cr.certified) return;
+  uint64_t key[2] = {KEY_NONE, KEY_NONE};
+  if (a.coop && a.L == 32) {
+    const int64_t qv[2] = {q, q};
+    const RowCert crs[2] = {cr, cr};
+    int nc0 = 0;
+    key[0] = rerank_coop(a, 1, qv, crs, lane, nc0);
+  } else {
+    const bool cosine = a.metric == MANN_METRIC_COSINE;
+    const uint64_t* lst = a.lists + q * a.L;
+    const float* qrow = a.qs + q * a.d;
+    const float qn = cr.qn, T = cr.T;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int e = s * 32 + lane;
+      if (e < a.L) {
+        const uint64_t k = lst[e];
+        if (k != KEY_NONE && __fadd_rd(key_dist(k), qn) <= T) {
+          const int id = key_id(k);
+          const float dist = cosine ? fp32_cos_row(qrow, a.base + (int64_t)id * a.d, a.d, a.cos_qn[q], a.cos_bn[id])
+                                    : fp32_dist_row(qrow, a.base + (int64_t)id * a.d, a.d, a.metric);
+          key[s] = make_key(dist, (uint32_t)id);
+        }
+      }
+    }
+  }
+  rerank_finish(a, q, lane, key, cr, cand_sum);
+}
+
+// Two query rows in one warp (the shared-memory path): both certified and
+// together at most 32 candidates -> one pass over both rows' candidates.
+__device__ __forceinline__ void rerank_pair(const RerankArgs& a, int64_t qa, int64_t qb, int lane, int* hist_w,
+                                            unsigned long long& cand_sum) {
+  const RowCert ca = rerank_certify(a, qa, lane, hist_w);
+  const RowCert cb = rerank_certify(a, qb, lane, hist_w);
+  auto count = [&](int64_t q, const RowCert& c) {
+    const uint64_t k0 = a.lists[q * a.L + lane];
+    return __popc(__ballot_sync(FULL, c.certified && k0 != KEY_NONE && __fadd_rd(key_dist(k0), c.qn) <= c.T));
+  };
+  const int na = count(qa, ca), nb = count(qb, cb);
+  const int64_t qv[2] = {qa, qb};
+  const RowCert crs[2] = {ca, cb};
+  if (ca.certified && cb.certified && na + nb <= 32) {
+    int nc0 = 0;
+    const uint64_t k = rerank_coop(a, 2, qv, crs, lane, nc0);
+    const uint64_t ka[2] = {lane < nc0 ? k : KEY_NONE, KEY_NONE};
+    const uint64_t kb[2] = {lane >= nc0 ? k : KEY_NONE, KEY_NONE};
+    rerank_finish(a, qa, lane, ka, ca, cand_sum);
+    rerank_finish(a, qb, lane, kb, cb, cand_sum);
+    return;
+  }
+  for (int g = 0; g < 2; ++g) {
+    if (!crs[g].certified) continue;
+    const int64_t qs1[2] = {qv[g], qv[g]};
+    const RowCert cs1[2] = {crs[g], crs[g]};
+    int nc0 = 0;
+    const uint64_t key[2] = {rerank_coop(a, 1, qs1, cs1, lane, nc0), KEY_NONE};
+    rerank_finish(a, qv[g], lane, key, crs[g], cand_sum);
+  }
+}
+
 // Warps stride over the query rows; per-warp histogram and candidate count
 // reach global memory with one set of atomics per warp, not per row.
 __global__ void __launch_bounds__(32 * RR_WARPS) k2_rerank(RerankArgs a) {
@@ -1583,7 +1667,17 @@ __global__ void __launch_bounds__(32 * RR_WARPS) k2_rerank(RerankArgs a) {
   __syncwarp();
   unsigned long long csum = 0;
   const int64_t nw = (int64_t)gridDim.x * RR_WARPS;
-  for (int64_t q = (int64_t)blockIdx.x * RR_WARPS + w; q < a.nq; q += nw) rerank_row(a, q, lane, hist[w], csum);
+  if (a.coop && a.L == 32) {
+    // the shared-memory path takes rows two at a time
+    for (int64_t q = 2 * ((int64_t)blockIdx.x * RR_WARPS + w); q < a.nq; q += 2 * nw) {
+      if (q + 1 < a.nq)
+        rerank_pair(a, q, q + 1, lane, hist[w], csum);
+      else
+        rerank_row(a, q, lane, hist[w], csum);
+    }
+  } else {
+    for (int64_t q = (int64_t)blockIdx.x * RR_WARPS + w; q < a.nq; q += nw) rerank_row(a, q, lane, hist[w], csum);
+  }
   __syncwarp();
   for (int i = lane; i < LIST + 2; i += 32)
     if (hist[w][i]) atomicAdd(&a.depth_hist[i], (unsigned long long)hist[w][i]);
