@@ -835,12 +835,13 @@ __device__ __forceinline__ void seed_chunk_fold(uint32_t (&v)[32], int nvalid, u
 
 // Shared-memory footprint of k2_main<CAP, NSETS>.
 template <bool PAIR>
-__host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets) {
-  return 1024 /* alignment */ + (size_t)Stg<PAIR>::N * Stg<PAIR>::BYTES +
-         (size_t)nsets * BM * cap * 8 /* lists */ + (2 * Stg<PAIR>::N + 4) * 8 + 16;
+__host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets, int stages = Stg<PAIR>::N) {
+  return 1024 /* alignment */ + (size_t)stages * Stg<PAIR>::BYTES +
+         (size_t)nsets * BM * cap * 8 /* lists */ + (2 * stages + 4) * 8 + 16;
 }
 static_assert(k2_smem_bytes<false>(32, 1) <= 232448 && k2_smem_bytes<false>(16, 2) <= 232448, "k2_main shared memory");
 static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2) <= 232448, "k2_main shared memory");
+static_assert(k2_smem_bytes<false>(24, 2, 3) <= 232448, "k2_main shared memory");
 
 // The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
 // ||q~||^2 is left out: it does not change the row's order).  A point is
@@ -865,14 +866,14 @@ static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2)
 // commits arrive on the stage and accumulator barriers of both CTAs, and both
 // CTAs' epilogue warps release an accumulator on the even CTA's barrier.  The
 // work unit (a walk item) is then one pair tile and `a.w.grid` counts pairs.
-template <int CAP, int NSETS, bool PAIR, bool FP8, bool GROUPED = false>
+template <int CAP, int NSETS, bool PAIR, bool FP8, bool GROUPED = false, int NST = 0>
 __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     k2_main(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
             MainArgs a) {
   constexpr int NEPI = 4 * NSETS;
   constexpr int EPS = FP8 ? 128 : BK;  // operand elements per 128-byte stage row
   constexpr int EPK = EPS / 4;         // elements per MMA (K): 16 BF16 or 32 E4M3
-  constexpr int STAGES = Stg<PAIR>::N;
+  constexpr int STAGES = NST > 0 ? NST : Stg<PAIR>::N;
   constexpr int STAGE_BYTES = Stg<PAIR>::BYTES;
   constexpr int QROWS = PAIR ? 2 * BM : BM;  // query rows of one work unit
   extern __shared__ __align__(1024) uint8_t k2_smem_raw[];
@@ -2410,10 +2411,10 @@ int h_cta_of(int64_t i, int64_t work, int grid) {
 }
 
 // Launch of one k2_main instance: `units` CTAs, or `units` clusters of two CTAs (PAIR).
-template <int CAP, int NSETS, bool PAIR, bool FP8 = false, bool GROUPED = false>
+template <int CAP, int NSETS, bool PAIR, bool FP8 = false, bool GROUPED = false, int NST = 0>
 mann_status launch_k2(const CUtensorMap& mapA, const CUtensorMap& mapB, const MainArgs& ma, int units, size_t smem,
                       cudaStream_t s) {
-  auto fn = k2_main<CAP, NSETS, PAIR, FP8, GROUPED>;
+  auto fn = k2_main<CAP, NSETS, PAIR, FP8, GROUPED, NST>;
   MANN_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(PAIR ? 2 * units : units));
@@ -2484,9 +2485,14 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
                           bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr,
                           const float* qscale = nullptr, const float* bscale = nullptr) {
   const bool fp8 = qscale != nullptr;
+  const int nkb = (int)(augx > 0 ? ceil_div(augx + AUG, BK) : ceil_div(mainw, fp8 ? 128 : BK));
+  // the many-set pass with at most three K-stages per tile (small d): three
+  // pipeline stages leave shared memory for two epilogue sets of 24-entry
+  // lists, so eight warps admit candidates instead of four
+  const bool seg3 = seg && !seedmode && !fp8 && depth > 16 && depth <= 24 && nkb <= 3;
   // two epilogue sets with 16-entry lists when the depth allows it; each set
   // writes its own slot
-  const int nsets = depth <= 16 ? 2 : 1;
+  const int nsets = (depth <= 16 || seg3) ? 2 : 1;
   // CTA pairs (cta_group::2) when there are at least two 128-row query blocks
   const int pairs = (K2_USE_PAIRS && nq > BM && !seg && !fp8)
                         ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx))
@@ -2547,7 +2553,7 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.n = n;
   ma.d = d;
   ma.dp = mainw;
-  ma.nkb = (int)(augx > 0 ? ceil_div(augx + AUG, BK) : ceil_div(mainw, fp8 ? 128 : BK));
+  ma.nkb = nkb;
   ma.augx = augx;
   ma.w = w;
   ma.titems = seg ? seg->items : nullptr;
@@ -2564,8 +2570,9 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.partial = partial;
   ma.err = err;
   ma.seedmode = seedmode;
-  const size_t smem = pair ? k2_smem_bytes<true>(nsets == 2 ? 16 : 32, nsets)
-                           : k2_smem_bytes<false>(nsets == 2 ? 16 : 32, nsets);
+  const size_t smem = pair   ? k2_smem_bytes<true>(nsets == 2 ? 16 : 32, nsets)
+                     : seg3 ? k2_smem_bytes<false>(24, 2, 3)
+                            : k2_smem_bytes<false>(nsets == 2 ? 16 : 32, nsets);
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
   if (timed) ctx->time_begin(s);
   if (pair) {
@@ -2578,6 +2585,8 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
       MANN_TRY((launch_k2<16, 2, false, true>(mapA, mapB, ma, w.grid, smem, s)));
     else
       MANN_TRY((launch_k2<32, 1, false, true>(mapA, mapB, ma, w.grid, smem, s)));
+  } else if (seg3) {
+    MANN_TRY((launch_k2<24, 2, false, false, true, 3>(mapA, mapB, ma, w.grid, smem, s)));
   } else if (!seedmode && (seg || depth >= GROUPED_MIN_DEPTH)) {
     // grouped list maxima where rows admit many candidates: the many-set pass
     // (short per-set scans) and deep lists
