@@ -760,6 +760,47 @@ __device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, f
   }
 }
 
+// In the plain-rescan instances, candidates of the norm-folded epilogue wait
+// in a per-lane register stack of ADMIT_Q keys and are admitted after the
+// tile's last chunk, when the lanes of a warp drain their stacks together
+// (admissions in step, instead of one lane at a time per chunk); a full stack
+// drains at once.  The list ends with the same keys: list_admit re-tests each
+// key against the row's current threshold, and a top-`depth` set does not
+// depend on the order.  Measured: the 60k x 784 self graph's main pass 4.40 ->
+// 4.27 ms with a stack of 2 (4 or 8: slower).  The grouped-maxima instances
+// serve the many-set segmented pass, whose rows admit many candidates per
+// tile against a threshold that a stack leaves stale until the tile ends
+// (42.8 -> 54.7 ms), and admit at once.
+constexpr int ADMIT_Q = 2;
+// points per work item of the batched form's exact fallback scan
+constexpr int64_t FB_CHUNK = 4096;
+
+// v[j] for a lane-varying j in [0, 32): a five-level select tree on the bits of j
+__device__ __forceinline__ uint32_t select32(const uint32_t (&v)[32], int j) {
+  uint32_t t16[16], t8[8], t4[4];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) t16[i] = (j & 1) ? v[2 * i + 1] : v[2 * i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) t8[i] = (j & 2) ? t16[2 * i + 1] : t16[2 * i];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) t4[i] = (j & 4) ? t8[2 * i + 1] : t8[2 * i];
+  const uint32_t a = (j & 8) ? t4[1] : t4[0], b = (j & 8) ? t4[3] : t4[2];
+  return (j & 16) ? b : a;
+}
+
+template <bool GROUPED>
+__device__ __forceinline__ void admit_drain(uint64_t (&dq)[ADMIT_Q], int& dn, uint64_t* __restrict__ mylist,
+                                            uint64_t& thr_key, float& thr_est, int& lslot, int& nfill, int depth,
+                                            uint64_t (&gmax)[LGROUPS], int (&gidx)[LGROUPS]) {
+  while (dn > 0) {
+    const uint64_t c = dq[0];
+#pragma unroll
+    for (int i = 0; i + 1 < ADMIT_Q; ++i) dq[i] = dq[i + 1];
+    --dn;
+    list_admit<GROUPED>(mylist, c, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
+  }
+}
+
 // Norm-folded epilogue (BF16 form).  Every operand row carries, after its
 // main columns, a 24-column block [P0 P1 P2 1 1 1 0 0 | 1 1 1 P0 P1 P2 0 0 |
 // 0 ...] with P0 + P1 + P2 = -||x~||^2 / 2 exactly (three BF16 pieces of an
@@ -773,7 +814,7 @@ template <bool GROUPED>
 __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t* __restrict__ mylist,
                                                uint64_t& thr_key, float& thr_est, int& lslot, int& nfill,
                                                uint32_t col0, int depth, uint64_t (&gmax)[LGROUPS],
-                                               int (&gidx)[LGROUPS]) {
+                                               int (&gidx)[LGROUPS], uint64_t (&dq)[ADMIT_Q], int& dn) {
   if (nvalid < 32) {
 #pragma unroll
     for (int j = 0; j < 32; ++j)
@@ -795,11 +836,17 @@ __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, ui
     while (mask) {
       const int j = __ffs(mask) - 1;
       mask &= mask - 1;
-      uint32_t bits = v[0];
+      const uint64_t c = make_key(-2.0f * __uint_as_float(select32(v, j)), col0 + (uint32_t)j);
+      if constexpr (!GROUPED) {
+        if (!(c < thr_key)) continue;
+        if (dn == ADMIT_Q) admit_drain<GROUPED>(dq, dn, mylist, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
 #pragma unroll
-      for (int u = 1; u < 32; ++u) bits = j == u ? v[u] : bits;
-      const uint64_t c = make_key(-2.0f * __uint_as_float(bits), col0 + (uint32_t)j);
-      list_admit<GROUPED>(mylist, c, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
+        for (int i = ADMIT_Q - 1; i > 0; --i) dq[i] = dq[i - 1];
+        dq[0] = c;
+        ++dn;
+      } else {
+        list_admit<GROUPED>(mylist, c, thr_key, thr_est, lslot, nfill, depth, gmax, gidx);
+      }
     }
   }
 }
@@ -1034,6 +1081,8 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     uint64_t thr_key = KEY_NONE;
     float thr_est = INF;
     int lslot = 0, nfill = 0;
+    uint64_t dq[ADMIT_Q];  // candidates waiting for the end of the tile (dn of them)
+    int dn = 0;
     uint64_t gmax[LGROUPS];  // the list's group maxima and their slots (list_admit)
     int gidx[LGROUPS];
 #pragma unroll
@@ -1153,7 +1202,7 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             seed_chunk_fold(va, nva, top, (uint32_t)(col0 + ch * 32));
           else
             epi_chunk_fold<GROUPED>(va, nva, mylist, thr_key, thr_est, lslot, nfill, (uint32_t)(col0 + ch * 32),
-                           a.depth, gmax, gidx);
+                           a.depth, gmax, gidx, dq, dn);
         }
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
@@ -1182,10 +1231,13 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             seed_chunk_fold(vb, nvb, top, (uint32_t)(col0 + (ch + 1) * 32));
           else
             epi_chunk_fold<GROUPED>(vb, nvb, mylist, thr_key, thr_est, lslot, nfill,
-                           (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx);
+                           (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx, dq, dn);
         }
         ptx::tmem_ld_wait();
       }
+      // the tile's queued candidates, every lane of the warp at once
+      if constexpr (!FP8 && !GROUPED)
+        admit_drain<GROUPED>(dq, dn, mylist, thr_key, thr_est, lslot, nfill, a.depth, gmax, gidx);
     }
     if (alive && cur_run >= 0) flush(cur_q0, cur_qend, seg_slot);
   }
@@ -1704,13 +1756,16 @@ __global__ void k2_scatter_fallback(const uint64_t* __restrict__ keys, const int
   }
 }
 
-// Work items of the segmented fallback: row r = fb_rows[i] against the
-// points of the set holding it; the exact FP32 list goes straight to the
-// row's candidate slots (cand[r][0, LIST)).
-__global__ void fb_items_kernel(const int* __restrict__ fb_rows, const int* __restrict__ fb_count,
-                                const int64_t* __restrict__ offs, int nsets, SegItem* __restrict__ items) {
-  const int cnt = *fb_count;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+// Work items of the segmented fallback: item i * nsplit + c is row
+// r = fb_rows[i] against points [c * chunk, (c + 1) * chunk) of the set
+// holding it (empty past the set's end); its exact FP32 list goes to split
+// slot c of compact row i.
+__global__ void fb_items_kernel(const int* __restrict__ fb_rows, int cnt, const int64_t* __restrict__ offs,
+                                int nsets, int nsplit, int64_t chunk, SegItem* __restrict__ items) {
+  const int64_t total = (int64_t)cnt * nsplit;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / nsplit), c = (int)(t % nsplit);
     const int64_t r = fb_rows[i];
     int lo = 0, hi = nsets - 1;
     while (lo < hi) {  // last set whose offset <= r
@@ -1719,28 +1774,33 @@ __global__ void fb_items_kernel(const int* __restrict__ fb_rows, const int* __re
       else hi = mid - 1;
     }
     SegItem it{};
-    it.q0 = r;
-    it.qend = r + 1;
-    it.nb0 = offs[lo];
+    it.q0 = i;
+    it.qend = i + 1;
     it.nb1 = offs[lo + 1];
-    it.split = 0;
-    items[i] = it;
+    it.nb0 = min(it.nb1, offs[lo] + c * chunk);
+    it.nb1 = min(it.nb1, it.nb0 + chunk);
+    it.split = c;
+    items[t] = it;
   }
 }
 
-// Candidate counts and floors of the fallback rows (their lists are exact
-// FP32 top-LIST lists: the LIST-th distance bounds every other point).
-__global__ void fb_finish_kernel(const int* __restrict__ fb_rows, const int* __restrict__ fb_count,
-                                 const uint64_t* __restrict__ cand, int* __restrict__ cand_count,
+// The fallback rows' exact FP32 top-LIST lists (compact row i) go to their
+// candidate slots, with their counts and floors (the LIST-th distance bounds
+// every other point).
+__global__ void fb_finish_kernel(const int* __restrict__ fb_rows, int cnt, const uint64_t* __restrict__ keys,
+                                 uint64_t* __restrict__ cand, int* __restrict__ cand_count,
                                  float* __restrict__ floor_val) {
-  const int cnt = *fb_count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     const int64_t r = fb_rows[i];
-    const uint64_t* row = cand + r * LIST;
+    const uint64_t* src = keys + (int64_t)i * LIST;
+    uint64_t* row = cand + r * LIST;
     int c = 0;
-    while (c < LIST && row[c] != KEY_NONE) ++c;
+    for (int e = 0; e < LIST; ++e) {
+      row[e] = src[e];
+      c += src[e] != KEY_NONE ? 1 : 0;
+    }
     cand_count[r] = c;
-    floor_val[r] = (c == LIST) ? key_dist(row[LIST - 1]) : 3.0e38f;
+    floor_val[r] = (c == LIST) ? key_dist(src[LIST - 1]) : 3.0e38f;
   }
 }
 
@@ -1955,23 +2015,38 @@ __global__ void resolve_sort_kernel(int d, int metric, int64_t nq, int L, int kr
 //   at most u^2 S (4 + (n + 3.01)(n + 1)(1.001) + 10 (n + 8.1)); E doubles the
 //   leading terms, adds the double rounding of sh + sl and, for gradual
 //   underflow, 4 d 2^-149 per distance.
+__device__ __forceinline__ void hp_step(float a, float b, float& sh, float& sl) {
+  const float th = __fsub_rn(a, b);
+  const float bb = __fsub_rn(th, a);
+  const float tl = __fadd_rn(__fsub_rn(a, __fsub_rn(th, bb)), __fsub_rn(-b, bb));
+  const float p = __fmul_rn(th, th);
+  const float e = __fmaf_rn(th, th, -p);
+  const float cc = __fmaf_rn(__fmul_rn(2.0f, th), tl, e);
+  const float hi = fmaxf(sh, p), lo = fminf(sh, p);
+  const float s2 = __fadd_rn(hi, lo);
+  const float r = __fsub_rn(lo, __fsub_rn(s2, hi));
+  sh = s2;
+  sl = __fadd_rn(sl, __fadd_rn(r, cc));
+}
+
+// The loads of U strides are issued before their arithmetic (the lane's
+// dimensions are still added in order).
+template <int U>
 __device__ __forceinline__ void hp_sqdist(const float* __restrict__ qr, const float* __restrict__ pr, int d,
                                           int lane, double& V, double& E) {
   float sh = 0.0f, sl = 0.0f;
-  for (int c = lane; c < d; c += 32) {
-    const float a = __ldg(qr + c), b = __ldg(pr + c);
-    const float th = __fsub_rn(a, b);
-    const float bb = __fsub_rn(th, a);
-    const float tl = __fadd_rn(__fsub_rn(a, __fsub_rn(th, bb)), __fsub_rn(-b, bb));
-    const float p = __fmul_rn(th, th);
-    const float e = __fmaf_rn(th, th, -p);
-    const float cc = __fmaf_rn(__fmul_rn(2.0f, th), tl, e);
-    const float hi = fmaxf(sh, p), lo = fminf(sh, p);
-    const float s2 = __fadd_rn(hi, lo);
-    const float r = __fsub_rn(lo, __fsub_rn(s2, hi));
-    sh = s2;
-    sl = __fadd_rn(sl, __fadd_rn(r, cc));
+  int c = lane;
+  for (; c + 32 * (U - 1) < d; c += 32 * U) {
+    float a[U], b[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      a[u] = __ldg(qr + c + 32 * u);
+      b[u] = __ldg(pr + c + 32 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) hp_step(a[u], b[u], sh, sl);
   }
+  for (; c < d; c += 32) hp_step(__ldg(qr + c), __ldg(pr + c), sh, sl);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const float oh = __shfl_xor_sync(FULL, sh, o), ol = __shfl_xor_sync(FULL, sl, o);
@@ -2112,7 +2187,8 @@ __global__ void __launch_bounds__(128) resolve_l2_kernel(const float* __restrict
     const bool need = !clear || cl[p] != p || (p + 1 <= end && cl[p + 1] == p);
     if (!need) continue;  // warp-uniform
     double V, E;
-    hp_sqdist(qr, base + (int64_t)key_id(K[p]) * d, d, lane, V, E);
+    // (four positions side by side measured slower: 0.31 vs 0.22 ms per headline step)
+    hp_sqdist<8>(qr, base + (int64_t)key_id(K[p]) * d, d, lane, V, E);
     if (lane == 0) {
       Vv[p] = V;
       Ee[p] = E;
@@ -3157,20 +3233,39 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   k2_rerank<<<(unsigned)std::min<int64_t>(ceil_div(N, RR_WARPS), (int64_t)ctx->num_sms * 6), 32 * RR_WARPS, 0,
               s>>>(ra);
   MANN_CHECK_LAUNCH();
-  // ---- uncertified rows: exact FP32 scan of their own set, on the device
-  SegItem* fitems = nullptr;
+  // ---- uncertified rows: exact FP32 scan of their own set, on the device;
+  // each row's set is cut into FB_CHUNK-point items so that a few rows of the
+  // largest sets spread over the GPU (one item per row: 1.8 ms for 124 rows)
+  int h_fbc = 0;
+  MANN_CUDA_TRY(cudaMemcpyAsync(&h_fbc, P.fb_count, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MANN_CUDA_TRY(cudaStreamSynchronize(s));
   SegQueue* fq = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_FALLBACK_KEYS, (size_t)N, &fitems));
   MANN_TRY(ctx->scratch_t(SLOT_SEG_QUEUE, 1, &fq));
-  const int gfb = ctx->num_sms * 8;
-  fb_items_kernel<<<gfb, 256, 0, s>>>(fb_rows, P.fb_count, offs_dev, nsets, fitems);
-  MANN_CHECK_LAUNCH();
-  static unsigned fb_epoch = 0x40000000u;
-  const unsigned ep = ++fb_epoch;
-  MANN_TRY(launch_publish_queue(fq, 0, P.fb_count, ep, s));
-  MANN_TRY(launch_k1_persistent(ctx->num_sms, data, fitems, fq, ep, 1ll << 31, d, metric, 32, L, 1, cand, s));
-  fb_finish_kernel<<<gfb, 256, 0, s>>>(fb_rows, P.fb_count, cand, cand_count, floor_val);
-  MANN_CHECK_LAUNCH();
+  if (h_fbc > 0) {
+    int64_t max_set = 1;
+    for (int i = 0; i < nsets; ++i) max_set = std::max(max_set, offs_host[i + 1] - offs_host[i]);
+    int64_t chunk = std::max<int64_t>(FB_CHUNK, ceil_div(max_set, 128));  // the merge takes <= 128 lists
+    const int nsplit = (int)ceil_div(max_set, chunk);
+    const int64_t nitems = (int64_t)h_fbc * nsplit;
+    if (nitems > INT32_MAX) return fail(MANN_EINVAL_ARG, "batched graphs: too many fallback items");
+    SegItem* fitems = nullptr;
+    uint64_t* fpart = nullptr;
+    uint64_t* fkeys = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_FALLBACK_KEYS, (size_t)nitems, &fitems));
+    MANN_TRY(ctx->scratch_t(SLOT_PARTIAL, (size_t)nitems * L, &fpart));  // the main pass's slots are merged
+    MANN_TRY(ctx->scratch_t(SLOT_SEED_PARTIAL, (size_t)h_fbc * L, &fkeys));
+    const int gfb = ctx->num_sms * 8;
+    fb_items_kernel<<<gfb, 256, 0, s>>>(fb_rows, h_fbc, offs_dev, nsets, nsplit, chunk, fitems);
+    MANN_CHECK_LAUNCH();
+    static unsigned fb_epoch = 0x40000000u;
+    const unsigned ep = ++fb_epoch;
+    MANN_TRY(launch_publish_queue(fq, (int)nitems, nullptr, ep, s));
+    MANN_TRY(launch_k1_persistent(ctx->num_sms, data, fitems, fq, ep, 1ll << 31, d, metric, 32, L, nsplit,
+                                  nsplit > 1 ? fpart : fkeys, s, fb_rows));
+    if (nsplit > 1) MANN_TRY(launch_merge_lists(fpart, h_fbc, nsplit, L, fkeys, s));
+    fb_finish_kernel<<<gfb, 256, 0, s>>>(fb_rows, h_fbc, fkeys, cand, cand_count, floor_val);
+    MANN_CHECK_LAUNCH();
+  }
   // ---- truncate to kreq (ties at the k-th distance keep the FP32 (distance, id) order)
   uint64_t* keys = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_OUT_KEYS_BF16, (size_t)N * kreq, &keys));
@@ -3179,8 +3274,8 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   // ---- status, report, and the depth for the next call of this layout
   unsigned long long hc[64];
   MANN_CUDA_TRY(cudaMemcpyAsync(hc, P.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
-  int qstatus = 0;
-  MANN_CUDA_TRY(cudaMemcpyAsync(&qstatus, &fq->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int qstatus = 0;  // (the queue is published only when some row fell back)
+  if (h_fbc > 0) MANN_CUDA_TRY(cudaMemcpyAsync(&qstatus, &fq->status, sizeof(int), cudaMemcpyDeviceToHost, s));
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
   const int h_err = reinterpret_cast<const int*>(hc + 8)[0];
   const int h_fb = reinterpret_cast<const int*>(hc + 8)[1];
