@@ -772,6 +772,9 @@ __device__ __forceinline__ void seed_chunk(const uint32_t (&v)[32], float nbv, f
 // tile against a threshold that a stack leaves stale until the tile ends
 // (42.8 -> 54.7 ms), and admit at once.
 constexpr int ADMIT_Q = 2;
+// the epilogue takes each 16-column half-chunk's largest accumulator from the
+// max-reduction form of the TMEM load
+constexpr bool LD_RED = true;
 // points per work item of the batched form's exact fallback scan
 constexpr int64_t FB_CHUNK = 4096;
 
@@ -808,13 +811,12 @@ __device__ __forceinline__ void admit_drain(uint64_t (&dq)[ADMIT_Q], int& dn, ui
 // the point block eight columns later, so it adds -(||q~||^2 + ||p~||^2) / 2 and the accumulator
 // holds acc = q~.p~ - (||q~||^2 + ||p~||^2) / 2.  The estimate is then
 // est = -2 acc = ||q~ - p~||^2 (an exact scaling): the chunk's smallest est is
-// -2 max(acc), one FMNMX per value and no per-column norm.  Columns j >=
-// nvalid lie past the tile's last point (or in another point set).
-template <bool GROUPED>
-__device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t* __restrict__ mylist,
-                                               uint64_t& thr_key, float& thr_est, int& lslot, int& nfill,
-                                               uint32_t col0, int depth, uint64_t (&gmax)[LGROUPS],
-                                               int (&gidx)[LGROUPS], uint64_t (&dq)[ADMIT_Q], int& dn) {
+// -2 max(acc), with no per-column norm.  With LD_RED the TMEM load returns
+// that max (tcgen05.ld.red); a chunk with columns j >= nvalid (past the
+// tile's last point, or in another point set) masks them and takes the max
+// by a tree of FMNMX.
+__device__ __forceinline__ float chunk_max(uint32_t (&v)[32], int nvalid, float rmax) {
+  if (LD_RED && nvalid == 32) return rmax;
   if (nvalid < 32) {
 #pragma unroll
     for (int j = 0; j < 32; ++j)
@@ -825,9 +827,16 @@ __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, ui
   for (int j4 = 0; j4 < 8; ++j4)
     m4[j4] = fmaxf(fmaxf(__uint_as_float(v[4 * j4 + 0]), __uint_as_float(v[4 * j4 + 1])),
                    fmaxf(__uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3])));
-  const float mx = fmaxf(fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3])),
-                         fmaxf(fmaxf(m4[4], m4[5]), fmaxf(m4[6], m4[7])));
-  const float mn = -2.0f * mx;
+  return fmaxf(fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3])), fmaxf(fmaxf(m4[4], m4[5]), fmaxf(m4[6], m4[7])));
+}
+
+template <bool GROUPED>
+__device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, float rmax,
+                                               uint64_t* __restrict__ mylist, uint64_t& thr_key, float& thr_est,
+                                               int& lslot, int& nfill, uint32_t col0, int depth,
+                                               uint64_t (&gmax)[LGROUPS], int (&gidx)[LGROUPS],
+                                               uint64_t (&dq)[ADMIT_Q], int& dn) {
+  const float mn = -2.0f * chunk_max(v, nvalid, rmax);
   if (!__any_sync(FULL, mn < thr_est)) return;
   if (mn < thr_est) {
     unsigned mask = 0;
@@ -852,21 +861,9 @@ __device__ __forceinline__ void epi_chunk_fold(uint32_t (&v)[32], int nvalid, ui
 }
 
 // Seed-pass form of epi_chunk_fold (the chunk minimum of est = -2 max(acc)).
-__device__ __forceinline__ void seed_chunk_fold(uint32_t (&v)[32], int nvalid, uint64_t (&top)[SEED_DEPTH],
-                                                uint32_t col0) {
-  if (nvalid < 32) {
-#pragma unroll
-    for (int j = 0; j < 32; ++j)
-      if (j >= nvalid) v[j] = 0xFF800000u;
-  }
-  float m4[8];
-#pragma unroll
-  for (int j4 = 0; j4 < 8; ++j4)
-    m4[j4] = fmaxf(fmaxf(__uint_as_float(v[4 * j4 + 0]), __uint_as_float(v[4 * j4 + 1])),
-                   fmaxf(__uint_as_float(v[4 * j4 + 2]), __uint_as_float(v[4 * j4 + 3])));
-  const float mx = fmaxf(fmaxf(fmaxf(m4[0], m4[1]), fmaxf(m4[2], m4[3])),
-                         fmaxf(fmaxf(m4[4], m4[5]), fmaxf(m4[6], m4[7])));
-  uint64_t c = make_key(-2.0f * mx, col0);
+__device__ __forceinline__ void seed_chunk_fold(uint32_t (&v)[32], int nvalid, float rmax,
+                                                uint64_t (&top)[SEED_DEPTH], uint32_t col0) {
+  uint64_t c = make_key(-2.0f * chunk_max(v, nvalid, rmax), col0);
   if (c < top[SEED_DEPTH - 1]) {
     top[SEED_DEPTH - 1] = c;
 #pragma unroll
@@ -1181,14 +1178,22 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
       ptx::tc_fence_after();
       const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * BN);
       uint32_t va[32], vb[32];
-      ptx::tmem_ld16(taddr + cbeg * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
-      ptx::tmem_ld16(taddr + cbeg * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
+      float ma[2] = {0.0f, 0.0f}, mb[2] = {0.0f, 0.0f};  // the halves' largest values (LD_RED)
+      auto ld_chunk = [&](int ch_, uint32_t (&v_)[32], float (&m_)[2]) {
+        if constexpr (!FP8 && LD_RED) {
+          ptx::tmem_ld16_max(taddr + ch_ * 32, *reinterpret_cast<uint32_t(*)[16]>(&v_[0]), m_[0]);
+          ptx::tmem_ld16_max(taddr + ch_ * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v_[16]), m_[1]);
+        } else {
+          ptx::tmem_ld16(taddr + ch_ * 32, *reinterpret_cast<uint32_t(*)[16]>(&v_[0]));
+          ptx::tmem_ld16(taddr + ch_ * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&v_[16]));
+        }
+      };
+      ld_chunk(cbeg, va, ma);
       ptx::tmem_ld_wait();
 #pragma unroll 1
       for (int ch = cbeg; ch < cend; ch += 2) {
         // chunk ch is in va; fetch ch+1 into vb while va is processed, and so on
-        ptx::tmem_ld16(taddr + (ch + 1) * 32, *reinterpret_cast<uint32_t(*)[16]>(&vb[0]));
-        ptx::tmem_ld16(taddr + (ch + 1) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&vb[16]));
+        ld_chunk(ch + 1, vb, mb);
         if constexpr (FP8) {
           const float cs_a = pick(csc, ch);
           if (a.seedmode)
@@ -1199,15 +1204,14 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         } else {
           const int nva = (int)min((int64_t)32, v.cend - (col0 + ch * 32));
           if (a.seedmode)
-            seed_chunk_fold(va, nva, top, (uint32_t)(col0 + ch * 32));
+            seed_chunk_fold(va, nva, fmaxf(ma[0], ma[1]), top, (uint32_t)(col0 + ch * 32));
           else
-            epi_chunk_fold<GROUPED>(va, nva, mylist, thr_key, thr_est, lslot, nfill, (uint32_t)(col0 + ch * 32),
-                           a.depth, gmax, gidx, dq, dn);
+            epi_chunk_fold<GROUPED>(va, nva, fmaxf(ma[0], ma[1]), mylist, thr_key, thr_est, lslot, nfill,
+                                    (uint32_t)(col0 + ch * 32), a.depth, gmax, gidx, dq, dn);
         }
         ptx::tmem_ld_wait();
         if (ch + 2 < cend) {
-          ptx::tmem_ld16(taddr + (ch + 2) * 32, *reinterpret_cast<uint32_t(*)[16]>(&va[0]));
-          ptx::tmem_ld16(taddr + (ch + 2) * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&va[16]));
+          ld_chunk(ch + 2, va, ma);
         } else {
           // every TMEM read of this tile is done: hand the buffer back before the last chunk
           ptx::tc_fence_before();
@@ -1228,10 +1232,10 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
         } else {
           const int nvb = (int)min((int64_t)32, v.cend - (col0 + (ch + 1) * 32));
           if (a.seedmode)
-            seed_chunk_fold(vb, nvb, top, (uint32_t)(col0 + (ch + 1) * 32));
+            seed_chunk_fold(vb, nvb, fmaxf(mb[0], mb[1]), top, (uint32_t)(col0 + (ch + 1) * 32));
           else
-            epi_chunk_fold<GROUPED>(vb, nvb, mylist, thr_key, thr_est, lslot, nfill,
-                           (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx, dq, dn);
+            epi_chunk_fold<GROUPED>(vb, nvb, fmaxf(mb[0], mb[1]), mylist, thr_key, thr_est, lslot, nfill,
+                                    (uint32_t)(col0 + (ch + 1) * 32), a.depth, gmax, gidx, dq, dn);
         }
         ptx::tmem_ld_wait();
       }

@@ -250,6 +250,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
       : "memory");
 }
 
+// tmem_ld16 that also returns the largest of the thread's 16 values (the
+// max-reduction form of tcgen05.ld of sm_103a; NaN elements take no part
+// unless every one is NaN, as with fmaxf).  Valid after tmem_ld_wait().
+__device__ __forceinline__ void tmem_ld16_max(uint32_t taddr, uint32_t (&r)[16], float& mx) {
+  float f[16];
+  asm volatile(
+      "tcgen05.ld.red.sync.aligned.32x32b.x16.max.f32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, %16, [%17];"
+      : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]),
+        "=f"(f[7]), "=f"(f[8]), "=f"(f[9]), "=f"(f[10]), "=f"(f[11]), "=f"(f[12]), "=f"(f[13]),
+        "=f"(f[14]), "=f"(f[15]), "=f"(mx)
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) r[i] = __float_as_uint(f[i]);
+}
+
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
