@@ -47,6 +47,11 @@ typedef int32_t mann_status;
                             top-(k+m), exact FP32 rerank (never chosen by AUTO: its certified
                             window is far wider than BF16's on the measured sets) */
 #define MANN_PREC_AUTO 3 /* library picks (BF16 form when d >= 128 and the metric is L2) */
+#define MANN_PREC_FP16 4 /* FP16 tcgen05 tiles: rows centred and scaled by a power of two into
+                            FP16's range (operand rounding 2^-11, one product per term at the
+                            16-bit tensor rate, where data that BF16 cannot hold exactly needs
+                            the three-product BF16 split), the norm fold as one BF16 step,
+                            certified top-(k+m), exact FP32 rerank */
 
 /* Flags */
 #define MANN_FLAG_FP64_TIES 1u   /* order near-ties at the k-th boundary by FP64 distances */

@@ -28,6 +28,7 @@ PREC_FP32 = 0
 PREC_BF16 = 1
 PREC_FP8 = 2
 PREC_AUTO = 3
+PREC_FP16 = 4
 
 FLAG_FP64_TIES = 1
 FLAG_TIME_KERNEL = 2

@@ -20,7 +20,7 @@ mann_status check_common(const mann_knn_params* p, int64_t n, int32_t d) {
   if (n > 0x7FFFFFFFll) return fail(MANN_EINVAL_ARG, "at most 2^31-1 points (int32 ids)");
   if (!valid_metric(p->metric)) return fail(MANN_EINVAL_ARG, "unknown metric code");
   if (p->precision != MANN_PREC_FP32 && p->precision != MANN_PREC_BF16 && p->precision != MANN_PREC_FP8 &&
-      p->precision != MANN_PREC_AUTO)
+      p->precision != MANN_PREC_AUTO && p->precision != MANN_PREC_FP16)
     return fail(MANN_EINVAL_ARG, "unknown precision code");
   return MANN_OK;
 }
@@ -70,9 +70,10 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
     return fail(MANN_EINVAL_ARG, "k = " + std::to_string(kreq) + " exceeds the fused top-k limit " +
                                      std::to_string(KMAX_FUSED));
   bool use_bf16 = false;
-  const bool fp8 = p->precision == MANN_PREC_FP8;
-  if (p->precision == MANN_PREC_BF16 || fp8) {
-    if (kreq > 24) return fail(MANN_EINVAL_ARG, "the BF16 and FP8 forms support k <= 24 (k+1 for graphs)");
+  const int form = p->precision == MANN_PREC_FP8 ? FORM_FP8 : (p->precision == MANN_PREC_FP16 ? FORM_FP16 : FORM_BF16);
+  if (p->precision == MANN_PREC_BF16 || form != FORM_BF16) {
+    if (kreq > 24)
+      return fail(MANN_EINVAL_ARG, "the BF16, FP16 and FP8 forms support k <= 24 (k+1 for graphs)");
     use_bf16 = true;
   } else if (p->precision == MANN_PREC_AUTO) {
     use_bf16 = kreq <= 24 && d >= 128 && n >= 4096;
@@ -95,7 +96,7 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
   uint64_t* keys = nullptr;
   if (use_bf16) {
     MANN_TRY(knn_bf16_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, p->margin,
-                           (p->flags & MANN_FLAG_FP64_TIES) != 0, &keys, rep, fp8));
+                           (p->flags & MANN_FLAG_FP64_TIES) != 0, &keys, rep, form));
     if (rep) rep->rows = nq;
   } else if (p->flags & MANN_FLAG_FP64_TIES) {
     // FP32 scan with a few extra entries, then FP64 order for near-ties

@@ -253,14 +253,15 @@ mann_status knn_graph_batched_device(Context* ctx, cudaStream_t s, const mann_kn
     return fail(MANN_EINVAL_ARG, "batched graphs: Euclidean or SqEuclidean");
   const int k = p->k;
   Shape sh{data, offs[nsets], nsets, d, p->metric, k, include_self ? k : k + 1, include_self ? 1 : 0, ids, dists};
-  if (p->precision == MANN_PREC_BF16) {
-    // the BF16 tensor-core form: one segmented pass over every set's (block, tile) items
+  if (p->precision == MANN_PREC_BF16 || p->precision == MANN_PREC_FP16) {
+    // the tensor-core form: one segmented pass over every set's (block, tile) items
     int64_t* offs_dev = nullptr;
     MANN_TRY(ctx->scratch_t(SLOT_BATCH_OFFS, (size_t)nsets + 1, &offs_dev));
     MANN_CUDA_TRY(cudaMemcpyAsync(offs_dev, offs, sizeof(int64_t) * (nsets + 1), cudaMemcpyHostToDevice, s));
     uint64_t* keys = nullptr;
     ctx->time_begin(s);
-    MANN_TRY(knn_bf16_batched_keys(ctx, s, data, offs, offs_dev, nsets, d, p->metric, sh.kk, p->margin, &keys, rep));
+    MANN_TRY(knn_bf16_batched_keys(ctx, s, data, offs, offs_dev, nsets, d, p->metric, sh.kk, p->margin, &keys, rep,
+                                   p->precision == MANN_PREC_FP16 ? FORM_FP16 : FORM_BF16));
     ctx->time_end(s);
     MANN_TRY(launch_finish(keys, sh.N, sh.kk, k, include_self ? -1 : 0, nullptr, ids, dists, s));
     localize_ids_kernel<<<(unsigned)ceil_div(sh.N, 256), 256, 0, s>>>(ids, sh.N, k, offs_dev, nsets);
@@ -365,7 +366,8 @@ mann_status mann_knn_graph_batched_device(const mann_knn_params* p, const float*
                                     report));
   if (report) {
     report->rows = set_offsets[nsets];
-    report->precision_used = p->precision == MANN_PREC_BF16 ? MANN_PREC_BF16 : MANN_PREC_FP32;
+    report->precision_used =
+        (p->precision == MANN_PREC_BF16 || p->precision == MANN_PREC_FP16) ? p->precision : MANN_PREC_FP32;
     report->launches = launch_count() - l0;
     report->kernel_ms = -1;
     if (ctx->timing && ctx->timed) {
@@ -402,7 +404,8 @@ mann_status mann_knn_graph_batched(const mann_knn_params* p, const float* data, 
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
   if (report) {
     report->rows = N;
-    report->precision_used = p->precision == MANN_PREC_BF16 ? MANN_PREC_BF16 : MANN_PREC_FP32;
+    report->precision_used =
+        (p->precision == MANN_PREC_BF16 || p->precision == MANN_PREC_FP16) ? p->precision : MANN_PREC_FP32;
     report->launches = launch_count() - l0;
     report->kernel_ms = -1;
   }

@@ -27,19 +27,23 @@ mann_status knn_fp32_keys(Context* ctx, cudaStream_t s, const float* base, int64
 mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, int64_t graph_self,
                           const int32_t* rows, int32_t* ids, float* dists, cudaStream_t s);
 
-// BF16 tensor-core form (SqEuclidean / Euclidean): certified candidates,
+// Operand forms of the tensor-core search: BF16 rows (the three-product split
+// when BF16 cannot hold the data), E4M3 rows with per-row power-of-two scales
+// (kind::f8f6f4), FP16 rows scaled by one power of two into FP16's range.
+enum : int { FORM_BF16 = 0, FORM_FP8 = 1, FORM_FP16 = 2 };
+
+// Tensor-core form (SqEuclidean / Euclidean / cosine): certified candidates,
 // exact FP32 rerank, optional FP64 near-tie order.  Result: keys [nq][kreq].
-// fp8: the same search with E4M3 tiles (per-row power-of-two scales, kind::f8f6f4).
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
-                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, bool fp8 = false);
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, int form = FORM_BF16);
 
 // Self-kNN keys [N][kreq] (global ids, the row itself included) of many point
 // sets stored back to back (set c = rows [offs[c], offs[c+1])), each against
 // its own points, in the BF16 form (offs on the host and on the device).
 mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* data, const int64_t* offs_host,
                                   const int64_t* offs_dev, int nsets, int d, int metric, int kreq, int margin,
-                                  uint64_t** out_keys, mann_knn_report* rep);
+                                  uint64_t** out_keys, mann_knn_report* rep, int form = FORM_BF16);
 
 // Orders near-ties of sorted FP32 candidate lists as the FP64 oracle does
 // (when fp64) and truncates them to kreq keys.  counters[0] += rows with a

@@ -35,6 +35,7 @@
 //   Rs = R_q + max R_p.  A slack of 3 (d+2) u U keeps every point that could
 //   enter the FP32 top-k or tie with its k-th FP32 distance.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_fp8.h>
 
 #include <algorithm>
@@ -145,7 +146,9 @@ __device__ __forceinline__ void scale_candidate(int i, float m, float* sc, float
   else { *sc = 1.0f; *mc = rintf(m); }
 }
 
-// per candidate: sum over sampled rows of ||cv - bf16(cv)||^2 / ||cv||^2
+// per candidate: sum over sampled rows of ||cv - bf16(cv)||^2 / ||cv||^2; the
+// first candidate also records the sampled max |x - mu| (float bits, integer
+// max) in score[NUM_SCALES] for the FP16 form's scale
 __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d,
                                    const float* __restrict__ mu, int64_t stride,
                                    double* __restrict__ score) {
@@ -153,7 +156,7 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
   const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * stride;
   const int cand = blockIdx.y;
   if (row >= n) return;
-  float rr = 0.0f, cc = 0.0f;  // a heuristic score: FP32 is plenty
+  float rr = 0.0f, cc = 0.0f, mx = 0.0f;  // a heuristic score: FP32 is plenty
   for (int c = lane; c < d; c += 32) {
     float sc, mc;
     scale_candidate(cand, mu[c], &sc, &mc);
@@ -161,21 +164,34 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
     const float bv = __bfloat162float(__float2bfloat16_rn(cv));
     rr = __fmaf_rn(cv - bv, cv - bv, rr);
     cc = __fmaf_rn(cv, cv, cc);
+    mx = fmaxf(mx, fabsf(cv));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     rr += __shfl_xor_sync(FULL, rr, o);
     cc += __shfl_xor_sync(FULL, cc, o);
+    mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
   }
-  if (lane == 0) atomicAdd(&score[cand], cc > 0.0f ? (double)rr / (double)cc : 0.0);
+  if (lane == 0) {
+    atomicAdd(&score[cand], cc > 0.0f ? (double)rr / (double)cc : 0.0);
+    if (cand == 0 && mx < 3.0e38f) atomicMax(reinterpret_cast<unsigned*>(&score[NUM_SCALES]), __float_as_uint(mx));
+  }
 }
 
 // pick the candidate with the smallest residual (moving off the plain mean
 // only for a clear win), replace mu by its centre and publish its scale
 __global__ void choose_scale_kernel(const double* __restrict__ score, float* __restrict__ mu, int d,
-                                    float* __restrict__ scale_out, int* __restrict__ inexact, int64_t nrows) {
+                                    float* __restrict__ scale_out, int* __restrict__ inexact, int64_t nrows,
+                                    float* __restrict__ f16_scale_out) {
   __shared__ int best;
   if (threadIdx.x == 0) {
+    // FP16 form: the power of two that takes the sampled max |x - mu| into
+    // [2^11, 2^12) -- 16x below FP16's largest value for rows off the sample
+    // (a value that still overflows saturates, and its row's bound says so)
+    const float smax = __uint_as_float(*reinterpret_cast<const unsigned*>(&score[NUM_SCALES]));
+    int e = 0;
+    if (smax > 0.0f) frexpf(smax, &e);  // smax in [2^(e-1), 2^e)
+    *f16_scale_out = ldexpf(1.0f, max(-120, min(120, 12 - e)));
     int b = 0;
     for (int i = 1; i < NUM_SCALES; ++i)
       if (score[i] < 0.25 * score[b]) b = i;
@@ -196,6 +212,10 @@ __global__ void choose_scale_kernel(const double* __restrict__ score, float* __r
 }
 
 // One warp per row: BF16 copy of scale*(x - mu) padded to dp, and the row's bound terms.
+// FP16 form (f16 = 1): the main columns are FP16 instead (values beyond FP16's
+// largest finite value saturate, and the row's residual bound becomes +inf,
+// so its certificate fails and the exact scan answers it); the fold block
+// stays BF16 (its K-step is a BF16 MMA of its own).
 // Split form (split = 1): x~ = hi + lo with hi = bf16(cv), lo = bf16(cv - hi),
 // written as three dp-wide segments -- [hi | hi | lo] for query rows (role 0),
 // [hi | lo | hi] for point rows (role 1) -- so one MMA over 3dp columns gives
@@ -207,7 +227,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
                                     const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
                                     float* __restrict__ norms, BaseMax* __restrict__ bmax, int split,
-                                    int role) {
+                                    int role, int f16) {
   const int lane = threadIdx.x & 31;
   const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -221,6 +241,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
   // certificate adds to its bound (norm_rel_err)
   float f_b = 0.0f, f_r = 0.0f, f_c = 0.0f, f_l = 0.0f;
+  bool sat = false;  // FP16 form: a value saturated (or was not a number)
   constexpr int PF = 8;  // loads in flight per lane (the kernel is latency-bound otherwise)
   for (int c0 = lane; valid && c0 < dp; c0 += 32 * PF) {
     float xv[PF], mv[PF];
@@ -236,8 +257,16 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     if (c >= dp) break;
     float cv = 0.0f;
     if (c < d) cv = __fmul_rn(scale, __fsub_rn(xv[u], mv[u]));
+    float bv;
+    if (f16) {
+      const float cl = fminf(fmaxf(cv, -65504.0f), 65504.0f);
+      const __half h = __float2half_rn(cl);
+      bv = __half2float(h);
+      sat |= !(cl == cv);
+      reinterpret_cast<__half*>(br)[c] = h;
+    } else {
     const __nv_bfloat16 b = __float2bfloat16_rn(cv);
-    float bv = __bfloat162float(b);
+    bv = __bfloat162float(b);
     if (split) {
       // cv - hi is exact in FP32; hi + lo spans at most 17 bits, also exact
       const __nv_bfloat16 lb = __float2bfloat16_rn(cv - bv);
@@ -250,12 +279,14 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     } else {
       br[c] = b;
     }
+    }
     const float rv = cv - bv;  // exact: the rounding residual of a float fits in a float
     f_b = __fmaf_rn(bv, bv, f_b);
     f_r = __fmaf_rn(rv, rv, f_r);
     f_c = __fmaf_rn(cv, cv, f_c);
     }
   }
+  const bool any_sat = __any_sync(FULL, sat);
   // cross-lane sums in FP32 (a 5-level tree of nonnegative terms adds at most
   // 5u of relative error; FP64 arithmetic is slow on this part)
 #pragma unroll
@@ -296,6 +327,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     ri.r_up = __fadd_ru(__fsqrt_ru(__fmul_ru(f_r, onep)),
                         __fmul_ru(__fmul_ru(1.1920928955078125e-07f, 1.0000002f), __fsqrt_ru(__fmul_ru(f_c, onep))));
     ri.lo_up = split ? __fsqrt_ru(__fmul_ru(f_l, onep)) : 0.0f;
+    if (any_sat) ri.r_up = __int_as_float(0x7F800000);
     info[row] = ri;
     if (norms) norms[row] = ri.nrm;
     if (bmax) {  // one global atomic per block and field, not per row
@@ -474,6 +506,7 @@ struct MainArgs {
   uint64_t* partial;  // [nq][smax][L]
   int* err;
   int seedmode;       // keep the SEED_DEPTH smallest 32-column chunk minima instead of points
+  int f16;            // FP16 main columns: their MMAs read FP16 (the fold step stays BF16)
 };
 
 // What one item means for the kernel's roles: rows [q0, qend), points
@@ -775,6 +808,10 @@ constexpr int ADMIT_Q = 2;
 // the epilogue takes each 16-column half-chunk's largest accumulator from the
 // max-reduction form of the TMEM load
 constexpr bool LD_RED = true;
+// single-matrix passes of at most this many K-stages per tile run the
+// three-stage, two-set instance (their MMA per tile is short against the
+// epilogue's work)
+constexpr int SHORT_K_STAGES = 3;
 // points per work item of the batched form's exact fallback scan
 constexpr int64_t FB_CHUNK = 4096;
 
@@ -885,7 +922,8 @@ __host__ __device__ constexpr size_t k2_smem_bytes(int cap, int nsets, int stage
 }
 static_assert(k2_smem_bytes<false>(32, 1) <= 232448 && k2_smem_bytes<false>(16, 2) <= 232448, "k2_main shared memory");
 static_assert(k2_smem_bytes<true>(32, 1) <= 232448 && k2_smem_bytes<true>(16, 2) <= 232448, "k2_main shared memory");
-static_assert(k2_smem_bytes<false>(24, 2, 3) <= 232448, "k2_main shared memory");
+static_assert(k2_smem_bytes<false>(24, 2, 3) <= 232448 && k2_smem_bytes<false>(32, 2, 3) <= 232448,
+              "k2_main shared memory");
 
 // The list keys are (est', id) with est' = ||p~||^2 - 2 q~.p~ (the row's own
 // ||q~||^2 is left out: it does not change the row's order).  A point is
@@ -1004,6 +1042,9 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0 && rank == 0) {
       constexpr uint32_t idesc = FP8 ? ptx::idesc_e4m3_f32(QROWS, BN) : ptx::idesc_bf16_f32(QROWS, BN);
+      // the main K-steps' operand type: FP16 in the FP16 form (both operands, as
+      // every kind::f16 MMA needs), else the form's own; the fold step is BF16
+      const uint32_t idesc_main = (!FP8 && a.f16) ? ptx::idesc_f16_f32(QROWS, BN) : idesc;
       uint32_t it = 0;
       int tcount = 0;
       bool ok = true;
@@ -1031,11 +1072,11 @@ __global__ void __launch_bounds__(64 + 128 * NSETS, 1)
             const uint64_t ad = ptx::sw128_desc(sa + kk * 32);
             const uint64_t bd = ptx::sw128_desc(sb + kk * 32);
             if (PAIR)
-              ptx::mma_f16_pair(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+              ptx::mma_f16_pair(dcol, ad, bd, idesc_main, (kb > 0 || kk > 0) ? 1u : 0u);
             else if (FP8)
               ptx::mma_f8(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
             else
-              ptx::mma_f16(dcol, ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+              ptx::mma_f16(dcol, ad, bd, idesc_main, (kb > 0 || kk > 0) ? 1u : 0u);
           }
           if (!FP8 && a.augx > 0 && kb == a.augx / EPS) {
             // the norm-fold K-step: the query block at its first column, the
@@ -2563,13 +2604,16 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
                           const RowInfo* qinfo, const RowInfo* binfo, const float* bnorm, int64_t n, int64_t nq,
                           int d, int dp, int mainw, int augx, int depth, const float* seed, int* err, int slot_partial, int slot_lists,
                           bool timed, uint64_t** lists_out, int seedmode = 0, const SegPass* seg = nullptr,
-                          const float* qscale = nullptr, const float* bscale = nullptr) {
+                          const float* qscale = nullptr, const float* bscale = nullptr, int f16 = 0) {
   const bool fp8 = qscale != nullptr;
   const int nkb = (int)(augx > 0 ? ceil_div(augx + AUG, BK) : ceil_div(mainw, fp8 ? 128 : BK));
-  // the many-set pass with at most three K-stages per tile (small d): three
-  // pipeline stages leave shared memory for two epilogue sets of 24-entry
-  // lists, so eight warps admit candidates instead of four
-  const bool seg3 = seg && !seedmode && !fp8 && depth > 16 && depth <= 24 && nkb <= 3;
+  // passes with few K-stages per tile (the many-set pass at small d, FP16
+  // rows of moderate d): three pipeline stages leave shared memory for two
+  // epilogue sets of 24- or 32-entry lists, so eight warps admit candidates
+  // instead of four
+  const bool seg3 = !seedmode && !fp8 && depth > 16 &&
+                    ((seg && depth <= 24 && nkb <= 3) || (!seg && nkb <= SHORT_K_STAGES));
+  const int cap3 = depth <= 24 ? 24 : 32;
   // two epilogue sets with 16-entry lists when the depth allows it; each set
   // writes its own slot
   const int nsets = (depth <= 16 || seg3) ? 2 : 1;
@@ -2650,8 +2694,9 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   ma.partial = partial;
   ma.err = err;
   ma.seedmode = seedmode;
+  ma.f16 = f16;
   const size_t smem = pair   ? k2_smem_bytes<true>(nsets == 2 ? 16 : 32, nsets)
-                     : seg3 ? k2_smem_bytes<false>(24, 2, 3)
+                     : seg3 ? k2_smem_bytes<false>(cap3, 2, 3)
                             : k2_smem_bytes<false>(nsets == 2 ? 16 : 32, nsets);
   if (smem > ctx->smem_optin) return fail(MANN_ECUDA, "shared memory budget exceeded");
   if (timed) ctx->time_begin(s);
@@ -2666,7 +2711,10 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
     else
       MANN_TRY((launch_k2<32, 1, false, true>(mapA, mapB, ma, w.grid, smem, s)));
   } else if (seg3) {
-    MANN_TRY((launch_k2<24, 2, false, false, true, 3>(mapA, mapB, ma, w.grid, smem, s)));
+    if (cap3 == 24)
+      MANN_TRY((launch_k2<24, 2, false, false, true, 3>(mapA, mapB, ma, w.grid, smem, s)));
+    else
+      MANN_TRY((launch_k2<32, 2, false, false, true, 3>(mapA, mapB, ma, w.grid, smem, s)));
   } else if (!seedmode && (seg || depth >= GROUPED_MIN_DEPTH)) {
     // grouped list maxima where rows admit many candidates: the many-set pass
     // (short per-set scans) and deep lists
@@ -2717,6 +2765,7 @@ struct Bf16Operand {
 struct Bf16Prep {
   Bf16Operand B, Q;
   int split = 0, dp = 0, dpe = 0;
+  int f16 = 0;    // FP16 main columns (the FP16 form)
   int width = 0;  // operand row length: mainw + AUG (BF16), dp (FP8)
   int mainw = 0;  // main columns: dpe zero-padded to a multiple of 16 (BF16), dp (FP8)
   int augx = 0;   // first augmented column (BF16: mainw), 0 without the norm fold
@@ -2729,8 +2778,9 @@ struct Bf16Prep {
 };
 
 mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_t n, const float* qs, int64_t nq,
-                         int d, int metric, Bf16Prep* P, bool fp8 = false) {
-  // operand rows: 16-byte multiples (8 BF16 or 16 E4M3 values)
+                         int d, int metric, Bf16Prep* P, int form = FORM_BF16) {
+  const bool fp8 = form == FORM_FP8, f16 = form == FORM_FP16;
+  // operand rows: 16-byte multiples (8 BF16 / FP16 or 16 E4M3 values)
   const int dp = fp8 ? (d + 15) & ~15 : (d + 7) & ~7;
   const bool self = (qs == base);
   const bool cosine = metric == MANN_METRIC_COSINE;
@@ -2775,7 +2825,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   }
   // pick the centre / scale with the smallest BF16 residual on a row sample
   double* score = cpart;  // probe scores
-  MANN_CUDA_TRY(cudaMemsetAsync(score, 0, NUM_SCALES * sizeof(double), s));
+  MANN_CUDA_TRY(cudaMemsetAsync(score, 0, (NUM_SCALES + 1) * sizeof(double), s));  // scores | sampled max
   const int64_t sample_rows = std::min<int64_t>(n, 1024);
   const int64_t stride = std::max<int64_t>(1, n / sample_rows);
   dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
@@ -2783,7 +2833,8 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   MANN_CHECK_LAUNCH();
   float* scale = reinterpret_cast<float*>(bmax + 1);
   int* inexact = reinterpret_cast<int*>(scale + 1);
-  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale, inexact, ceil_div(n, stride));
+  float* f16_scale = reinterpret_cast<float*>(inexact + 1);
+  choose_scale_kernel<<<1, 128, 0, s>>>(score, mu, d, scale, inexact, ceil_div(n, stride), f16_scale);
   MANN_CHECK_LAUNCH();
   MANN_CUDA_TRY(cudaMemsetAsync(bmax, 0, sizeof(BaseMax), s));
   // Data that BF16 cannot hold exactly (after the best centre and scale) runs
@@ -2792,7 +2843,8 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   int h_inexact = 0;
   MANN_CUDA_TRY(cudaMemcpyAsync(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost, s));
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
-  const int split = (h_inexact && !fp8) ? 1 : 0;  // the FP8 form has no split
+  const int split = (h_inexact && form == FORM_BF16) ? 1 : 0;  // the FP8 and FP16 forms have no split
+  if (f16) scale = f16_scale;  // the conversion and the certificate use the FP16 form's scale
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
   Bf16Operand B, Q;
   if (fp8) {
@@ -2832,7 +2884,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
   MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
   convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, augx, width, mu, scale, B.xb,
-                                                              B.info, B.norms, bmax, split, 1);
+                                                              B.info, B.norms, bmax, split, 1, f16 ? 1 : 0);
   MANN_CHECK_LAUNCH();
   if (self && !split) {
     Q = B;
@@ -2840,7 +2892,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
     MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * width, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
     convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, augx, width, mu, scale, Q.xb,
-                                                                  Q.info, nullptr, nullptr, split, 0);
+                                                                  Q.info, nullptr, nullptr, split, 0, f16 ? 1 : 0);
     MANN_CHECK_LAUNCH();
   }
   P->width = width;
@@ -2853,6 +2905,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   P->B = B;
   P->Q = Q;
   P->split = split;
+  P->f16 = f16 ? 1 : 0;
   P->dp = dp;
   P->dpe = dpe;
   P->scale = scale;
@@ -2886,21 +2939,22 @@ int tuned_depth(const unsigned long long* hist, int kreq) {
 
 mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64_t n,
                           const float* qs, int64_t nq, int d, int metric, int kreq, int margin,
-                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, bool fp8) {
+                          bool fp64, uint64_t** out_keys, mann_knn_report* rep, int form) {
   if (nq <= 0) return MANN_OK;
   const int L = LIST;
+  const bool fp8 = form == FORM_FP8;
   // admission depth = k + margin.  margin > 0: as given.  margin == 0: the
   // autotuner's choice for this shape class -- the full list on first sight,
   // then the depth 99.9% of rows needed plus one (refreshed after every call).
   const uint64_t tkey = ((uint64_t)kreq << 56) ^ ((uint64_t)d << 36) ^ ((uint64_t)metric << 32) ^
-                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63) ^ ((uint64_t)fp8 << 61);
+                        (uint64_t)(n >> 10) ^ ((uint64_t)(qs == base) << 63) ^ ((uint64_t)form << 60);
   int depth = L;
   if (kreq > KREQ_MAX_BF16)
     return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
                                      " (k+1 for graphs)");
   const bool cosine = metric == MANN_METRIC_COSINE;
   Bf16Prep P;
-  MANN_TRY(bf16_prepare(ctx, s, base, n, qs, nq, d, metric, &P, fp8));
+  MANN_TRY(bf16_prepare(ctx, s, base, n, qs, nq, d, metric, &P, form));
   const int split = P.split, dpe = P.dpe;
   if (margin > 0) {
     depth = std::min(L, kreq + margin);
@@ -2931,7 +2985,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
     uint64_t* slists = nullptr;
     MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, bstride, Q.info, B.info, B.norms, SEED_SAMPLE, nq, d, P.width, P.mainw, P.augx,
                            SEED_DEPTH, nullptr, err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists, 1,
-                           nullptr, Q.rscale, B.rscale));
+                           nullptr, Q.rscale, B.rscale, P.f16));
     MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)nq, &seed));
     seed_from_lists_kernel<<<(unsigned)ceil_div(nq, 256), 256, 0, s>>>(slists, nq, SEED_DEPTH - 1, seed);
     MANN_CHECK_LAUNCH();
@@ -2940,7 +2994,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   // ---- main pass over every point
   uint64_t* lists = nullptr;
   MANN_TRY(run_main_pass(ctx, s, mapA, B.xb, 1, Q.info, B.info, B.norms, n, nq, d, P.width, P.mainw, P.augx, depth, seed, err,
-                         SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, nullptr, Q.rscale, B.rscale));
+                         SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, nullptr, Q.rscale, B.rscale, P.f16));
 
   // ---- certify + rerank
   uint64_t* cand = nullptr;
@@ -3032,7 +3086,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
       rep->rows_fp64_ties = (int64_t)h[4];
       rep->rows_ties_widened = fp64 ? (int64_t)h[5] : 0;
       rep->rows_unresolved = left;
-      rep->precision_used = fp8 ? MANN_PREC_FP8 : MANN_PREC_BF16;
+      rep->precision_used = fp8 ? MANN_PREC_FP8 : (P.f16 ? MANN_PREC_FP16 : MANN_PREC_BF16);
       rep->margin_used = depth - kreq;
     }
   }
@@ -3118,7 +3172,7 @@ void build_seg_tables(const int64_t* offs, int nsets, SegTables* T) {
 // Result: keys [N][kreq] with global ids (the row itself included).
 mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* data, const int64_t* offs_host,
                                   const int64_t* offs_dev, int nsets, int d, int metric, int kreq, int margin,
-                                  uint64_t** out_keys, mann_knn_report* rep) {
+                                  uint64_t** out_keys, mann_knn_report* rep, int form) {
   const int L = LIST;
   if (kreq > KREQ_MAX_BF16)
     return fail(MANN_EINVAL_ARG, "the BF16 form supports k <= " + std::to_string(KREQ_MAX_BF16) +
@@ -3154,10 +3208,10 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
     T.uploaded_hash = T.hash;
   }
   Bf16Prep P;
-  MANN_TRY(bf16_prepare(ctx, s, data, N, data, N, d, metric, &P));
+  MANN_TRY(bf16_prepare(ctx, s, data, N, data, N, d, metric, &P, form));
   // the admission depth (k-margin): tuned per (layout, k, d, metric, form)
   const uint64_t tkey = 0x5E6B000000000000ull ^ (T.hash >> 8) ^ ((uint64_t)kreq << 40) ^ ((uint64_t)d << 24) ^
-                        ((uint64_t)metric << 20) ^ ((uint64_t)P.split << 19);
+                        ((uint64_t)metric << 20) ^ ((uint64_t)P.split << 19) ^ ((uint64_t)P.f16 << 18);
   int depth = L;
   if (margin > 0) {
     depth = std::min(L, kreq + margin);
@@ -3189,14 +3243,14 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   const int64_t nsample = (N + SEG_SEED_STRIDE - 1) / SEG_SEED_STRIDE;
   MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, SEG_SEED_STRIDE, P.Q.info, P.B.info, P.B.norms, nsample, N, d, P.width,
                          P.mainw, P.augx, SEED_DEPTH, nullptr, P.err, SLOT_SEED_PARTIAL, SLOT_SEED_LISTS, false, &slists,
-                         1, &ssp));
+                         1, &ssp, nullptr, nullptr, P.f16));
   float* seed = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_SEED, (size_t)N, &seed));
   seed_from_lists_kernel<<<(unsigned)ceil_div(N, 256), 256, 0, s>>>(slists, N, SEED_DEPTH - 1, seed);
   MANN_CHECK_LAUNCH();
   uint64_t* lists = nullptr;
   MANN_TRY(run_main_pass(ctx, s, mapA, P.B.xb, 1, P.Q.info, P.B.info, P.B.norms, N, N, d, P.width, P.mainw, P.augx, depth, seed,
-                         P.err, SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, &sp));
+                         P.err, SLOT_PARTIAL, SLOT_KEYS, true, &lists, 0, &sp, nullptr, nullptr, P.f16));
   // ---- certify + rerank (per row; the bounds are global, so valid for every set)
   uint64_t* cand = nullptr;
   int* cand_count = nullptr;
@@ -3290,7 +3344,7 @@ mann_status knn_bf16_batched_keys(Context* ctx, cudaStream_t s, const float* dat
   if (rep) {
     rep->rows_fallback = h_fb;
     rep->candidates = (int64_t)hc[2];
-    rep->precision_used = MANN_PREC_BF16;
+    rep->precision_used = P.f16 ? MANN_PREC_FP16 : MANN_PREC_BF16;
     rep->margin_used = depth - kreq;
   }
   *out_keys = keys;

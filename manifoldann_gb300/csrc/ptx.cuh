@@ -313,6 +313,13 @@ __host__ __device__ constexpr uint32_t idesc_e4m3_f32(int M, int N) {
          | ((uint32_t)(M >> 4) << 24);  // M / 16
 }
 
+// Instruction descriptor, kind::f16: FP16 A/B (format 0), FP32 D, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+  return (1u << 4)                      // D format: F32
+         | ((uint32_t)(N >> 3) << 17)   // N / 8
+         | ((uint32_t)(M >> 4) << 24);  // M / 16
+}
+
 // Instruction descriptor, kind::f16: BF16 A/B, FP32 D, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
   return (1u << 4)                      // D format: F32

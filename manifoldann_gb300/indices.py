@@ -18,7 +18,8 @@ from . import _lib
 from ._lib import ArgumentError, DimensionMismatch
 from .distances import Metric, default_distance, metric_code
 
-PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16, "fp8": _lib.PREC_FP8, "auto": _lib.PREC_AUTO}
+PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16, "fp8": _lib.PREC_FP8, "auto": _lib.PREC_AUTO,
+              "fp16": _lib.PREC_FP16}
 
 
 class Neighbor(NamedTuple):

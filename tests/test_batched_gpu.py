@@ -114,6 +114,21 @@ def test_batched_bf16_form_equals_oracle_per_set(gpu_lib, orc, metric, d, k):
         assert np.array_equal(dists[offs[c]:offs[c + 1]].view(np.uint32), d_o.view(np.uint32)), c
 
 
+@pytest.mark.parametrize("metric,d,k", [(1, 32, 15), (0, 12, 9)])
+def test_batched_fp16_form_equals_oracle_per_set(gpu_lib, orc, metric, d, k):
+    import manifoldann_gb300 as M
+
+    clouds = _clouds(7, 26, 3000, d, seed=200 + d)
+    dist = M.SqEuclidean() if metric == 1 else M.Euclidean()
+    ids, dists, offs, rep = M.knn_graph_batched_arrays([c.T for c in clouds], k, distance=dist, report=True,
+                                                       precision="fp16")
+    assert rep["precision_used"] == 4
+    for c, cl in enumerate(clouds):
+        i_o, d_o = orc.knn_graph_f32(cl, k, metric)
+        assert np.array_equal(ids[offs[c]:offs[c + 1]], i_o), c
+        assert np.array_equal(dists[offs[c]:offs[c + 1]].view(np.uint32), d_o.view(np.uint32)), c
+
+
 def test_batched_bf16_form_ties_duplicates_and_full_size(gpu_lib, orc):
     import manifoldann_gb300 as M
 

@@ -268,6 +268,71 @@ def test_fp8_form_graph(gpu_lib, orc):
     assert np.array_equal(g, g_o) and same_bits(gd, gd_o)
 
 
+# ---- FP16 form (MANN_PREC_FP16): FP16 main columns scaled by a power of two,
+# the norm fold as a BF16 step; the same certificate and exact FP32 rerank
+
+
+@pytest.mark.parametrize("kind,n,nq,d,k,metric", [("ang", 20000, 600, 256, 20, M_COS), ("aniso", 20000, 400, 128, 10, M_SQ),
+                                                 ("aniso", 8000, 300, 96, 10, M_EUC), ("iid", 5000, 200, 40, 7, M_SQ),
+                                                 ("mix", 6000, 300, 784, 10, M_SQ), ("ang", 9000, 200, 200, 24, M_COS)])
+def test_fp16_form_equals_oracle(gpu_lib, orc, kind, n, nq, d, k, metric):
+    from manifoldann_gb300 import synthetic
+
+    if kind == "mix":
+        base, q = synthetic.quantized_mixture(n, d, seed=21), synthetic.quantized_mixture(nq, d, seed=22)
+    elif kind == "ang":
+        base, q = _angular(n, d, 21), _angular(nq, d, 22)
+    elif kind == "aniso":
+        base = synthetic.anisotropic_clusters(n, d, seed=21, clusters=64)
+        q = synthetic.anisotropic_clusters(nq, d, seed=22, clusters=64)
+    else:
+        base, q = synthetic.iid_normal(n, d, seed=21), synthetic.iid_normal(nq, d, seed=22)
+    ids, dd, rep = gpu_knn(base, q, k, metric, precision="fp16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, k, metric)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dd, d_o)
+    assert rep["precision_used"] == 4
+    assert rep["rows_fallback"] <= nq // 50, rep
+    ids64, _ = gpu_knn(base, q, k, metric, precision="fp16", fp64_ties=True)
+    assert np.array_equal(ids64, orc.knn_f64(base, q, k, metric)[0])
+
+
+def test_fp16_form_graph(gpu_lib, orc):
+    from manifoldann_gb300 import synthetic
+
+    data = synthetic.anisotropic_clusters(7000, 64, seed=23, clusters=32)
+    g, gd = gpu_graph(data, 12, M_SQ, precision="fp16")
+    g_o, gd_o = orc.knn_graph_f32(data, 12, M_SQ)
+    assert np.array_equal(g, g_o) and same_bits(gd, gd_o)
+
+
+@pytest.mark.parametrize("mag", [1e15, 1e-15])
+def test_fp16_form_scales_into_range(gpu_lib, orc, mag):
+    """Rows far outside FP16's range are scaled by a power of two into it (the
+    answers and their distance bits stay the FP32 form's)."""
+    from manifoldann_gb300 import synthetic
+
+    base = (synthetic.iid_normal(6000, 64, seed=24) * np.float32(mag)).astype(np.float32)
+    q = (synthetic.iid_normal(150, 64, seed=25) * np.float32(mag)).astype(np.float32)
+    ids, dd, rep = gpu_knn(base, q, 10, M_SQ, precision="fp16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 10, M_SQ)
+    assert np.array_equal(ids, ids_o) and same_bits(dd, d_o)
+    assert rep["rows_fallback"] <= 3, rep
+
+
+def test_fp16_form_outlier_beyond_range_stays_exact(gpu_lib, orc):
+    """A point far beyond the sampled range saturates in FP16; its bound makes
+    the certificate fail instead of admitting a wrong answer."""
+    from manifoldann_gb300 import synthetic
+
+    base = synthetic.iid_normal(5000, 32, seed=26)
+    base[4321] *= np.float32(1e6)  # not among the scale probe's rows (every 4th row)
+    q = synthetic.iid_normal(100, 32, seed=27)
+    q[7] = base[4321] * np.float32(0.999)
+    ids, dd, rep = gpu_knn(base, q, 5, M_SQ, precision="fp16", report=True)
+    ids_o, d_o = orc.knn_f32(base, q, 5, M_SQ)
+    assert np.array_equal(ids, ids_o) and same_bits(dd, d_o)
+
 
 def test_fp64_tie_order_at_the_bit_level(gpu_lib, orc):
     """Squared distances from the origin that FP32 cannot tell apart (all round
