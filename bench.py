@@ -321,13 +321,18 @@ def run_ivf_leg(args, stream_ptr=0):
         return e0.elapsed_time(e1) / reps
 
     exact = {}
-    for name, prec in (("fp32", _lib.PREC_FP32), ("bf16", _lib.PREC_BF16)):
+    answers = {}
+    for name, prec in (("fp32", _lib.PREC_FP32), ("fp16", _lib.PREC_FP16), ("bf16", _lib.PREC_BF16)):
         pp = _lib.params(_lib.METRIC_SQEUCLIDEAN, K, prec)
         ms = timed(lambda: _lib.check(lib.mann_knn_device(pp, Xd.data_ptr(), IVF_N, Qd.data_ptr(), IVF_Q, IVF_D,
                                                           oi.data_ptr(), odist.data_ptr(), None, stream_ptr)),
                    2 if prec == _lib.PREC_FP32 else 5)
         exact[name] = {"ms": ms, "qps": IVF_Q / (ms / 1e3)}
-    truth = oi.cpu().numpy().copy()  # the BF16 form's certified exact top-10
+        answers[name] = (oi.cpu().numpy().copy(), odist.cpu().numpy().copy())
+    exact["fp16"]["equals_bf16_form"] = bool(np.array_equal(answers["fp16"][0], answers["bf16"][0]) and
+                                             np.array_equal(answers["fp16"][1].view(np.uint32),
+                                                            answers["bf16"][1].view(np.uint32)))
+    truth = answers["bf16"][0]  # the BF16 form's certified exact top-10
     t0 = time.perf_counter()
     labels = neighbour_list_labels(idx, X.T, TQ.T, K)
     label_s = time.perf_counter() - t0
@@ -454,7 +459,7 @@ def run_ivf_leg(args, stream_ptr=0):
                                              "kind": "port", "nprobe": npc,
                                              "sample": f"{m2} queries, nprobe {npc}, {ivf_dt:.1f} s "
                                                        "(reference IVF-Flat query restated in C)"}}
-    best_exact = max(exact["fp32"]["qps"], exact["bf16"]["qps"])
+    best_exact = max(exact["fp32"]["qps"], exact["bf16"]["qps"], exact["fp16"]["qps"])
     res = {"workload": IVF_WORKLOAD, "build_s": build_s, "label_s": label_s, "train_s": train_s,
            "train_epochs": args.ivf_epochs, "final_loss": float(loss[-1]), "exact": exact,
            "learned": out["learned"], "centroid_routing": out["centroid"], "e2e_learned": e2e,
@@ -673,7 +678,8 @@ ANG_WORKLOAD = ("angular-clusters-256d: N=290,000 points and Q=10,000 queries, G
 
 def run_angular_leg(args, stream_ptr=0):
     """Angular set: the cosine BF16 form (unit-normalised tensor-core pass,
-    FP32-form cosine rerank) beside the FP32 form on the same queries."""
+    FP32-form cosine rerank), the FP16 and FP8 forms, beside the FP32 form on
+    the same queries."""
     import torch
 
     from manifoldann_gb300 import _lib, synthetic
@@ -687,7 +693,8 @@ def run_angular_leg(args, stream_ptr=0):
     stream = torch.cuda.current_stream()
     out = {"workload": ANG_WORKLOAD}
     res = {}
-    for name, prec, reps in (("bf16", _lib.PREC_BF16, max(3, min(args.steps, 10))), ("fp8", _lib.PREC_FP8, 3),
+    for name, prec, reps in (("bf16", _lib.PREC_BF16, max(3, min(args.steps, 10))),
+                             ("fp16", _lib.PREC_FP16, max(3, min(args.steps, 10))), ("fp8", _lib.PREC_FP8, 3),
                              ("fp32", _lib.PREC_FP32, 2)):
         p = _lib.params(_lib.METRIC_COSINE, k, prec)
         r = _lib.KnnReport()
@@ -714,11 +721,18 @@ def run_angular_leg(args, stream_ptr=0):
                                         np.array_equal(res["bf16"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
     out["fp8_equals_fp32_form"] = bool(np.array_equal(res["fp8"][0], res["fp32"][0]) and
                                        np.array_equal(res["fp8"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
+    out["fp16_over_fp32"] = out["fp16"]["qps"] / out["fp32"]["qps"]
+    out["fp16_equals_fp32_form"] = bool(np.array_equal(res["fp16"][0], res["fp32"][0]) and
+                                        np.array_equal(res["fp16"][1].view(np.uint32), res["fp32"][1].view(np.uint32)))
     peak_tf, _, _, src = measured_peaks()
     flops = 2.0 * d * n * nq
     ach = flops / (out["bf16"]["ms"] / 1e3) / 1e12
     out["roofline_bf16"] = {"bound": "tensor", "achieved": ach, "peak": peak_tf, "unit": "TFLOP/s",
                             "frac": ach / peak_tf, "peak_source": f"{src} bf16 dense (burst)",
+                            "work": "2*d flops per (query, point) pair", "note": "whole call (normalise, passes, rerank)"}
+    ach16 = flops / (out["fp16"]["ms"] / 1e3) / 1e12
+    out["roofline_fp16"] = {"bound": "tensor", "achieved": ach16, "peak": peak_tf, "unit": "TFLOP/s",
+                            "frac": ach16 / peak_tf, "peak_source": f"{src} bf16 dense (burst; FP16 runs at the same rate)",
                             "work": "2*d flops per (query, point) pair", "note": "whole call (normalise, passes, rerank)"}
     if args.cpu_seconds > 0:
         import oracle
