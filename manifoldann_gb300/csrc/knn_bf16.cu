@@ -631,10 +631,36 @@ __device__ __forceinline__ uint64_t warp_sort32(uint64_t v, int lane) {
 constexpr int LGROUPS = 4;             // LIST / 8
 constexpr int GROUPED_MIN_DEPTH = 24;  // single-set passes use the groups from this list depth
 
+// List rescans compare the keys' distance words only (the high 32 bits, one
+// 32-bit load and compare per entry): among entries of equal distance the
+// first slot is taken as the largest.  The list then holds `depth` keys of
+// the smallest distances with ties broken by slot instead of id, which keeps
+// the certificate's premise (every point left out has a distance >= the
+// depth-th entry's), so the candidate sets and answers are the same.
+constexpr bool LIST_HI_SCAN = true;
+
+__device__ __forceinline__ uint32_t key_hi(const uint64_t* __restrict__ list, int e) {
+  return reinterpret_cast<const uint32_t*>(list)[2 * e * BM + 1];  // little-endian: the high word
+}
+
 __device__ __forceinline__ void list_group_max(const uint64_t* __restrict__ list, int g, int depth, uint64_t& m,
                                                int& ms) {
-  m = 0;
   ms = 8 * g;
+  if constexpr (LIST_HI_SCAN) {
+    uint32_t mh = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int e = 8 * g + i;
+      const uint32_t h = e < depth ? key_hi(list, e) : 0u;
+      if (h > mh) {
+        mh = h;
+        ms = e;
+      }
+    }
+    m = ms < depth ? list[ms * BM] : 0ull;
+    return;
+  }
+  m = 0;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int e = 8 * g + i;
@@ -661,14 +687,27 @@ __device__ __forceinline__ void list_admit(uint64_t* __restrict__ list, uint64_t
     } else {
       list[lslot * BM] = c;  // the largest entry drops out
     }
-    uint64_t m = 0;
     int ms = 0;
+    uint64_t m = 0;
+    if constexpr (LIST_HI_SCAN) {
+      uint32_t mh = 0;
 #pragma unroll 8
-    for (int e2 = 0; e2 < depth; ++e2) {
-      const uint64_t v2 = list[e2 * BM];
-      if (v2 > m) {
-        m = v2;
-        ms = e2;
+      for (int e2 = 0; e2 < depth; ++e2) {
+        const uint32_t h = key_hi(list, e2);
+        if (h > mh) {
+          mh = h;
+          ms = e2;
+        }
+      }
+      m = list[ms * BM];
+    } else {
+#pragma unroll 8
+      for (int e2 = 0; e2 < depth; ++e2) {
+        const uint64_t v2 = list[e2 * BM];
+        if (v2 > m) {
+          m = v2;
+          ms = e2;
+        }
       }
     }
     lslot = ms;
