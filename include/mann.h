@@ -46,7 +46,9 @@ typedef int32_t mann_status;
 #define MANN_PREC_FP8 2  /* FP8-e4m3 tcgen05 tiles with per-row power-of-two scales, certified
                             top-(k+m), exact FP32 rerank (never chosen by AUTO: its certified
                             window is far wider than BF16's on the measured sets) */
-#define MANN_PREC_AUTO 3 /* library picks (BF16 form when d >= 128 and the metric is L2) */
+#define MANN_PREC_AUTO 3 /* library picks: the tensor-core form when k <= 24, d >= 128 and n >= 4096
+                            (FP16 rows when BF16 cannot hold the centred, scaled data exactly, BF16
+                            rows otherwise), else the FP32 form */
 #define MANN_PREC_FP16 4 /* FP16 tcgen05 tiles: rows centred and scaled by a power of two into
                             FP16's range (operand rounding 2^-11, one product per term at the
                             16-bit tensor rate, where data that BF16 cannot hold exactly needs

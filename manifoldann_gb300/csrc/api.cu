@@ -78,6 +78,7 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
   } else if (p->precision == MANN_PREC_AUTO) {
     use_bf16 = kreq <= 24 && d >= 128 && n >= 4096;
   }
+  const int form_used = p->precision == MANN_PREC_AUTO ? FORM_AUTO16 : form;
   const float* qn = nullptr;
   const float* bn = nullptr;
   if (p->metric == MANN_METRIC_COSINE && !use_bf16) {
@@ -96,7 +97,7 @@ mann_status search_device_body(Context* ctx, cudaStream_t s, const mann_knn_para
   uint64_t* keys = nullptr;
   if (use_bf16) {
     MANN_TRY(knn_bf16_keys(ctx, s, base, n, qs, nq, d, p->metric, kreq, p->margin,
-                           (p->flags & MANN_FLAG_FP64_TIES) != 0, &keys, rep, form));
+                           (p->flags & MANN_FLAG_FP64_TIES) != 0, &keys, rep, form_used));
     if (rep) rep->rows = nq;
   } else if (p->flags & MANN_FLAG_FP64_TIES) {
     // FP32 scan with a few extra entries, then FP64 order for near-ties

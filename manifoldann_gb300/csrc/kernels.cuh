@@ -30,7 +30,9 @@ mann_status launch_finish(const uint64_t* keys, int64_t nq, int kk, int kout, in
 // Operand forms of the tensor-core search: BF16 rows (the three-product split
 // when BF16 cannot hold the data), E4M3 rows with per-row power-of-two scales
 // (kind::f8f6f4), FP16 rows scaled by one power of two into FP16's range.
-enum : int { FORM_BF16 = 0, FORM_FP8 = 1, FORM_FP16 = 2 };
+// FORM_AUTO16: FP16 rows when BF16 cannot hold the data exactly (one
+// product per term instead of the split's three), BF16 rows otherwise.
+enum : int { FORM_BF16 = 0, FORM_FP8 = 1, FORM_FP16 = 2, FORM_AUTO16 = 3 };
 
 // Tensor-core form (SqEuclidean / Euclidean / cosine): certified candidates,
 // exact FP32 rerank, optional FP64 near-tie order.  Result: keys [nq][kreq].

@@ -2818,7 +2818,8 @@ struct Bf16Prep {
 
 mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_t n, const float* qs, int64_t nq,
                          int d, int metric, Bf16Prep* P, int form = FORM_BF16) {
-  const bool fp8 = form == FORM_FP8, f16 = form == FORM_FP16;
+  const bool fp8 = form == FORM_FP8;
+  bool f16 = form == FORM_FP16;  // FORM_AUTO16 decides below, from the row sample
   // operand rows: 16-byte multiples (8 BF16 / FP16 or 16 E4M3 values)
   const int dp = fp8 ? (d + 15) & ~15 : (d + 7) & ~7;
   const bool self = (qs == base);
@@ -2882,6 +2883,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   int h_inexact = 0;
   MANN_CUDA_TRY(cudaMemcpyAsync(&h_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost, s));
   MANN_CUDA_TRY(cudaStreamSynchronize(s));
+  if (form == FORM_AUTO16 && h_inexact) f16 = true;
   const int split = (h_inexact && form == FORM_BF16) ? 1 : 0;  // the FP8 and FP16 forms have no split
   if (f16) scale = f16_scale;  // the conversion and the certificate use the FP16 form's scale
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
@@ -2998,7 +3000,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   if (margin > 0) {
     depth = std::min(L, kreq + margin);
   } else {
-    auto it = ctx->tune.find(tkey ^ ((uint64_t)split << 62));
+    auto it = ctx->tune.find(tkey ^ ((uint64_t)split << 62) ^ ((uint64_t)P.f16 << 59));
     depth = it != ctx->tune.end() ? (int)it->second : L;
   }
   Bf16Operand B = P.B, Q = P.Q;
@@ -3090,7 +3092,7 @@ mann_status knn_bf16_keys(Context* ctx, cudaStream_t s, const float* base, int64
   const int h_fb = reinterpret_cast<const int*>(hc + 8)[1];
   if (margin <= 0 && h_err == 0) {
     // autotune the admission depth (the k-margin) from the depths the certificates needed
-    ctx->tune[tkey ^ ((uint64_t)split << 62)] = (uint64_t)tuned_depth(hc + 16, kreq);
+    ctx->tune[tkey ^ ((uint64_t)split << 62) ^ ((uint64_t)P.f16 << 59)] = (uint64_t)tuned_depth(hc + 16, kreq);
   }
   if (h_err != 0)
     return fail(MANN_ETIMEOUT, "tensor-core kernel: a bounded wait ran out (role " + std::to_string(h_err) + ")");

@@ -402,6 +402,54 @@ __global__ void __launch_bounds__(K1_THREADS, 2)
 constexpr int FEW_Q = 32;
 constexpr int FEW_T = 256;
 constexpr int FEW_DC = 32;
+// up to FEW_QS rows with d <= FEW_STAGED_D: the rows are staged whole in shared
+// memory once, and each thread streams its point with no barrier per chunk
+constexpr int FEW_QS = 4;
+constexpr int FEW_STAGED_D = 2048;
+
+// the FP32 form's distance from the sequential sum `acc` (row qrow, point pi)
+template <int METRIC>
+__device__ __forceinline__ float few_distance(float acc, const float* __restrict__ qnorm, int64_t qrow,
+                                              const float* __restrict__ bnorm, int64_t pi, bool valid) {
+  float v = acc;
+  if constexpr (METRIC == MANN_METRIC_EUCLIDEAN) {
+    v = __fsqrt_rn(v);
+  } else if constexpr (METRIC == MANN_METRIC_COSINE) {
+    const float qnv = qnorm[qrow];
+    const float bnv = valid ? bnorm[pi] : 1.0f;
+    const float den = __fmul_rn(__fsqrt_rn(qnv), __fsqrt_rn(bnv));
+    v = __fsub_rn(1.0f, __fdiv_rn(v, den));
+    if (v < 0.0f) v = 0.0f;
+  }
+  return v;
+}
+
+// the block's distances dsm[j][0, np) (points p0 ...) into the lists of rows
+// j = warp + 8 m, held by that warp
+template <int KW, int M>
+__device__ __forceinline__ void few_fold(const float (*dsm)[FEW_T + 1], uint64_t (&L)[M][KW], int nq, int warp,
+                                         int lane, int64_t p0, int np, int k) {
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int j = warp + 8 * m;
+    if (j >= nq) continue;  // warp-uniform
+    uint64_t thr = list_get<KW>(L[m], k - 1);
+    for (int c8 = 0; c8 < FEW_T; c8 += 32) {
+      const int col = c8 + lane;
+      const uint64_t key = col < np ? make_key(dsm[j][col], (uint32_t)(p0 + col)) : KEY_NONE;
+      unsigned pend = __ballot_sync(FULL, key < thr);
+      while (pend) {
+        const int src = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const uint64_t cnd = __shfl_sync(FULL, key, src);
+        if (cnd < thr) {
+          list_insert<KW>(L[m], cnd, lane);
+          thr = list_get<KW>(L[m], k - 1);
+        }
+      }
+    }
+  }
+}
 
 template <int METRIC, int KW, bool VEC>
 __global__ void __launch_bounds__(FEW_T, 2)
@@ -476,43 +524,10 @@ __global__ void __launch_bounds__(FEW_T, 2)
       }
     }
 #pragma unroll
-    for (int j = 0; j < FEW_Q; ++j) {
-      if (j < nq) {
-        float v = acc[j];
-        if constexpr (METRIC == MANN_METRIC_EUCLIDEAN) {
-          v = __fsqrt_rn(v);
-        } else if constexpr (METRIC == MANN_METRIC_COSINE) {
-          const float qnv = qnorm[qrows ? qrows[j] : j];
-          const float bnv = valid ? bnorm[pi] : 1.0f;
-          const float den = __fmul_rn(__fsqrt_rn(qnv), __fsqrt_rn(bnv));
-          v = __fsub_rn(1.0f, __fdiv_rn(v, den));
-          if (v < 0.0f) v = 0.0f;
-        }
-        dsm[j][t] = v;
-      }
-    }
+    for (int j = 0; j < FEW_Q; ++j)
+      if (j < nq) dsm[j][t] = few_distance<METRIC>(acc[j], qnorm, qrows ? qrows[j] : j, bnorm, pi, valid);
     __syncthreads();
-    const int np = (int)min((int64_t)FEW_T, n - p0);
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const int j = warp + 8 * m;
-      if (j >= nq) continue;  // warp-uniform
-      uint64_t thr = list_get<KW>(L[m], k - 1);
-      for (int c8 = 0; c8 < FEW_T; c8 += 32) {
-        const int col = c8 + lane;
-        const uint64_t key = col < np ? make_key(dsm[j][col], (uint32_t)(p0 + col)) : KEY_NONE;
-        unsigned pend = __ballot_sync(FULL, key < thr);
-        while (pend) {
-          const int src = __ffs(pend) - 1;
-          pend &= pend - 1;
-          const uint64_t cnd = __shfl_sync(FULL, key, src);
-          if (cnd < thr) {
-            list_insert<KW>(L[m], cnd, lane);
-            thr = list_get<KW>(L[m], k - 1);
-          }
-        }
-      }
-    }
+    few_fold<KW, 4>(dsm, L, nq, warp, lane, p0, (int)min((int64_t)FEW_T, n - p0), k);
   }
 #pragma unroll
   for (int m = 0; m < 4; ++m) {
@@ -527,13 +542,113 @@ __global__ void __launch_bounds__(FEW_T, 2)
   }
 }
 
+// few_rows_kernel for nq <= FEW_QS rows of d <= FEW_STAGED_D: the rows sit in
+// shared memory ([FEW_QS][d], staged once), and each thread reads its point
+// with eight float4 loads in flight and no barrier per chunk (the chunked
+// form waits for its loads 25 times per point at d = 784); the same
+// sequential sums in dimension order, the same lists and layout.
+template <int METRIC, int KW, bool VEC>
+__global__ void __launch_bounds__(FEW_T, 2)
+    few_rows_staged_kernel(const float* __restrict__ base, int64_t n, const float* __restrict__ qs,
+                           const int32_t* __restrict__ qrows, int nq, int d, const float* __restrict__ qnorm,
+                           const float* __restrict__ bnorm, int k, uint64_t* __restrict__ partial) {
+  extern __shared__ __align__(16) float fq[];  // [FEW_QS][d]
+  __shared__ float dsm[FEW_QS][FEW_T + 1];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  for (int e = t; e < FEW_QS * d; e += FEW_T) {
+    const int r = e / d, c = e % d;
+    fq[e] = r < nq ? __ldg(&qs[(int64_t)(qrows ? qrows[r] : r) * d + c]) : 0.0f;
+  }
+  __syncthreads();
+  uint64_t L[1][KW];
+#pragma unroll
+  for (int s = 0; s < KW; ++s) L[0][s] = KEY_NONE;
+  for (int64_t p0 = (int64_t)blockIdx.x * FEW_T; p0 < n; p0 += (int64_t)gridDim.x * FEW_T) {
+    const int64_t pi = p0 + t;
+    const bool valid = pi < n;
+    const float* prow = base + (valid ? pi : 0) * d;
+    float acc[FEW_QS];
+#pragma unroll
+    for (int j = 0; j < FEW_QS; ++j) acc[j] = 0.0f;
+    if (valid) {
+      if (VEC) {  // d % 4 == 0 and 16-byte aligned rows
+#pragma unroll 8
+        for (int c = 0; c < d; c += 4) {
+          const float4 v = __ldg(reinterpret_cast<const float4*>(prow + c));
+#pragma unroll
+          for (int j = 0; j < FEW_QS; ++j) {
+            if (j < nq) {
+              const float4 q4 = *reinterpret_cast<const float4*>(&fq[j * d + c]);
+              float a = acc[j];
+              if constexpr (METRIC == MANN_METRIC_COSINE) {
+                a = __fmaf_rn(q4.x, v.x, a);
+                a = __fmaf_rn(q4.y, v.y, a);
+                a = __fmaf_rn(q4.z, v.z, a);
+                a = __fmaf_rn(q4.w, v.w, a);
+              } else {
+                float u = __fsub_rn(q4.x, v.x);
+                a = __fmaf_rn(u, u, a);
+                u = __fsub_rn(q4.y, v.y);
+                a = __fmaf_rn(u, u, a);
+                u = __fsub_rn(q4.z, v.z);
+                a = __fmaf_rn(u, u, a);
+                u = __fsub_rn(q4.w, v.w);
+                a = __fmaf_rn(u, u, a);
+              }
+              acc[j] = a;
+            }
+          }
+        }
+      } else {
+#pragma unroll 8
+        for (int c = 0; c < d; ++c) {
+          const float pv = __ldg(prow + c);
+#pragma unroll
+          for (int j = 0; j < FEW_QS; ++j) {
+            if (j < nq) {
+              const float qv = fq[j * d + c];
+              if constexpr (METRIC == MANN_METRIC_COSINE) {
+                acc[j] = __fmaf_rn(qv, pv, acc[j]);
+              } else {
+                const float u = __fsub_rn(qv, pv);
+                acc[j] = __fmaf_rn(u, u, acc[j]);
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // the previous points' fold has read dsm
+#pragma unroll
+    for (int j = 0; j < FEW_QS; ++j)
+      if (j < nq) dsm[j][t] = few_distance<METRIC>(acc[j], qnorm, qrows ? qrows[j] : j, bnorm, pi, valid);
+    __syncthreads();
+    few_fold<KW, 1>(dsm, L, nq, warp, lane, p0, (int)min((int64_t)FEW_T, n - p0), k);
+  }
+  if (warp < nq) {
+    uint64_t* dst = partial + ((int64_t)warp * gridDim.x + blockIdx.x) * k;
+#pragma unroll
+    for (int s = 0; s < KW; ++s) {
+      const int e = s * 32 + lane;
+      if (e < k) dst[e] = L[0][s];
+    }
+  }
+}
+
 template <int METRIC, bool VEC>
 mann_status launch_few_m(int grid, const float* base, int64_t n, const float* qs, const int32_t* rows, int nq,
                          int d, const float* qn, const float* bn, int kk, uint64_t* partial, cudaStream_t s) {
-  if (kk <= 32)
+  if (nq <= FEW_QS && d <= FEW_STAGED_D) {
+    const size_t smem = sizeof(float) * FEW_QS * d;  // <= 32 KB
+    if (kk <= 32)
+      few_rows_staged_kernel<METRIC, 1, VEC><<<grid, FEW_T, smem, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
+    else
+      few_rows_staged_kernel<METRIC, 2, VEC><<<grid, FEW_T, smem, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
+  } else if (kk <= 32) {
     few_rows_kernel<METRIC, 1, VEC><<<grid, FEW_T, 0, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
-  else
+  } else {
     few_rows_kernel<METRIC, 2, VEC><<<grid, FEW_T, 0, s>>>(base, n, qs, rows, nq, d, qn, bn, kk, partial);
+  }
   MANN_CHECK_LAUNCH();
   return MANN_OK;
 }

@@ -297,6 +297,18 @@ def test_fp16_form_equals_oracle(gpu_lib, orc, kind, n, nq, d, k, metric):
     assert np.array_equal(ids64, orc.knn_f64(base, q, k, metric)[0])
 
 
+def test_auto_takes_fp16_rows_where_bf16_cannot_hold_the_data(gpu_lib, orc):
+    from manifoldann_gb300 import synthetic
+
+    for data, q, want in ((synthetic.anisotropic_clusters(6000, 128, seed=31, clusters=16),
+                           synthetic.anisotropic_clusters(200, 128, seed=32, clusters=16), 4),
+                          (synthetic.quantized_mixture(6000, 256, seed=33), synthetic.quantized_mixture(200, 256, seed=34), 1)):
+        ids, dd, rep = gpu_knn(data, q, 10, M_SQ, precision="auto", report=True)
+        ids_o, d_o = orc.knn_f32(data, q, 10, M_SQ)
+        assert np.array_equal(ids, ids_o) and same_bits(dd, d_o)
+        assert rep["precision_used"] == want, rep
+
+
 def test_fp16_form_graph(gpu_lib, orc):
     from manifoldann_gb300 import synthetic
 

@@ -123,6 +123,20 @@ def test_fp32_edge_shapes(gpu_lib, orc, n, d, k):
     assert np.array_equal(ids, ids_o) and same_bits(dist, d_o)
 
 
+@pytest.mark.parametrize("nq,n,d,k,metric", [(1, 60000, 784, 10, M_SQ), (3, 20000, 129, 40, M_EUC), (4, 9000, 2048, 7, M_COS),
+                                              (2, 5000, 37, 64, M_SQ), (5, 7000, 64, 12, M_SQ), (4, 3000, 2100, 5, M_EUC)])
+def test_fp32_few_rows_equal_oracle(gpu_lib, orc, nq, n, d, k, metric):
+    """A handful of query rows (the shared-memory staged scan for <= 4 rows of
+    d <= 2048, the chunked one above): ids and distance bits of the oracle."""
+    rng = np.random.default_rng(nq * 1000 + d)
+    base = rng.standard_normal((n, d)).astype(np.float32)
+    q = rng.standard_normal((nq, d)).astype(np.float32)
+    ids, dd = gpu_knn(base, q, k, metric)
+    ids_o, d_o = orc.knn_f32(base, q, k, metric)
+    assert np.array_equal(ids, ids_o)
+    assert same_bits(dd, d_o)
+
+
 def test_fp32_exact_ties_and_duplicates(gpu_lib, orc):
     # all-equal points: every distance ties, the order must be by id
     base = np.ones((500, 8), np.float32)
