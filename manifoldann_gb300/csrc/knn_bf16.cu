@@ -1381,32 +1381,35 @@ __global__ void k2_merge(const uint64_t* __restrict__ partial, int64_t nq, int s
     }
     return band_first_slot[b] + g;
   };
+  static_assert(LIST == 32, "one list entry per lane");
   uint64_t Lr = lane < depth ? partial[(q * smax + slot_of(0)) * L + lane] : KEY_NONE;
   uint64_t pre[4];  // the next lists, one coalesced load each, issued together
 #pragma unroll
-  for (int u = 0; u < 4; ++u) pre[u] = 1 + u < nseg ? partial[(q * smax + slot_of(1 + u)) * L + lane] : KEY_NONE;
+  for (int u = 0; u < 4; ++u)
+    pre[u] = (1 + u < nseg && lane < depth) ? partial[(q * smax + slot_of(1 + u)) * L + lane] : KEY_NONE;
   for (int g = 1; g < nseg; ++g) {
-    // entries then come by shuffle
-    uint64_t mine;
+    uint64_t b;
     if (g <= 4) {
-      mine = pre[0];
+      b = pre[0];
 #pragma unroll
       for (int u = 1; u < 4; ++u)
-        if (g == 1 + u) mine = pre[u];
+        if (g == 1 + u) b = pre[u];
     } else {
-      mine = partial[(q * smax + slot_of(g)) * L + lane];
+      b = lane < depth ? partial[(q * smax + slot_of(g)) * L + lane] : KEY_NONE;
     }
-    uint64_t tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
-    for (int e = 0; e < depth; ++e) {
-      const uint64_t c = __shfl_sync(FULL, (unsigned long long)mine, e);  // sorted: stop at the first that cannot enter
-      if (!(c < tk)) break;
-      uint64_t one[1] = {Lr};
-      wl_insert<1>(one, c, lane);
-      Lr = lane < depth ? one[0] : KEY_NONE;
-      tk = __shfl_sync(FULL, (unsigned long long)Lr, depth - 1);
+    // bitonic merge of two ascending lists: against the other list reversed,
+    // the lane-wise minima are the 32 smallest keys of both (a bitonic
+    // sequence), which five half-cleaner steps sort
+    const uint64_t br = __shfl_sync(FULL, (unsigned long long)b, 31 - lane);
+    uint64_t m = br < Lr ? br : Lr;
+#pragma unroll
+    for (int j = 16; j > 0; j >>= 1) {
+      const uint64_t o = __shfl_xor_sync(FULL, (unsigned long long)m, j);
+      m = (lane & j) ? (o > m ? o : m) : (o < m ? o : m);
     }
+    Lr = m;
   }
-  out[q * L + lane] = Lr;
+  out[q * L + lane] = lane < depth ? Lr : KEY_NONE;
 }
 
 // ---------------------------------------------------------------- certify + rerank
