@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain 64-d FP32 leg")
     ap.add_argument("--no-fp8", action="store_true", help="skip the FP8-form measurement")
     ap.add_argument("--case", choices=["full", "profile", "ivf", "batched", "batched-profile", "ivf-profile", "angular",
-                                       "plain"],
+                                       "angular-profile", "plain"],
                     default="full",
                     help="profile: BF16 steps only (query batch + self graph, two k2_main "
                          "launches per step), for ncu captures")
@@ -279,6 +279,29 @@ def run_profile_case(args):
     torch.cuda.synchronize()
     print(json.dumps({"case": "profile", "steps": args.warmup + args.steps,
                       "k2_main_launches": 2 * (args.warmup + args.steps)}), flush=True)
+    return 0
+
+
+def run_angular_profile_case(args):
+    """Case for ncu: the FP16-form cosine call on the angular set (290,000 x
+    256 points, 10,000 queries, k = 20) only, warmup + steps calls."""
+    import torch
+
+    from manifoldann_gb300 import _lib, synthetic
+
+    lib = _lib.load()
+    n, nq, d, k = 290000, 10000, 256, 20
+    base = torch.from_numpy(synthetic.angular_clusters(n, d, seed=1)).cuda()
+    q = torch.from_numpy(synthetic.angular_clusters(nq, d, seed=2)).cuda()
+    ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+    dd = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+    sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = _lib.params(_lib.METRIC_COSINE, k, _lib.PREC_FP16)
+    for _ in range(args.warmup + args.steps):
+        _lib.check(lib.mann_knn_device(p, base.data_ptr(), n, q.data_ptr(), nq, d, ids.data_ptr(), dd.data_ptr(),
+                                       None, sp))
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "angular-profile", "calls": args.warmup + args.steps}), flush=True)
     return 0
 
 
@@ -1090,6 +1113,8 @@ def main():
         print(json.dumps({"case": "angular", "angular_cosine": run_angular_leg(
             args, C.c_void_p(torch.cuda.current_stream().cuda_stream))}), flush=True)
         return 0
+    if args.case == "angular-profile":
+        return run_angular_profile_case(args)
     if args.case == "plain":
         import torch
 

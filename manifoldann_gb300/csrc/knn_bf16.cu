@@ -117,14 +117,23 @@ __global__ void scale_rows_kernel(const float* __restrict__ x, int64_t n, int d,
   for (int c = threadIdx.x & 31; c < d; c += 32) o[c] = nr > 0.0f ? __fdiv_rn(__ldg(r + c), nr) : 0.0f;
 }
 
+// Value c of row r as the tensor-core passes see it: with row norms (cosine),
+// x / sqrt(|x|^2) exactly as scale_rows_kernel writes it (a zero or
+// non-finite row gives 0), else x itself.
+__device__ __forceinline__ float unit_value(float xv, const float* __restrict__ rnorm, int64_t r) {
+  if (!rnorm) return xv;
+  const float nr = __fsqrt_rn(rnorm[r]);
+  return nr > 0.0f ? __fdiv_rn(xv, nr) : 0.0f;
+}
+
 __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
-                                     int64_t rows, float* __restrict__ mu) {
+                                     int64_t rows, float* __restrict__ mu, const float* __restrict__ rnorm) {
   __shared__ double part[32][33];
   const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + cl;
   float s = 0.0f;
   if (c < d)
-    for (int64_t i = g; i < rows; i += 32) s += x[(i * stride) * d + c];
+    for (int64_t i = g; i < rows; i += 32) s += unit_value(x[(i * stride) * d + c], rnorm, i * stride);
   part[g][cl] = (double)s;
   __syncthreads();
   if (g == 0 && c < d) {
@@ -151,7 +160,7 @@ __device__ __forceinline__ void scale_candidate(int i, float m, float* sc, float
 // max) in score[NUM_SCALES] for the FP16 form's scale
 __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d,
                                    const float* __restrict__ mu, int64_t stride,
-                                   double* __restrict__ score) {
+                                   double* __restrict__ score, const float* __restrict__ rnorm) {
   const int lane = threadIdx.x & 31;
   const int64_t row = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * stride;
   const int cand = blockIdx.y;
@@ -160,7 +169,7 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
   for (int c = lane; c < d; c += 32) {
     float sc, mc;
     scale_candidate(cand, mu[c], &sc, &mc);
-    const float cv = __fmul_rn(sc, __fsub_rn(x[row * d + c], mc));
+    const float cv = __fmul_rn(sc, __fsub_rn(unit_value(x[row * d + c], rnorm, row), mc));
     const float bv = __bfloat162float(__float2bfloat16_rn(cv));
     rr = __fmaf_rn(cv - bv, cv - bv, rr);
     cc = __fmaf_rn(cv, cv, cc);
@@ -227,7 +236,7 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
                                     const float* __restrict__ mu, const float* __restrict__ scale_ptr,
                                     __nv_bfloat16* __restrict__ xb, RowInfo* __restrict__ info,
                                     float* __restrict__ norms, BaseMax* __restrict__ bmax, int split,
-                                    int role, int f16) {
+                                    int role, int f16, const float* __restrict__ rnorm) {
   const int lane = threadIdx.x & 31;
   const float scale = *scale_ptr;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -237,6 +246,8 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   const bool valid = row < n;
   const float* xr = x + (valid ? row : 0) * d;
   __nv_bfloat16* br = xb + (valid ? row : 0) * (int64_t)width;
+  // cosine: the unit row x / sqrt(|x|^2), as unit_value computes it
+  const float unr = (rnorm && valid) ? __fsqrt_rn(rnorm[row]) : 1.0f;
   // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
   // certificate adds to its bound (norm_rel_err)
@@ -256,7 +267,10 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
     const int c = c0 + 32 * u;
     if (c >= dp) break;
     float cv = 0.0f;
-    if (c < d) cv = __fmul_rn(scale, __fsub_rn(xv[u], mv[u]));
+    if (c < d) {
+      const float uv = rnorm ? (unr > 0.0f ? __fdiv_rn(xv[u], unr) : 0.0f) : xv[u];
+      cv = __fmul_rn(scale, __fsub_rn(uv, mv[u]));
+    }
     float bv;
     if (f16) {
       const float cl = fminf(fmaxf(cv, -65504.0f), 65504.0f);
@@ -2829,28 +2843,39 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const bool cosine = metric == MANN_METRIC_COSINE;
 
   // ---- cosine: the tensor-core passes run on unit-normalised rows
-  // (1 - cos = ||q^ - p^||^2 / 2); the rerank uses the original rows
+  // (1 - cos = ||q^ - p^||^2 / 2); the rerank uses the original rows.  The
+  // BF16 and FP16 forms normalise on the fly (rn_b / rn_q: the row norms the
+  // prep kernels divide by); the FP8 conversion reads a normalised copy.
   const float* mbase = base;
   const float* mqs = qs;
   float *cos_bn = nullptr, *cos_qn = nullptr;
+  const float *rn_b = nullptr, *rn_q = nullptr;
   if (cosine) {
-    float *xb = nullptr, *xq = nullptr;
-    MANN_TRY(ctx->scratch_t(SLOT_COS_B, (size_t)n * d, &xb));
     MANN_TRY(ctx->scratch_t(SLOT_COS_NB, (size_t)n, &cos_bn));
     MANN_TRY(launch_row_sqnorm(base, n, d, cos_bn, s));
-    scale_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, cos_bn, xb);
-    MANN_CHECK_LAUNCH();
-    mbase = xb;
     if (self) {
-      mqs = xb;
       cos_qn = cos_bn;
     } else {
-      MANN_TRY(ctx->scratch_t(SLOT_COS_Q, (size_t)nq * d, &xq));
       MANN_TRY(ctx->scratch_t(SLOT_COS_NQ, (size_t)nq, &cos_qn));
       MANN_TRY(launch_row_sqnorm(qs, nq, d, cos_qn, s));
-      scale_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, cos_qn, xq);
+    }
+    if (fp8) {
+      float *xb = nullptr, *xq = nullptr;
+      MANN_TRY(ctx->scratch_t(SLOT_COS_B, (size_t)n * d, &xb));
+      scale_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(base, n, d, cos_bn, xb);
       MANN_CHECK_LAUNCH();
-      mqs = xq;
+      mbase = xb;
+      if (self) {
+        mqs = xb;
+      } else {
+        MANN_TRY(ctx->scratch_t(SLOT_COS_Q, (size_t)nq * d, &xq));
+        scale_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(qs, nq, d, cos_qn, xq);
+        MANN_CHECK_LAUNCH();
+        mqs = xq;
+      }
+    } else {
+      rn_b = cos_bn;
+      rn_q = cos_qn;
     }
   }
 
@@ -2863,7 +2888,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   {
     const int64_t rows = std::min<int64_t>(n, 4096);
     const int64_t stride = n / rows;
-    centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(mbase, n, d, stride, rows, mu);
+    centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(mbase, n, d, stride, rows, mu, rn_b);
     MANN_CHECK_LAUNCH();
   }
   // pick the centre / scale with the smallest BF16 residual on a row sample
@@ -2872,7 +2897,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const int64_t sample_rows = std::min<int64_t>(n, 1024);
   const int64_t stride = std::max<int64_t>(1, n / sample_rows);
   dim3 pg((unsigned)ceil_div(ceil_div(n, stride), 8), NUM_SCALES);
-  scale_probe_kernel<<<pg, 256, 0, s>>>(mbase, n, d, mu, stride, score);
+  scale_probe_kernel<<<pg, 256, 0, s>>>(mbase, n, d, mu, stride, score, rn_b);
   MANN_CHECK_LAUNCH();
   float* scale = reinterpret_cast<float*>(bmax + 1);
   int* inexact = reinterpret_cast<int*>(scale + 1);
@@ -2928,7 +2953,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
   MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
   convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, augx, width, mu, scale, B.xb,
-                                                              B.info, B.norms, bmax, split, 1, f16 ? 1 : 0);
+                                                              B.info, B.norms, bmax, split, 1, f16 ? 1 : 0, rn_b);
   MANN_CHECK_LAUNCH();
   if (self && !split) {
     Q = B;
@@ -2936,7 +2961,8 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
     MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * width, &Q.xb));
     MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
     convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, augx, width, mu, scale, Q.xb,
-                                                                  Q.info, nullptr, nullptr, split, 0, f16 ? 1 : 0);
+                                                                  Q.info, nullptr, nullptr, split, 0, f16 ? 1 : 0,
+                                                                  rn_q);
     MANN_CHECK_LAUNCH();
   }
   P->width = width;

@@ -30,7 +30,8 @@ using wl::list_insert;
 // Squared row norms as the FP32 form's sequential sum (dimension order, one
 // fmaf per term).  One warp per 32 rows: 32 x 32 tiles come in through
 // shared memory with coalesced loads (a row's 32 columns per load
-// instruction), then lane l adds row l's squares in order.
+// instruction), then lane l adds row l's squares in order; the next tile's
+// loads are issued before the current tile's sums.
 __global__ void __launch_bounds__(256) row_sqnorm_kernel(const float* __restrict__ x, int64_t n, int d,
                                                          float* __restrict__ out) {
   __shared__ float tile[8][32][33];
@@ -38,11 +39,20 @@ __global__ void __launch_bounds__(256) row_sqnorm_kernel(const float* __restrict
   const int64_t r0 = ((int64_t)blockIdx.x * 8 + w) * 32;
   if (r0 >= n) return;
   const int nr = (int)min((int64_t)32, n - r0);
+  float nxt[32];
+  auto fetch = [&](int c0) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+      nxt[i] = (i < nr && c0 + lane < d) ? __ldg(&x[(r0 + i) * d + c0 + lane]) : 0.0f;
+  };
+  fetch(0);
   float s = 0.0f;
   for (int c0 = 0; c0 < d; c0 += 32) {
     const int cw = min(32, d - c0);
-    for (int i = 0; i < nr; ++i) tile[w][i][lane] = lane < cw ? __ldg(&x[(r0 + i) * d + c0 + lane]) : 0.0f;
+#pragma unroll
+    for (int i = 0; i < 32; ++i) tile[w][i][lane] = nxt[i];
     __syncwarp();
+    if (c0 + 32 < d) fetch(c0 + 32);
     if (lane < nr)
       for (int c = 0; c < cw; ++c) s = __fmaf_rn(tile[w][lane][c], tile[w][lane][c], s);
     __syncwarp();
