@@ -101,11 +101,8 @@ struct BaseMax {
 
 // ---------------------------------------------------------------- prep kernels
 
-// Column means over an evenly spaced sample of rows.  Any centre keeps the
-// distances unchanged; a good one shrinks the BF16 values and their rounding.
-// Block (32 columns x 32 row groups): FP32 partial sums per thread, FP64 across groups.
-// Unit-normalised copy of every row (cosine): x^ = x / sqrt(|x|^2) with
-// |x|^2 the FP32 form's sequential sum (row_sqnorm_kernel, kept for the
+// Unit-normalised copy of every row (cosine, FP8 form): x^ = x / sqrt(|x|^2)
+// with |x|^2 the FP32 form's sequential sum (row_sqnorm_kernel, kept for the
 // rerank); a zero row stays zero.  One warp per row, coalesced.
 __global__ void scale_rows_kernel(const float* __restrict__ x, int64_t n, int d, const float* __restrict__ sqn,
                                   float* __restrict__ xh) {
@@ -117,23 +114,32 @@ __global__ void scale_rows_kernel(const float* __restrict__ x, int64_t n, int d,
   for (int c = threadIdx.x & 31; c < d; c += 32) o[c] = nr > 0.0f ? __fdiv_rn(__ldg(r + c), nr) : 0.0f;
 }
 
-// Value c of row r as the tensor-core passes see it: with row norms (cosine),
-// x / sqrt(|x|^2) exactly as scale_rows_kernel writes it (a zero or
-// non-finite row gives 0), else x itself.
-__device__ __forceinline__ float unit_value(float xv, const float* __restrict__ rnorm, int64_t r) {
-  if (!rnorm) return xv;
-  const float nr = __fsqrt_rn(rnorm[r]);
-  return nr > 0.0f ? __fdiv_rn(xv, nr) : 0.0f;
-}
-
+// Column means over an evenly spaced sample of rows (rows <= CENTRE_ROWS).
+// Any centre keeps the distances unchanged; a good one shrinks the BF16
+// values and their rounding.  Block (32 columns x 32 row groups): FP32
+// partial sums per thread, FP64 across groups.  With row norms (cosine) each
+// sampled row is scaled by one reciprocal, computed once per block: the
+// centre only needs to be near the unit rows' mean, not their exact bits.
+constexpr int CENTRE_ROWS = 4096;
 __global__ void centre_sample_kernel(const float* __restrict__ x, int64_t n, int d, int64_t stride,
                                      int64_t rows, float* __restrict__ mu, const float* __restrict__ rnorm) {
   __shared__ double part[32][33];
+  __shared__ float inv[CENTRE_ROWS];
   const int cl = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + cl;
+  if (rnorm) {
+    for (int64_t i = threadIdx.x; i < rows; i += blockDim.x) {
+      const float nr = __fsqrt_rn(rnorm[i * stride]);
+      inv[i] = nr > 0.0f ? 1.0f / nr : 0.0f;
+    }
+    __syncthreads();
+  }
   float s = 0.0f;
   if (c < d)
-    for (int64_t i = g; i < rows; i += 32) s += unit_value(x[(i * stride) * d + c], rnorm, i * stride);
+    for (int64_t i = g; i < rows; i += 32) {
+      const float xv = x[(i * stride) * d + c];
+      s += rnorm ? xv * inv[i] : xv;
+    }
   part[g][cl] = (double)s;
   __syncthreads();
   if (g == 0 && c < d) {
@@ -166,10 +172,15 @@ __global__ void scale_probe_kernel(const float* __restrict__ x, int64_t n, int d
   const int cand = blockIdx.y;
   if (row >= n) return;
   float rr = 0.0f, cc = 0.0f, mx = 0.0f;  // a heuristic score: FP32 is plenty
+  float inv = 1.0f;  // unit rows: one reciprocal of the row's norm (a heuristic needs no exact division)
+  if (rnorm) {
+    const float nr = __fsqrt_rn(rnorm[row]);
+    inv = nr > 0.0f ? 1.0f / nr : 0.0f;
+  }
   for (int c = lane; c < d; c += 32) {
     float sc, mc;
     scale_candidate(cand, mu[c], &sc, &mc);
-    const float cv = __fmul_rn(sc, __fsub_rn(unit_value(x[row * d + c], rnorm, row), mc));
+    const float cv = __fmul_rn(sc, __fsub_rn(x[row * d + c] * inv, mc));
     const float bv = __bfloat162float(__float2bfloat16_rn(cv));
     rr = __fmaf_rn(cv - bv, cv - bv, rr);
     cc = __fmaf_rn(cv, cv, cc);
@@ -246,7 +257,8 @@ __global__ void convert_rows_kernel(const float* __restrict__ x, int64_t n, int 
   const bool valid = row < n;
   const float* xr = x + (valid ? row : 0) * d;
   __nv_bfloat16* br = xb + (valid ? row : 0) * (int64_t)width;
-  // cosine: the unit row x / sqrt(|x|^2), as unit_value computes it
+  // cosine: the unit row x / sqrt(|x|^2), divided exactly as scale_rows_kernel
+  // writes it (a zero or non-finite row gives 0)
   const float unr = (rnorm && valid) ? __fsqrt_rn(rnorm[row]) : 1.0f;
   // per-lane FP32 sums (ceil(dp/32) terms each), cross-lane sum in FP64: every
   // sum carries a relative error below (ceil(dp/32) + 2) u, which the
@@ -2886,7 +2898,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));  // mu | BaseMax | scale
   BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + ((d + 31) & ~31));
   {
-    const int64_t rows = std::min<int64_t>(n, 4096);
+    const int64_t rows = std::min<int64_t>(n, CENTRE_ROWS);
     const int64_t stride = n / rows;
     centre_sample_kernel<<<(unsigned)ceil_div(d, 32), 1024, 0, s>>>(mbase, n, d, stride, rows, mu, rn_b);
     MANN_CHECK_LAUNCH();
