@@ -2224,7 +2224,7 @@ __device__ void sort_range(uint64_t* K, double* Vv, double* Ee, int p, int e) {
 // n_unresolved and (with unres_rows) listed for a wider list.
 // counters: [0] rows with a tie, [1] unresolved rows, [2] rows that needed
 // FP64 sequential sums.
-__global__ void __launch_bounds__(128) resolve_l2_kernel(const float* __restrict__ base,
+__global__ void __launch_bounds__(128, 10) resolve_l2_kernel(const float* __restrict__ base,
                                                          const float* __restrict__ qs, int d, int metric,
                                                          int64_t nq, int L, int kreq, float eps_up, double eps,
                                                          const uint64_t* __restrict__ cand,
@@ -2234,12 +2234,17 @@ __global__ void __launch_bounds__(128) resolve_l2_kernel(const float* __restrict
                                                          unsigned long long* __restrict__ counters,
                                                          const int32_t* __restrict__ rows,
                                                          int32_t* __restrict__ unres_rows) {
-  __shared__ uint64_t s_key[4][256];
-  __shared__ double s_v[4][256];
-  __shared__ double s_e[4][256];
-  __shared__ short s_cl[4][256];
-  __shared__ short s_g[4][256];
+  // per warp, lc = min(L, 256) entries each: keys, values, bounds (8 bytes),
+  // cluster and group starts (2 bytes) -- sized by the call, so that short
+  // lists leave room for more blocks per SM
+  extern __shared__ __align__(16) uint8_t rs_smem[];
+  const int lc = min(L, 256);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* K = reinterpret_cast<uint64_t*>(rs_smem) + w * lc;
+  double* Vv = reinterpret_cast<double*>(rs_smem + (size_t)4 * lc * 8) + w * lc;
+  double* Ee = reinterpret_cast<double*>(rs_smem + (size_t)8 * lc * 8) + w * lc;
+  short* cl = reinterpret_cast<short*>(rs_smem + (size_t)12 * lc * 8) + w * lc;
+  short* gr = reinterpret_cast<short*>(rs_smem + (size_t)12 * lc * 8 + (size_t)4 * lc * 2) + w * lc;
   const int64_t i = (int64_t)blockIdx.x * 4 + w;
   if (i >= nq) return;
   const int64_t q = rows ? (int64_t)rows[i] : i;
@@ -2248,12 +2253,7 @@ __global__ void __launch_bounds__(128) resolve_l2_kernel(const float* __restrict
   uint64_t* out = keys_out + q * kreq;
   for (int e = lane; e < kreq; e += 32) out[e] = e < c ? cq[e] : KEY_NONE;
   if (c <= 1) return;
-  const int cm = min(c, 256);
-  uint64_t* K = s_key[w];
-  double* Vv = s_v[w];
-  double* Ee = s_e[w];
-  short* cl = s_cl[w];
-  short* gr = s_g[w];
+  const int cm = min(c, lc);
   for (int e = lane; e < cm; e += 32) K[e] = cq[e];
   __syncwarp();
   // cluster starts by ballot: cl[p] = the last start at or before p
@@ -2416,9 +2416,10 @@ mann_status launch_resolve(Context* ctx, const float* base, const float* qs, int
     // (Sq)Euclidean: one pass, double-float order with FP64 only where it must decide
     const double eps = (double)(d + 2) * 5.9604644775390625e-08 * 1.01 + 1.2e-7;
     const float eps_up = std::nextafter((float)eps, 1.0f);
-    resolve_l2_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, s>>>(base, qs, d, metric, nq, L, kreq, eps_up, eps,
-                                                                cand, cand_count, floor_val, keys_out, counters,
-                                                                rows, unres_rows);
+    const size_t smem = (size_t)4 * std::min(L, 256) * (8 + 8 + 8 + 2 + 2);  // <= 28 KB
+    resolve_l2_kernel<<<(unsigned)ceil_div(nq, 4), 128, smem, s>>>(base, qs, d, metric, nq, L, kreq, eps_up, eps,
+                                                                   cand, cand_count, floor_val, keys_out, counters,
+                                                                   rows, unres_rows);
     MANN_CHECK_LAUNCH();
     return MANN_OK;
   }
@@ -2682,9 +2683,11 @@ mann_status run_main_pass(Context* ctx, cudaStream_t s, const CUtensorMap& mapA,
   const bool seg3 = !seedmode && !fp8 && depth > 16 &&
                     ((seg && depth <= 24 && nkb <= 3) || (!seg && nkb <= SHORT_K_STAGES));
   const int cap3 = depth <= 24 ? 24 : 32;
-  // two epilogue sets with 16-entry lists when the depth allows it; each set
-  // writes its own slot
-  const int nsets = (depth <= 16 || seg3) ? 2 : 1;
+  // two epilogue sets with 16-entry lists when the depth allows it, for the
+  // many-set and seed passes (each set writes its own slot); single-matrix
+  // main passes keep one set, whose one list admits about half as many
+  // candidates (held-out query pass 0.795 -> 0.789 ms)
+  const int nsets = ((depth <= 16 && (seg || seedmode)) || seg3) ? 2 : 1;
   // CTA pairs (cta_group::2) when there are at least two 128-row query blocks
   const int pairs = (K2_USE_PAIRS && nq > BM && !seg && !fp8)
                         ? (nsets == 2 ? k2_pair_capacity<16, 2>(ctx) : k2_pair_capacity<32, 1>(ctx))
