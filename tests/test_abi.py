@@ -27,6 +27,24 @@ def test_library_exports_every_declared_symbol():
     assert set(syms) <= set(_lib.SIGNATURES), set(syms) - set(_lib.SIGNATURES)
 
 
+def test_python_constants_match_the_header():
+    """Every MANN_METRIC_*, MANN_PREC_* and MANN_FLAG_* code the ctypes layer
+    names has the value include/mann.h defines."""
+    from manifoldann_gb300 import _lib
+
+    txt = (ROOT / "include" / "mann.h").read_text()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define MANN_([A-Z0-9_]+) (\d+)u?\b", txt)}
+    pairs = {"PREC_FP32": _lib.PREC_FP32, "PREC_BF16": _lib.PREC_BF16, "PREC_FP8": _lib.PREC_FP8,
+             "PREC_AUTO": _lib.PREC_AUTO, "PREC_FP16": _lib.PREC_FP16, "FLAG_FP64_TIES": _lib.FLAG_FP64_TIES,
+             "FLAG_TIME_KERNEL": _lib.FLAG_TIME_KERNEL, "FLAG_FP64_ERR": _lib.FLAG_FP64_ERR,
+             "METRIC_SQEUCLIDEAN": _lib.METRIC_SQEUCLIDEAN}
+    for name, value in pairs.items():
+        assert defs.get(name) == value, (name, defs.get(name), value)
+    from manifoldann_gb300.indices import PRECISIONS
+
+    assert PRECISIONS == {"fp32": 0, "bf16": 1, "fp8": 2, "auto": 3, "fp16": 4}
+
+
 def test_version_and_errors_without_gpu():
     from manifoldann_gb300 import _lib
 
