@@ -181,15 +181,31 @@ mann_status graph_impl(const mann_knn_params* p, const float* data, int64_t n, i
   return MANN_OK;
 }
 
+// Names the dataset handle of the current call to the tensor-core forms
+// (which keep the handle's prepared points between calls) while it lives.
+struct PointsOwnerScope {
+  Context* ctx;
+  PointsOwnerScope(Context* c, const void* owner, const float* base, uint64_t generation) : ctx(c) {
+    ctx->points_owner = owner;
+    ctx->points_base = base;
+    ctx->points_generation = generation;
+  }
+  ~PointsOwnerScope() {
+    ctx->points_owner = nullptr;
+    ctx->points_base = nullptr;
+  }
+};
+
 // the points of a dataset handle are device memory; queries and outputs are host
-mann_status knn_dataset_impl(const mann_knn_params* p, const float* dbase, int64_t n, const float* qs,
-                             int64_t q, int32_t d, int64_t graph_self, int kreq, int32_t* ids, float* dists,
-                             mann_knn_report* rep) {
+mann_status knn_dataset_impl(const mann_knn_params* p, const void* owner, uint64_t generation, const float* dbase,
+                             int64_t n, const float* qs, int64_t q, int32_t d, int64_t graph_self, int kreq,
+                             int32_t* ids, float* dists, mann_knn_report* rep) {
   const int kout = p->k;
   Context* ctx = nullptr;
   MANN_TRY(get_context(&ctx));
   cudaStream_t s = ctx->stream;
   CallScope scope(ctx, s);
+  PointsOwnerScope owner_scope(ctx, owner, dbase, generation);
   const int64_t rows = qs ? q : n;
   float *dq = nullptr, *dd = nullptr;
   int32_t* di = nullptr;
@@ -260,6 +276,7 @@ struct mann_dataset {
   int64_t n = 0, cap = 0;
   int32_t d = 0;
   int device = -1;
+  uint64_t generation = 0;  // bumped by every upload: prepared points of an older one are stale
 };
 
 namespace {
@@ -290,6 +307,7 @@ mann_status dataset_copy_in(mann_dataset* ds, const float* data, int64_t n) {
                                 ctx->stream));
   MANN_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   ds->n = n;
+  ++ds->generation;
   return MANN_OK;
 }
 
@@ -336,6 +354,13 @@ mann_status mann_dataset_destroy(mann_dataset* ds) {
     int prev = -1;
     (void)cudaGetDevice(&prev);
     if (prev != ds->device) (void)cudaSetDevice(ds->device);
+    Context* ctx = nullptr;
+    if (get_context(&ctx) == MANN_OK) {
+      CallScope scope(ctx, ctx->stream);
+      ctx->release_points(ds);  // the handle's prepared tensor-core operand
+    } else {
+      clear_error();
+    }
     (void)cudaFree(ds->dev);
     if (prev >= 0 && prev != ds->device) (void)cudaSetDevice(prev);
   }
@@ -354,7 +379,8 @@ mann_status mann_knn_dataset(const mann_knn_params* p, const mann_dataset* ds, c
   if (!queries || !out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
   MANN_TRY(dataset_device_check(ds));
   const int kreq = (int)std::min<int64_t>(p->k, ds->n);
-  return knn_dataset_impl(p, ds->dev, ds->n, queries, q, ds->d, -1, kreq, out_ids, out_dists, report);
+  return knn_dataset_impl(p, ds, ds->generation, ds->dev, ds->n, queries, q, ds->d, -1, kreq, out_ids, out_dists,
+                          report);
 }
 
 mann_status mann_knn_graph_dataset(const mann_knn_params* p, const mann_dataset* ds, int32_t include_self,
@@ -371,8 +397,8 @@ mann_status mann_knn_graph_dataset(const mann_knn_params* p, const mann_dataset*
   if (!out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
   MANN_TRY(dataset_device_check(ds));
   const int kreq = p->k + (include_self ? 0 : 1);
-  return knn_dataset_impl(p, ds->dev, n, nullptr, n, ds->d, include_self ? -1 : 0, kreq, out_ids, out_dists,
-                          report);
+  return knn_dataset_impl(p, ds, ds->generation, ds->dev, n, nullptr, n, ds->d, include_self ? -1 : 0, kreq,
+                          out_ids, out_dists, report);
 }
 
 mann_status mann_knn(const mann_knn_params* p, const float* base, int64_t n, const float* queries,

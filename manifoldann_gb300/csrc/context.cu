@@ -60,6 +60,14 @@ mann_status Context::scratch(int slot, size_t bytes, void** out) {
   return MANN_OK;
 }
 
+void Context::release_points(const void* owner) {
+  auto it = points_cache.find(owner);
+  if (it == points_cache.end()) return;
+  if (it->second.rows) (void)cudaFree(it->second.rows);
+  if (it->second.misc) (void)cudaFree(it->second.misc);
+  points_cache.erase(it);
+}
+
 mann_status get_context(Context** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -108,6 +108,22 @@ enum ScratchSlot : int {
   SLOT_COUNT
 };
 
+// Prepared tensor-core operand of a dataset handle's points, kept between
+// calls on the handle: the converted rows with their bound terms and norms
+// (`rows`), and the centre, scales, bounds and cosine row norms (`misc`).
+// `key` names the upload generation, metric and form it was prepared for
+// (0: empty); knn_bf16.cu fills and reads it, the handle's destruction frees it.
+struct PointsOperand {
+  uint64_t key = 0;
+  int64_t n = 0;
+  int d = 0;
+  void* rows = nullptr;
+  size_t rows_bytes = 0;
+  float* misc = nullptr;
+  size_t misc_bytes = 0;
+  int split = 0, f16 = 0, dp = 0, dpe = 0, width = 0, mainw = 0, augx = 0;
+};
+
 struct Context {
   int device = 0;
   int num_sms = 0;
@@ -126,6 +142,14 @@ struct Context {
   void time_end(cudaStream_t s);
   // autotune cache: shape class -> chosen configuration word
   std::unordered_map<uint64_t, uint64_t> tune;
+  // prepared points of dataset handles (by handle), and the handle, its
+  // points and upload generation during a call on a handle (owner NULL: none)
+  std::unordered_map<const void*, PointsOperand> points_cache;
+  const void* points_owner = nullptr;
+  const float* points_base = nullptr;
+  uint64_t points_generation = 0;
+  // frees a handle's prepared points (the handle is going away)
+  void release_points(const void* owner);
 
   // Device buffer of at least `bytes` for `slot`.  Grows by reallocation
   // (cudaFree synchronises the device, so no kernel still uses the old one).

@@ -2848,6 +2848,66 @@ struct Bf16Prep {
   int* fb_count = nullptr;
 };
 
+// Fills P's query-side operand (converting the queries unless they are the
+// points themselves in an unsplit form), the zeroed counters and the fields.
+static mann_status prep_finish(Context* ctx, cudaStream_t s, const float* mqs, int64_t nq, int d, bool self,
+                               const float* rn_q, const float* mu, float* scale, BaseMax* bmax, int split, bool f16,
+                               int dp, int dpe, int mainw, int augx, int width, const Bf16Operand& B,
+                               float* cos_bn, float* cos_qn, Bf16Prep* P) {
+  Bf16Operand Q;
+  if (self && !split) {
+    Q = B;
+  } else {
+    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * width, &Q.xb));
+    MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
+    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, augx, width, mu, scale, Q.xb,
+                                                                  Q.info, nullptr, nullptr, split, 0, f16 ? 1 : 0,
+                                                                  rn_q);
+    MANN_CHECK_LAUNCH();
+  }
+  unsigned long long* counters = nullptr;
+  MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
+  MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
+  P->B = B;
+  P->Q = Q;
+  P->split = split;
+  P->f16 = f16 ? 1 : 0;
+  P->dp = dp;
+  P->dpe = dpe;
+  P->width = width;
+  P->mainw = mainw;
+  P->augx = augx;
+  P->scale = scale;
+  P->bmax = bmax;
+  P->cos_bn = cos_bn;
+  P->cos_qn = cos_qn;
+  P->counters = counters;
+  P->err = reinterpret_cast<int*>(counters + 8);
+  P->fb_count = P->err + 1;
+  return MANN_OK;
+}
+
+// misc buffer of the prepared points: mu (d, padded to 32) | BaseMax | scale |
+// inexact | FP16 scale, 64 floats past mu; then the cosine row norms (n)
+static inline size_t misc_floats(int d, int64_t n, bool cosine) {
+  return (size_t)((d + 31) & ~31) + 64 + (cosine ? (size_t)n : 0);
+}
+
+// grows one cached device buffer (the old one is freed: cudaFree waits for the device)
+static bool cache_reserve(void** buf, size_t* have, size_t want) {
+  if (*buf && *have >= want) return true;
+  if (*buf) (void)cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  if (cudaMalloc(buf, want) != cudaSuccess) {
+    (void)cudaGetLastError();
+    *buf = nullptr;
+    return false;
+  }
+  *have = want;
+  return true;
+}
+
 mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_t n, const float* qs, int64_t nq,
                          int d, int metric, Bf16Prep* P, int form = FORM_BF16) {
   const bool fp8 = form == FORM_FP8;
@@ -2856,6 +2916,49 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const int dp = fp8 ? (d + 15) & ~15 : (d + 7) & ~7;
   const bool self = (qs == base);
   const bool cosine = metric == MANN_METRIC_COSINE;
+  const size_t mu_pad = (size_t)((d + 31) & ~31);
+
+  // ---- a dataset handle's points prepared by an earlier call with the same
+  // upload, metric and form: only the queries are prepared (no probe, no
+  // host synchronisation, no conversion of the points)
+  PointsOperand* pc = nullptr;
+  uint64_t pkey = 0;
+  if (!fp8 && ctx->points_owner && base == ctx->points_base) {
+    pc = &ctx->points_cache[ctx->points_owner];
+    pkey = (ctx->points_generation << 8) | ((uint64_t)metric << 4) | (uint64_t)form | (1ull << 63);
+  }
+  if (pc && pc->key == pkey && pc->n == n && pc->d == d) {
+    float* mu = pc->misc;
+    BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + mu_pad);
+    float* scale = reinterpret_cast<float*>(bmax + 1);
+    float* f16_scale = reinterpret_cast<float*>(reinterpret_cast<int*>(scale + 1) + 1);
+    float *cos_bn = nullptr, *cos_qn = nullptr;
+    const float* rn_q = nullptr;
+    if (cosine) {
+      cos_bn = mu + mu_pad + 64;
+      if (self) {
+        cos_qn = cos_bn;
+      } else {
+        MANN_TRY(ctx->scratch_t(SLOT_COS_NQ, (size_t)nq, &cos_qn));
+        MANN_TRY(launch_row_sqnorm(qs, nq, d, cos_qn, s));
+      }
+      rn_q = cos_qn;
+    }
+    Bf16Operand B;
+    B.xb = static_cast<__nv_bfloat16*>(pc->rows);
+    const size_t off_info = ((size_t)n * pc->width * 2 + 255) & ~(size_t)255;
+    B.info = reinterpret_cast<RowInfo*>(static_cast<char*>(pc->rows) + off_info);
+    B.norms = reinterpret_cast<float*>(static_cast<char*>(pc->rows) + off_info +
+                                       (((size_t)n * sizeof(RowInfo) + 255) & ~(size_t)255));
+    return prep_finish(ctx, s, qs, nq, d, self, rn_q, mu, pc->f16 ? f16_scale : scale, bmax, pc->split,
+                       pc->f16 != 0, pc->dp, pc->dpe, pc->mainw, pc->augx, pc->width, B, cos_bn, cos_qn, P);
+  }
+  if (pc) {
+    pc->key = 0;  // (re)prepared below
+    if (!cache_reserve(reinterpret_cast<void**>(&pc->misc), &pc->misc_bytes,
+                       sizeof(float) * misc_floats(d, n, cosine)))
+      pc = nullptr;  // no room to keep them: this call prepares into scratch
+  }
 
   // ---- cosine: the tensor-core passes run on unit-normalised rows
   // (1 - cos = ||q^ - p^||^2 / 2); the rerank uses the original rows.  The
@@ -2866,7 +2969,10 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   float *cos_bn = nullptr, *cos_qn = nullptr;
   const float *rn_b = nullptr, *rn_q = nullptr;
   if (cosine) {
-    MANN_TRY(ctx->scratch_t(SLOT_COS_NB, (size_t)n, &cos_bn));
+    if (pc)
+      cos_bn = pc->misc + mu_pad + 64;
+    else
+      MANN_TRY(ctx->scratch_t(SLOT_COS_NB, (size_t)n, &cos_bn));
     MANN_TRY(launch_row_sqnorm(base, n, d, cos_bn, s));
     if (self) {
       cos_qn = cos_bn;
@@ -2898,8 +3004,11 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   double* cpart = nullptr;
   float* mu = nullptr;
   MANN_TRY(ctx->scratch_t(SLOT_CENTRE, 64, &cpart));
-  MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));  // mu | BaseMax | scale
-  BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + ((d + 31) & ~31));
+  if (pc)
+    mu = pc->misc;
+  else
+    MANN_TRY(ctx->scratch_t(SLOT_MISC3, (size_t)d + 64, &mu));  // mu | BaseMax | scale
+  BaseMax* bmax = reinterpret_cast<BaseMax*>(mu + mu_pad);
   {
     const int64_t rows = std::min<int64_t>(n, CENTRE_ROWS);
     const int64_t stride = n / rows;
@@ -2930,9 +3039,10 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const int split = (h_inexact && form == FORM_BF16) ? 1 : 0;  // the FP8 and FP16 forms have no split
   if (f16) scale = f16_scale;  // the conversion and the certificate use the FP16 form's scale
   const int dpe = split ? 3 * dp : dp;  // columns of the tensor-core operands
-  Bf16Operand B, Q;
+  Bf16Operand B;
   if (fp8) {
     // E4M3 rows with per-row power-of-two scales (dp bytes per row), no norm fold
+    Bf16Operand Q;
     P->width = dp;
     P->mainw = dp;
     P->augx = 0;
@@ -2955,7 +3065,24 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
                                                                        Q.info, nullptr, nullptr);
       MANN_CHECK_LAUNCH();
     }
-  } else {
+    unsigned long long* counters = nullptr;
+    MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
+    MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
+    P->B = B;
+    P->Q = Q;
+    P->split = 0;
+    P->f16 = 0;
+    P->dp = dp;
+    P->dpe = dpe;
+    P->scale = scale;
+    P->bmax = bmax;
+    P->cos_bn = cos_bn;
+    P->cos_qn = cos_qn;
+    P->counters = counters;
+    P->err = reinterpret_cast<int*>(counters + 8);
+    P->fb_count = P->err + 1;
+    return MANN_OK;
+  }
   // rows: [main (dpe) | zeros up to augx | the first 16 norm-fold columns];
   // the fold's last 8 columns (zeros) lie past the row, where TMA fills zeros.
   // augx is mainw (dpe rounded up to 16) when the fold's 24 columns fit in
@@ -2964,43 +3091,36 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   const int mainw = (dpe + 15) & ~15;
   const int augx = (mainw % BK) + AUG <= BK ? mainw : (mainw + BK - 1) / BK * BK;  // fold inside one stage
   const int width = augx + 16;
-  MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * width, &B.xb));
-  MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
-  MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
+  const size_t off_info = ((size_t)n * width * 2 + 255) & ~(size_t)255;
+  const size_t off_norms = off_info + (((size_t)n * sizeof(RowInfo) + 255) & ~(size_t)255);
+  if (pc && !cache_reserve(&pc->rows, &pc->rows_bytes, off_norms + (size_t)n * sizeof(float))) pc = nullptr;
+  if (pc) {
+    B.xb = static_cast<__nv_bfloat16*>(pc->rows);
+    B.info = reinterpret_cast<RowInfo*>(static_cast<char*>(pc->rows) + off_info);
+    B.norms = reinterpret_cast<float*>(static_cast<char*>(pc->rows) + off_norms);
+  } else {
+    MANN_TRY(ctx->scratch_t(SLOT_BF16_B, (size_t)n * width, &B.xb));
+    MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_B, (size_t)n, &B.info));
+    MANN_TRY(ctx->scratch_t(SLOT_NORMS_B, (size_t)n, &B.norms));
+  }
   convert_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(mbase, n, d, dp, augx, width, mu, scale, B.xb,
                                                               B.info, B.norms, bmax, split, 1, f16 ? 1 : 0, rn_b);
   MANN_CHECK_LAUNCH();
-  if (self && !split) {
-    Q = B;
-  } else {
-    MANN_TRY(ctx->scratch_t(SLOT_BF16_Q, (size_t)nq * width, &Q.xb));
-    MANN_TRY(ctx->scratch_t(SLOT_ROWINFO_Q, (size_t)nq, &Q.info));
-    convert_rows_kernel<<<(unsigned)ceil_div(nq, 8), 256, 0, s>>>(mqs, nq, d, dp, augx, width, mu, scale, Q.xb,
-                                                                  Q.info, nullptr, nullptr, split, 0, f16 ? 1 : 0,
-                                                                  rn_q);
-    MANN_CHECK_LAUNCH();
+  if (pc) {
+    // the handle's points are prepared: later calls with this upload, metric and form reuse them
+    pc->n = n;
+    pc->d = d;
+    pc->split = split;
+    pc->f16 = f16 ? 1 : 0;
+    pc->dp = dp;
+    pc->dpe = dpe;
+    pc->width = width;
+    pc->mainw = mainw;
+    pc->augx = augx;
+    pc->key = pkey;
   }
-  P->width = width;
-  P->mainw = mainw;
-  P->augx = augx;
-  }
-  unsigned long long* counters = nullptr;
-  MANN_TRY(ctx->scratch_t(SLOT_COUNTERS, 64, &counters));
-  MANN_CUDA_TRY(cudaMemsetAsync(counters, 0, 64 * sizeof(unsigned long long), s));
-  P->B = B;
-  P->Q = Q;
-  P->split = split;
-  P->f16 = f16 ? 1 : 0;
-  P->dp = dp;
-  P->dpe = dpe;
-  P->scale = scale;
-  P->bmax = bmax;
-  P->cos_bn = cos_bn;
-  P->cos_qn = cos_qn;
-  P->counters = counters;
-  P->err = reinterpret_cast<int*>(counters + 8);
-  P->fb_count = P->err + 1;
-  return MANN_OK;
+  return prep_finish(ctx, s, mqs, nq, d, self, rn_q, mu, scale, bmax, split, f16, dp, dpe, mainw, augx, width, B,
+                     cos_bn, cos_qn, P);
 }
 
 // The autotuned admission depth (list entries a certificate may need) from

@@ -53,6 +53,46 @@ def test_dataset_upload_after_insert(gpu_lib, orc):
     ds.close()  # idempotent
 
 
+def test_prepared_points_follow_uploads_metrics_and_forms(gpu_lib, orc):
+    """A handle keeps its points' prepared tensor-core operand between calls:
+    repeated calls, other metrics and forms, graphs, a second handle in
+    between and a re-upload of the same size must all give the oracle's
+    answer (a stale operand would not)."""
+    import manifoldann_gb300 as M
+    from manifoldann_gb300 import synthetic
+
+    a = synthetic.anisotropic_clusters(8000, 128, seed=41, clusters=32)
+    b = synthetic.anisotropic_clusters(8000, 128, seed=42, clusters=32)  # same shape, other points
+    q = synthetic.anisotropic_clusters(250, 128, seed=43, clusters=32)
+    dists = {M_SQ: M.SqEuclidean(), M_EUC: M.Euclidean(), M_COS: M.CosineDist()}
+    ds = M.DeviceDataset(a.T)
+    other = M.DeviceDataset(b.T)
+    cur = a
+    steps = [(M_SQ, "bf16"), (M_SQ, "bf16"), (M_SQ, "fp16"), (M_COS, "fp16"), (M_SQ, "bf16"), ("other", None),
+             (M_SQ, "bf16"), ("upload", None), (M_SQ, "bf16"), (M_COS, "bf16"), ("graph", "fp16"), (M_EUC, "fp16")]
+    for metric, prec in steps:
+        if metric == "other":
+            idx = M.build_index(M.BruteForceIndex, b.T, distance=M.SqEuclidean())
+            ids, d = M.knn_arrays(idx, other, q.T, 10, precision="bf16")
+            ids_o, d_o = orc.knn_f32(b, q, 10, M_SQ)
+        elif metric == "upload":
+            ds.upload(b.T)
+            cur = b
+            continue
+        elif metric == "graph":
+            idx = M.build_index(M.BruteForceIndex, cur.T, distance=M.SqEuclidean())
+            ids, d = M.knn_graph_arrays(idx, ds, 8, precision=prec)
+            ids_o, d_o = orc.knn_graph_f32(cur, 8, M_SQ)
+        else:
+            idx = M.build_index(M.BruteForceIndex, cur.T, distance=dists[metric])
+            ids, d = M.knn_arrays(idx, ds, q.T, 10, precision=prec)
+            ids_o, d_o = orc.knn_f32(cur, q, 10, metric)
+        assert np.array_equal(ids, ids_o), (metric, prec)
+        assert same_bits(d, d_o), (metric, prec)
+    ds.close()
+    other.close()
+
+
 def test_dataset_argument_errors(gpu_lib):
     import ctypes as C
 
