@@ -133,7 +133,12 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
  * (src/indices/bruteforce.jl:82-95).  A handle belongs to the device that
  * was current at create; calls from another device fail with MANN_EINVAL_ARG.
  * Searches may share a handle across threads; an upload or destroy must not
- * overlap a search on the same handle (the handle has no lock). */
+ * overlap a search on the same handle (the handle has no lock).  The first
+ * BF16 / FP16 / AUTO search of an upload also keeps the points' prepared
+ * tensor-core operand on the device (about 2 bytes per value, three times
+ * that for data the BF16 form splits), which later searches of the same
+ * upload, metric and form reuse; the next upload or mann_dataset_destroy
+ * frees it. */
 typedef struct mann_dataset mann_dataset;
 /* data: host [n][d] FP32; copied to the device before the call returns. */
 mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_dataset** out);
