@@ -137,8 +137,8 @@ mann_status mann_knn_graph_device(const mann_knn_params* p, const float* data, i
  * BF16 / FP16 / AUTO search of an upload also keeps the points' prepared
  * tensor-core operand on the device (about 2 bytes per value, three times
  * that for data the BF16 form splits), which later searches of the same
- * upload, metric and form reuse; the next upload or mann_dataset_destroy
- * frees it. */
+ * upload, metric and form reuse; the next upload retires it (its memory is
+ * reused) and mann_dataset_destroy frees it. */
 typedef struct mann_dataset mann_dataset;
 /* data: host [n][d] FP32; copied to the device before the call returns. */
 mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_dataset** out);
