@@ -1,4 +1,5 @@
 // api.cu -- extern "C" entry points of libmanngpu (declared in include/mann.h).
+#include <atomic>
 #include <new>
 #include <string>
 
@@ -276,8 +277,15 @@ struct mann_dataset {
   int64_t n = 0, cap = 0;
   int32_t d = 0;
   int device = -1;
+  uint64_t serial = 0;      // never reused, unlike the handle's address
   uint64_t generation = 0;  // bumped by every upload: prepared points of an older one are stale
 };
+
+namespace {
+std::atomic<uint64_t> g_dataset_serial{0};
+// the name of a handle's current upload in the prepared-points cache
+uint64_t upload_name(const mann_dataset* ds) { return (ds->serial << 24) ^ ds->generation; }
+}  // namespace
 
 namespace {
 
@@ -324,6 +332,7 @@ mann_status mann_dataset_create(const float* data, int64_t n, int32_t d, mann_da
   auto* ds = new (std::nothrow) mann_dataset();
   if (!ds) return fail(MANN_ENOMEM, "dataset: host allocation failed");
   ds->d = d;
+  ds->serial = ++g_dataset_serial;
   if (cudaGetDevice(&ds->device) != cudaSuccess) {
     (void)cudaGetLastError();
     delete ds;
@@ -379,7 +388,7 @@ mann_status mann_knn_dataset(const mann_knn_params* p, const mann_dataset* ds, c
   if (!queries || !out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
   MANN_TRY(dataset_device_check(ds));
   const int kreq = (int)std::min<int64_t>(p->k, ds->n);
-  return knn_dataset_impl(p, ds, ds->generation, ds->dev, ds->n, queries, q, ds->d, -1, kreq, out_ids, out_dists,
+  return knn_dataset_impl(p, ds, upload_name(ds), ds->dev, ds->n, queries, q, ds->d, -1, kreq, out_ids, out_dists,
                           report);
 }
 
@@ -397,7 +406,7 @@ mann_status mann_knn_graph_dataset(const mann_knn_params* p, const mann_dataset*
   if (!out_ids || !out_dists) return fail(MANN_EINVAL_ARG, "NULL buffer");
   MANN_TRY(dataset_device_check(ds));
   const int kreq = p->k + (include_self ? 0 : 1);
-  return knn_dataset_impl(p, ds, ds->generation, ds->dev, n, nullptr, n, ds->d, include_self ? -1 : 0, kreq,
+  return knn_dataset_impl(p, ds, upload_name(ds), ds->dev, n, nullptr, n, ds->d, include_self ? -1 : 0, kreq,
                           out_ids, out_dists, report);
 }
 

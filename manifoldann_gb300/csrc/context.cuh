@@ -147,7 +147,7 @@ struct Context {
   std::unordered_map<const void*, PointsOperand> points_cache;
   const void* points_owner = nullptr;
   const float* points_base = nullptr;
-  uint64_t points_generation = 0;
+  uint64_t points_generation = 0;  // the handle's serial and upload generation
   // frees a handle's prepared points (the handle is going away)
   void release_points(const void* owner);
 

@@ -2925,6 +2925,7 @@ mann_status bf16_prepare(Context* ctx, cudaStream_t s, const float* base, int64_
   uint64_t pkey = 0;
   if (!fp8 && ctx->points_owner && base == ctx->points_base) {
     pc = &ctx->points_cache[ctx->points_owner];
+    // the upload's name (handle serial, generation), metric and form; never 0
     pkey = (ctx->points_generation << 8) | ((uint64_t)metric << 4) | (uint64_t)form | (1ull << 63);
   }
   if (pc && pc->key == pkey && pc->n == n && pc->d == d) {
